@@ -1,0 +1,363 @@
+"""Benchmark: adjoint gradients/s on one GB300 (forward sweep + backward sweep
+per instance), batched vs plain, at a stated error against FP64.
+
+Default workload: the Van der Pol batch (262,144 instances, mu = 10^U[-1,1],
+x0 ~ U[-2,2]^2, t in [0,20], DOPRI5, atol = rtol = 1e-6), the configuration
+the batched-vs-plain target is quoted on; seeded synthetic inputs.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config vdpb|dho|glv10|vdp1]
+                  [--precision mixed|fp64] [--impl ours|reference]
+
+One JSON line on rank 0.  `value` = gradients/s of va_gradient with inputs
+resident in HBM (CUDA events around each step, L2 flushed between steps);
+`e2e` = the same through va_gradient_host (host buffers, copies inside the
+timed region); `roofline` = the dominant sweep kernel's algorithmic FLOP rate
+against the FP64 FMA peak measured in the same run (cuBLAS DGEMM);
+`cpu_baseline` = the CPU port of the reference algorithm (oracle/) on the
+host cores, on a bounded sample.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic FLOPs (FMA = 2) per attempted forward step and per accepted
+# backward step: s_f C_f + 2N(nnz_a + nnz_b + nnz_e) + 6N + 30 and
+# s_f C_f + 2N nnz_a + s_f C_v + 2N (nnz_a + nnz_b) + N s_f.
+TAB_NNZ = {"dopri5": dict(s=6, a=15, b=5, e=6), "ck54": dict(s=6, a=15, b=4, e=5)}
+
+
+def model_cost(model, n):
+    if model in ("vdp", "vdp_petsc"):
+        return 5, 13
+    if model == "dho":
+        return 6, 12
+    if model in ("glv", "glv_shared"):
+        return 2 * n * n + 2 * n, 4 * n * n + 4 * n
+    return 2, 4
+
+
+def flops(model, tableau, n, attempts, accepted):
+    t = TAB_NNZ[tableau]
+    cf, cv = model_cost(model, n)
+    fwd = t["s"] * cf + 2 * n * (t["a"] + t["b"] + t["e"]) + 6 * n + 30
+    adj = t["s"] * cf + 2 * n * t["a"] + t["s"] * cv + 2 * n * (t["a"] + t["b"]) + n * t["s"]
+    return fwd * attempts, adj * accepted
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.p:
+            time.sleep(0.3)
+            self.p.terminate()
+            try:
+                out = self.p.communicate(timeout=5)[0]
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(cfg_name, w, seconds=10.0, threads=None):
+    """The oracle's multi-threaded batch gradient on a bounded sample."""
+    from oracle import oracle_py as O
+    c = w["cfg"]
+    threads = threads or os.cpu_count() or 1
+    pb = O.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"])
+    B = c["batch"]
+    pilot = min(B, 64 * threads)
+    t0 = time.perf_counter()
+    O.gradient_batch(pb, c["cost"], w["y0"][:pilot], w["params"][:pilot], w["t0"][:pilot], w["t1"][:pilot],
+                     nthreads=threads)
+    dt = time.perf_counter() - t0
+    m = int(min(B, max(pilot, pilot * seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    O.gradient_batch(pb, c["cost"], w["y0"][:m], w["params"][:m], w["t0"][:m], w["t1"][:m], nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": m / dt, "unit": "gradients/s", "cores": threads, "kind": "port",
+            "sample": f"first {m} of {B} instances of {cfg_name}, {dt:.1f} s on {threads} threads"}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference algorithm's CPU implementation on the host
+    cores.  The reference's own build needs AADC (x86-only binary) and Boost; on
+    this host the oracle port of the same algorithm stands in for it."""
+    from vectorizedadjoint_gb300 import workloads as W
+    if rank != 0:
+        return
+    w = W.make(args.config)
+    c = w["cfg"]
+    for _ in range(args.warmup):
+        cpu_baseline(args.config, w, seconds=1.0)
+    vals = []
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(args.config, w, seconds=max(1.0, 60.0 / max(args.steps, 1))))
+    v = float(np.mean([x["value"] for x in vals]))
+    cb = dict(vals[-1])
+    cb["value"] = v
+    print(json.dumps({
+        "impl": "reference", "metric": "adjoint gradients/s", "value": v, "unit": "gradients/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded PCG64)", "config": {"workload": args.config, "batch": c["batch"]},
+        "cpu_baseline": cb, "e2e": {"value": v, "unit": "gradients/s", "h2d_bytes_per_step": 0,
+                                    "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def fp64_peak_tflops(torch):
+    """FP64 peak of this GPU measured as cuBLAS DGEMM throughput (best of 5)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--config", default="vdpb")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    # a non-default stream, so va_gradient captures both sweeps in one CUDA graph
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        _bench(args, rank, world, local, torch, dist)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def _bench(args, rank, world, local, torch, dist):
+    from vectorizedadjoint_gb300 import Solver
+    from vectorizedadjoint_gb300 import workloads as W
+
+    w = W.make(args.config)
+    c = w["cfg"]
+    B = c["batch"]
+    dev = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")
+    y0, par, t0, t1 = dev(w["y0"]), dev(w["params"]), dev(w["t0"]), dev(w["t1"])
+    s = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision=args.precision,
+               atol=c["tol"], rtol=c["tol"], ckpt_budget_bytes=c.get("budget", 0))
+    s.autotune(c["cost"], y0, par, t0, t1)
+    out = s.gradient(c["cost"], y0, par, t0, t1)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        s.gradient(c["cost"], y0, par, t0, t1, out=out)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    times = []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.gradient(c["cost"], y0, par, t0, t1, out=out)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    ms = float(np.mean(times))
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    status = out["status"].cpu().numpy()
+    n_acc = out["n_acc"].cpu().numpy().astype(np.int64)
+    value = world * B / (ms * 1e-3)
+
+    # per-kernel timing (forward / backward launched separately) for the roofline
+    lam = None
+    fw_ms, bw_ms = [], []
+    for _ in range(3):
+        flush.zero_()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        f = s.forward(y0, par, t0, t1)
+        e1.record(stream)
+        if lam is None:
+            torch.cuda.synchronize()
+            if c["cost"] == "sumsq":
+                lam = (2.0 * f["yT"]).reshape(B, 1, c["n"]).contiguous()
+            else:
+                lam = torch.ones(B, 1, c["n"], dtype=torch.float64, device="cuda")
+            e1.record(stream)
+        bwo = s.backward(par, lam)
+        e2.record(stream)
+        e2.synchronize()
+        fw_ms.append(e0.elapsed_time(e1))
+        bw_ms.append(e1.elapsed_time(e2))
+    n_rej = f["n_rej"].cpu().numpy().astype(np.int64)
+    fl_f, fl_b = flops(c["model"], c["tableau"], c["n"], int((n_acc + n_rej).sum()), int(n_acc.sum()))
+    fms, bms = float(np.median(fw_ms)), float(np.median(bw_ms))
+    peak = fp64_peak_tflops(torch)
+    dom = ("forward", fl_f, fms) if fms >= bms else ("backward", fl_b, bms)
+    achieved = dom[1] / (dom[2] * 1e-3) / 1e12
+
+    # FP64 reference gradients on the same batch: error of this run against FP64
+    err = None
+    if args.precision == "mixed":
+        s64 = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision="fp64",
+                     atol=c["tol"], rtol=c["tol"], ckpt_budget_bytes=c.get("budget", 0))
+        o64 = s64.gradient(c["cost"], y0, par, t0, t1)
+        torch.cuda.synchronize()
+        t64 = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s64.gradient(c["cost"], y0, par, t0, t1, out=o64)
+            e1.record(stream)
+            e1.synchronize()
+            t64.append(e0.elapsed_time(e1))
+        g = torch.cat([out["dy0"], out["dp"]], 1)
+        g64 = torch.cat([o64["dy0"], o64["dp"]], 1)
+        rel = ((g - g64).abs().amax(1) / g64.abs().amax(1).clamp_min(1e-300)).cpu().numpy()
+        ok = (status == 0) & (o64["status"].cpu().numpy() == 0)
+        err = {"median": float(np.median(rel[ok])), "p99": float(np.quantile(rel[ok], 0.99)),
+               "max": float(rel[ok].max()), "vs": "FP64 path of this library (oracle-checked)"}
+        fp64_value = B / (float(np.median(t64)) * 1e-3)
+        s64.close()
+    else:
+        fp64_value = value
+
+    # plain drop-in: the FP64 path called once per instance through the host entry point
+    M = 64
+    s1 = Solver(c["model"], c["n"], c["npar"], 1, tableau=c["tableau"], precision="fp64",
+                atol=c["tol"], rtol=c["tol"])
+    s1.gradient_host(c["cost"], w["y0"][:1], w["params"][:1], w["t0"][:1], w["t1"][:1])
+    tp = time.perf_counter()
+    for b in range(M):
+        s1.gradient_host(c["cost"], w["y0"][b:b + 1], w["params"][b:b + 1], w["t0"][b:b + 1], w["t1"][b:b + 1])
+    plain = M / (time.perf_counter() - tp)
+    s1.close()
+
+    # e2e: host buffers (pinned) through va_gradient_host, copies inside the timed region
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    hy0, hpar, ht0, ht1 = pin(w["y0"]), pin(w["params"]), pin(w["t0"]), pin(w["t1"])
+    hout = dict(yT=torch.empty(B, c["n"], dtype=torch.float64).pin_memory(),
+                dy0=torch.empty(B, c["n"], dtype=torch.float64).pin_memory(),
+                dp=torch.empty(B, c["npar"], dtype=torch.float64).pin_memory(),
+                n_acc=torch.empty(B, dtype=torch.int32).pin_memory(),
+                status=torch.empty(B, dtype=torch.int32).pin_memory())
+    s.gradient_host(c["cost"], hy0, hpar, ht0, ht1, out=hout)
+    te = []
+    for _ in range(max(3, args.steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        tq = time.perf_counter()
+        s.gradient_host(c["cost"], hy0, hpar, ht0, ht1, out=hout)
+        te.append(time.perf_counter() - tq)
+    e2e = B / float(np.mean(te))
+    h2d = B * (c["n"] + c["npar"] + 2) * 8
+    d2h = B * (2 * c["n"] + c["npar"]) * 8 + 2 * B * 4
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(args.config, w)
+
+    if rank == 0:
+        line = {
+            "metric": "adjoint gradients/s", "value": value, "unit": "gradients/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 stages / f64 controller+accumulators" if args.precision == "mixed" else "f64",
+            "data": "synthetic (seeded PCG64)",
+            "config": {"workload": f"{args.config}: {c['model']} B={B} {c['tableau']} tol={c['tol']}",
+                       "batch": B, "precision": args.precision, "cost": c["cost"],
+                       "l2": "flushed between timed steps (256 MB write)",
+                       "launch": s.launch(), "status_ok": int((status == 0).sum())},
+            "e2e": {"value": e2e, "unit": "gradients/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": 2 * args.steps,
+            "roofline": {"bound": "fp64", "kernel": dom[0], "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak,
+                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 is absent from "
+                                        "the measured-peaks file)",
+                         "flops_per_launch": dom[1], "launch_ms": dom[2], "traffic": None,
+                         "forward_ms": fms, "backward_ms": bms},
+            "fp64_batched": fp64_value,
+            "plain_fp64_per_instance": plain,
+            "batched_vs_plain": value / plain,
+            "grad_err_vs_fp64": err,
+            "steps_per_instance": {"mean_accepted": float(n_acc.mean()), "max_accepted": int(n_acc.max()),
+                                   "mean_rejected": float(n_rej.mean())},
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,186 @@
+/*
+ * va.h -- C ABI of the GB300 discrete-adjoint library (libva_gb300.so).
+ *
+ * The reference exposes its solver as a C++ template API
+ * (lib/include/runge_kutta.hpp, lib/include/backpropagation.hpp,
+ * lib/include/Driver.hpp).  This header is the thin C layer under which the
+ * same operations run on one GPU.  Each entry point cites the reference
+ * interface it replaces.  Plain pointers and sizes only: no CUDA or C++
+ * types, so ctypes, cgo, JNI or any C FFI can bind it.
+ *
+ * Conventions
+ *  - A handle describes one batch of B independent instances of one model
+ *    (one ODE, parameters and horizon per instance).  It owns the device
+ *    checkpoint pool and scratch; the caller owns every input and output
+ *    buffer.
+ *  - Unless a name ends in _host, array arguments are DEVICE pointers in
+ *    row-major per-instance layout: y0[B][n], params[B][npar], t0[B], t1[B],
+ *    seeds lambdaT[B][nout][n], mu_direct[B][nout][npar].
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *  - Functions return va_status.  Per-instance outcomes go to status[B].
+ *  - A handle is not thread-safe; use one handle per host thread/stream.
+ */
+#ifndef VA_GB300_H
+#define VA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VA_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define VA_API __attribute__((visibility("default")))
+#else
+#define VA_API
+#endif
+
+typedef struct va_handle va_handle;
+
+/* Built-in right-hand sides (the reference records the user functor with
+ * AADC, lib/include/AadData.hpp:124-171; here each model ships a
+ * hand-written device RHS and vector-Jacobian product). */
+typedef enum {
+    VA_MODEL_VDP = 0,       /* x0'=x1, x1'=mu(1-x0^2)x1-x0;          n=2, npar=1        */
+    VA_MODEL_VDP_PETSC = 1, /* x0'=x1, x1'=mu((1-x0^2)x1-x0)  (examples/VanDerPol/main.cpp:41-42) */
+    VA_MODEL_DHO = 2,       /* x'=v, v'=-w^2 x-2 z w v, p=(w,z);     n=2, npar=2        */
+    VA_MODEL_GLV = 3,       /* x_i'=x_i(r_i+sum_j A_ij x_j), p=(r, A row-major)
+                               per instance (examples/GeneralizedLotkaVolterra/main.cpp:105-119);
+                               npar = n + n*n                                            */
+    VA_MODEL_DECAY = 4,     /* y'=-k y;                              n=1, npar=1        */
+    VA_MODEL_GLV_SHARED = 5 /* GLV with one A shared by the batch; per-instance
+                               params = r[n]; shared params = A[n][n]                   */
+} va_model;
+
+/* Embedded pairs (ButcherTable.hpp:259-308 for Cash-Karp; Dormand-Prince is
+ * added from the published tableau). */
+typedef enum { VA_TAB_DOPRI5 = 0, VA_TAB_CK54 = 1 } va_tableau;
+
+typedef enum {
+    VA_PREC_FP64 = 0, /* all arithmetic FP64: the drop-in path                          */
+    VA_PREC_MIXED = 1 /* FP32 stages and VJPs; FP64 t, h, y, error norm, controller and
+                         gradient accumulators                                           */
+} va_precision;
+
+typedef enum { VA_COST_SEEDS = -1, VA_COST_SUMSQ = 0, VA_COST_SUM = 1 } va_cost;
+
+typedef enum {
+    VA_OK = 0,
+    VA_MAX_REJECTS = 1,  /* odeint failed_step_checker: > max_rejects attempts on one step */
+    VA_MAX_STEPS = 2,    /* more than max_steps accepted steps                             */
+    VA_NONFINITE = 3,    /* NaN/Inf in the state, error norm or gradient                   */
+    VA_CKPT_BUDGET = 4,  /* checkpoint pool exhausted under the stated budget              */
+    VA_BAD_ARGS = 5,
+    VA_CUDA_ERROR = 6,
+    VA_NOT_READY = 7,    /* backward called before a forward                               */
+    VA_RECOMPUTE_MISMATCH = 8, /* two-level re-integration did not land on the checkpoint */
+    VA_NOT_RUN = 9
+} va_status;
+
+typedef struct {
+    int32_t model;  /* va_model                                                   */
+    int32_t n;      /* state dimension                                            */
+    int32_t npar;   /* per-instance parameter count                               */
+    int32_t batch;  /* B                                                          */
+    int32_t nout;   /* cost functions (seed rows) per instance, >= 1              */
+} va_problem;
+
+typedef struct {
+    int32_t tableau;     /* va_tableau                                            */
+    int32_t precision;   /* va_precision                                          */
+    double atol, rtol;   /* odeint make_controlled(abs, rel)                      */
+    double dt0;          /* initial step (runge_kutta(..., dt, ...))              */
+    int32_t max_steps;   /* accepted-step cap per instance                        */
+    int32_t max_rejects; /* odeint failed_step_checker limit (500)                */
+    int64_t ckpt_budget_bytes; /* HBM budget for checkpoints (0 = default 16 GiB) */
+    int32_t ckpt_stride; /* 0 = automatic; k > 1 stores every k-th accepted step
+                            and re-integrates segments during the backward sweep   */
+    int32_t block_size;  /* 0 = autotuned / default                               */
+    int32_t blocks_per_sm; /* 0 = occupancy limit                                 */
+    int32_t chunk_len;   /* records per checkpoint chunk (0 = 64)                 */
+    int32_t reserved[6];
+} va_options;
+
+/* Fills the reference's defaults: DOPRI5, FP64, atol=rtol=1e-6, dt0=1e-3,
+ * max_rejects=500 (odeint failed_step_checker), max_steps=1000000. */
+VA_API va_status va_default_options(va_options *opt);
+
+/* Replaces Driver(Nin, Nout, Npar) (Driver.hpp:39-42) together with
+ * constructDriverButcherTableau (Driver.hpp:87-93) and
+ * recordDriverRHSFunction (Driver.hpp:95-100): the model id stands for the
+ * recorded RHS, opt->tableau for the tableau. */
+VA_API va_status va_create(const va_problem *prob, const va_options *opt, va_handle **out);
+
+/* Replaces delete_driver_handle (Driver.hpp:81-85). */
+VA_API va_status va_destroy(va_handle *h);
+
+/* Forward sweep over all B instances; replaces the controlled overload of
+ * runge_kutta (runge_kutta.hpp:47-59 -> detail/runge_kutta.hpp:137-180).
+ * Writes y(T) (the reference overwrites x0), the accepted-step count
+ * (runge_kutta's return value), the rejected-attempt count and a status per
+ * instance; every accepted (t_n, y_n) goes to the handle's checkpoint pool.
+ * yT, n_acc, n_rej and status may be NULL. */
+VA_API va_status va_forward(va_handle *h, const double *y0, const double *params, const double *t0,
+                     const double *t1, double *yT, int32_t *n_acc, int32_t *n_rej,
+                     int32_t *status, void *stream);
+
+/* Backward sweep; replaces setCostGradients (Driver.hpp:103-114) plus
+ * adjointSolve (backpropagation.hpp:18-43 -> detail/backpropagation.hpp:280-348).
+ * lambdaT[B][nout][n] = dG/dy(T), mu_direct[B][nout][npar] = direct dG/dp
+ * (NULL = 0).  Outputs dy0[B][nout][n] (the reference's overwritten lambda)
+ * and dparams[B][nout][npar] = mu_direct + sum J_p^T Kbar (its accumulated
+ * mu).  params must be the ones the forward ran with.  Step sizes are frozen
+ * (h_n = t_{n+1} - t_n as in StateStorage.hpp:22). */
+VA_API va_status va_backward(va_handle *h, const double *params, const double *lambdaT,
+                      const double *mu_direct, double *dy0, double *dparams, int32_t *status,
+                      void *stream);
+
+/* Forward + backward for a built-in scalar cost (nout must be 1):
+ * VA_COST_SUMSQ g = sum_i y_i(T)^2, VA_COST_SUM g = sum_i y_i(T).  The two
+ * sweeps are captured in one CUDA graph on the first call and replayed. */
+VA_API va_status va_gradient(va_handle *h, int32_t cost, const double *y0, const double *params,
+                      const double *t0, const double *t1, double *yT, double *dy0,
+                      double *dparams, int32_t *n_acc, int32_t *status, void *stream);
+
+/* va_gradient with HOST buffers: copies inputs to the device, runs both
+ * sweeps and copies the results back, then synchronises `stream`.  Pinned
+ * host memory gives the fastest copies.  Any output may be NULL. */
+VA_API va_status va_gradient_host(va_handle *h, int32_t cost, const double *y0, const double *params,
+                           const double *t0, const double *t1, double *yT, double *dy0,
+                           double *dparams, int32_t *n_acc, int32_t *status, void *stream);
+
+/* Picks the block size and resident blocks per SM of both sweeps by timing
+ * candidate launches on the given inputs (device pointers); the choice is
+ * kept in the handle.  Runs forward+backward several times. */
+VA_API va_status va_autotune(va_handle *h, int32_t cost, const double *y0, const double *params,
+                      const double *t0, const double *t1, void *stream);
+
+/* Launch configuration in use: block size and grid of each sweep. */
+VA_API va_status va_get_launch(const va_handle *h, int32_t *fwd_block, int32_t *fwd_grid,
+                        int32_t *bwd_block, int32_t *bwd_grid);
+
+/* Checkpoint pool: bytes reserved, bytes used by the last forward, stride. */
+VA_API va_status va_checkpoint_info(const va_handle *h, int64_t *capacity_bytes, int64_t *used_bytes,
+                             int32_t *stride);
+
+/* Copies the accepted-step record of one instance from the checkpoint pool
+ * to HOST buffers (synchronous): t[k], dt[k] (trial step at the top of step
+ * k) and y[k][n] for k = 0..T, the reference's StateStorage contents
+ * (StateStorage.hpp:23-42).  *n_records = T + 1; at most `capacity` records
+ * are written.  Valid after a forward sweep with stride 1. */
+VA_API va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double *t,
+                               double *dt, double *y, int32_t *n_records);
+
+/* Message of the last failing call on this handle ("" if none). */
+VA_API const char *va_last_error(const va_handle *h);
+
+/* Name of a va_status value. */
+VA_API const char *va_status_string(int32_t status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,594 @@
+/*
+ * CPU oracle (test infrastructure only) -- see oracle.h for what it restates
+ * and where each part comes from in the reference.  Compiled with
+ * -ffp-contract=off so that every product and sum is rounded separately, in
+ * the operation order of the reference / Boost.odeint expressions.
+ */
+#include "oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define SMAX 8
+
+typedef struct {
+    int s;                 /* stages that feed y_{n+1}                        */
+    int fsal;              /* derivative at the new point is the next k_1     */
+    double a[SMAX][SMAX];  /* strictly lower triangular                       */
+    double b[SMAX];        /* higher-order weights                            */
+    double c[SMAX];
+    double e[SMAX];        /* error weights on k_1..k_s                       */
+    double e_new;          /* error weight on f(y_{n+1}) (FSAL stage)        */
+    int error_order;       /* odeint error_order_value                        */
+    int stepper_order;     /* odeint stepper_order_value                      */
+} tableau;
+
+/* Cash-Karp 5(4): Cash & Karp (1990), the coefficients the reference reads
+ * through odeint's rk54_ck_coefficients_* (ButcherTable.hpp:259-308). */
+static void tab_ck54(tableau *T)
+{
+    memset(T, 0, sizeof(*T));
+    T->s = 6;
+    T->fsal = 0;
+    T->a[1][0] = 1.0 / 5.0;
+    T->a[2][0] = 3.0 / 40.0;
+    T->a[2][1] = 9.0 / 40.0;
+    T->a[3][0] = 3.0 / 10.0;
+    T->a[3][1] = -9.0 / 10.0;
+    T->a[3][2] = 6.0 / 5.0;
+    T->a[4][0] = -11.0 / 54.0;
+    T->a[4][1] = 5.0 / 2.0;
+    T->a[4][2] = -70.0 / 27.0;
+    T->a[4][3] = 35.0 / 27.0;
+    T->a[5][0] = 1631.0 / 55296.0;
+    T->a[5][1] = 175.0 / 512.0;
+    T->a[5][2] = 575.0 / 13824.0;
+    T->a[5][3] = 44275.0 / 110592.0;
+    T->a[5][4] = 253.0 / 4096.0;
+    T->b[0] = 37.0 / 378.0;
+    T->b[1] = 0.0;
+    T->b[2] = 250.0 / 621.0;
+    T->b[3] = 125.0 / 594.0;
+    T->b[4] = 0.0;
+    T->b[5] = 512.0 / 1771.0;
+    T->c[0] = 0.0;
+    T->c[1] = 1.0 / 5.0;
+    T->c[2] = 3.0 / 10.0;
+    T->c[3] = 3.0 / 5.0;
+    T->c[4] = 1.0;
+    T->c[5] = 7.0 / 8.0;
+    /* b - b_hat, each difference of two rounded quotients */
+    T->e[0] = 37.0 / 378.0 - 2825.0 / 27648.0;
+    T->e[1] = 0.0;
+    T->e[2] = 250.0 / 621.0 - 18575.0 / 48384.0;
+    T->e[3] = 125.0 / 594.0 - 13525.0 / 55296.0;
+    T->e[4] = -277.0 / 14336.0;
+    T->e[5] = 512.0 / 1771.0 - 1.0 / 4.0;
+    T->e_new = 0.0;
+    T->error_order = 4;
+    T->stepper_order = 5;
+}
+
+/* Dormand-Prince 5(4): Dormand & Prince (1980).  Seven stages, the seventh
+ * (b_7 = 0) is f(y_{n+1}) and is reused as the next step's first stage. */
+static void tab_dopri5(tableau *T)
+{
+    memset(T, 0, sizeof(*T));
+    T->s = 6;
+    T->fsal = 1;
+    T->a[1][0] = 1.0 / 5.0;
+    T->a[2][0] = 3.0 / 40.0;
+    T->a[2][1] = 9.0 / 40.0;
+    T->a[3][0] = 44.0 / 45.0;
+    T->a[3][1] = -56.0 / 15.0;
+    T->a[3][2] = 32.0 / 9.0;
+    T->a[4][0] = 19372.0 / 6561.0;
+    T->a[4][1] = -25360.0 / 2187.0;
+    T->a[4][2] = 64448.0 / 6561.0;
+    T->a[4][3] = -212.0 / 729.0;
+    T->a[5][0] = 9017.0 / 3168.0;
+    T->a[5][1] = -355.0 / 33.0;
+    T->a[5][2] = 46732.0 / 5247.0;
+    T->a[5][3] = 49.0 / 176.0;
+    T->a[5][4] = -5103.0 / 18656.0;
+    T->b[0] = 35.0 / 384.0;
+    T->b[1] = 0.0;
+    T->b[2] = 500.0 / 1113.0;
+    T->b[3] = 125.0 / 192.0;
+    T->b[4] = -2187.0 / 6784.0;
+    T->b[5] = 11.0 / 84.0;
+    T->c[0] = 0.0;
+    T->c[1] = 1.0 / 5.0;
+    T->c[2] = 3.0 / 10.0;
+    T->c[3] = 4.0 / 5.0;
+    T->c[4] = 8.0 / 9.0;
+    T->c[5] = 1.0;
+    T->e[0] = 35.0 / 384.0 - 5179.0 / 57600.0;
+    T->e[1] = 0.0;
+    T->e[2] = 500.0 / 1113.0 - 7571.0 / 16695.0;
+    T->e[3] = 125.0 / 192.0 - 393.0 / 640.0;
+    T->e[4] = -2187.0 / 6784.0 - -92097.0 / 339200.0;
+    T->e[5] = 11.0 / 84.0 - 187.0 / 2100.0;
+    T->e_new = -1.0 / 40.0;
+    T->error_order = 4;
+    T->stepper_order = 5;
+}
+
+static int get_tableau(int id, tableau *T)
+{
+    if (id == ORC_TAB_DOPRI5) {
+        tab_dopri5(T);
+        return 0;
+    }
+    if (id == ORC_TAB_CK54) {
+        tab_ck54(T);
+        return 0;
+    }
+    return -1;
+}
+
+/* ------------------------------------------------------------------ models */
+
+void orc_rhs(const orc_problem *pb, const double *x, const double *p, double t, double *f)
+{
+    (void)t;
+    int n = pb->n;
+    switch (pb->model) {
+    case ORC_MODEL_VDP:
+        f[0] = x[1];
+        f[1] = p[0] * (1.0 - x[0] * x[0]) * x[1] - x[0];
+        break;
+    case ORC_MODEL_VDP_PETSC: /* examples/VanDerPol/main.cpp:41-42 */
+        f[0] = x[1];
+        f[1] = p[0] * ((1.0 - x[0] * x[0]) * x[1] - x[0]);
+        break;
+    case ORC_MODEL_DHO:
+        f[0] = x[1];
+        f[1] = -p[0] * p[0] * x[0] - 2.0 * p[1] * p[0] * x[1];
+        break;
+    case ORC_MODEL_GLV: /* examples/GeneralizedLotkaVolterra/main.cpp:109-118 */
+        for (int i = 0; i < n; i++) {
+            double sum = 0.0;
+            for (int j = 0; j < n; j++)
+                sum += p[n * (i + 1) + j] * x[j];
+            f[i] = x[i] * (p[i] + sum);
+        }
+        break;
+    case ORC_MODEL_DECAY:
+        for (int i = 0; i < n; i++)
+            f[i] = -p[i] * x[i];
+        break;
+    }
+}
+
+/* gx = J_x^T w, gp = J_p^T w (overwritten, not accumulated). */
+void orc_vjp(const orc_problem *pb, const double *w, const double *x, const double *p, double t,
+             double *gx, double *gp)
+{
+    (void)t;
+    int n = pb->n;
+    switch (pb->model) {
+    case ORC_MODEL_VDP: {
+        double mu = p[0];
+        gx[0] = w[1] * (-2.0 * mu * x[0] * x[1] - 1.0);
+        gx[1] = w[0] + w[1] * (mu * (1.0 - x[0] * x[0]));
+        gp[0] = w[1] * ((1.0 - x[0] * x[0]) * x[1]);
+        break;
+    }
+    case ORC_MODEL_VDP_PETSC: {
+        double mu = p[0];
+        gx[0] = w[1] * (mu * (-2.0 * x[0] * x[1] - 1.0));
+        gx[1] = w[0] + w[1] * (mu * (1.0 - x[0] * x[0]));
+        gp[0] = w[1] * ((1.0 - x[0] * x[0]) * x[1] - x[0]);
+        break;
+    }
+    case ORC_MODEL_DHO: {
+        double om = p[0], ze = p[1];
+        gx[0] = w[1] * (-om * om);
+        gx[1] = w[0] + w[1] * (-2.0 * ze * om);
+        gp[0] = w[1] * (-2.0 * om * x[0] - 2.0 * ze * x[1]);
+        gp[1] = w[1] * (-2.0 * om * x[1]);
+        break;
+    }
+    case ORC_MODEL_GLV: {
+        /* f_i = x_i s_i,  s_i = r_i + sum_j A_ij x_j
+         * gx_k = w_k s_k + sum_i A_ik w_i x_i ; gr_i = w_i x_i ; gA_ij = w_i x_i x_j */
+        for (int k = 0; k < n; k++) {
+            double sum = 0.0;
+            for (int j = 0; j < n; j++)
+                sum += p[n * (k + 1) + j] * x[j];
+            gx[k] = w[k] * (p[k] + sum);
+        }
+        for (int i = 0; i < n; i++) {
+            double v = w[i] * x[i];
+            gp[i] = v;
+            for (int k = 0; k < n; k++) {
+                gx[k] += p[n * (i + 1) + k] * v;
+                gp[n * (i + 1) + k] = v * x[k];
+            }
+        }
+        break;
+    }
+    case ORC_MODEL_DECAY:
+        for (int i = 0; i < n; i++) {
+            gx[i] = -p[i] * w[i];
+            gp[i] = -x[i] * w[i];
+        }
+        break;
+    }
+}
+
+/* ------------------------------------------------------------- controller */
+
+/* odeint detail::less_with_sign for dt > 0: t2 - t1 > epsilon */
+static int less_with_sign(double t1, double t2) { return t2 - t1 > DBL_EPSILON; }
+
+/* One odeint error-stepper step from (x, dxdt, t) with step dt.  Writes the
+ * new state, the derivative at the new point (FSAL tableaux only) and the
+ * error vector.  K[0] must hold dxdt on entry. */
+static void rk_error_step(const orc_problem *pb, const tableau *T, const double *x, double t,
+                          double dt, const double *p, double K[SMAX][64], double *out,
+                          double *dxdt_new, double *xerr, double *xtmp)
+{
+    int n = pb->n;
+    for (int m = 1; m < T->s; m++) {
+        for (int i = 0; i < n; i++) {
+            double acc = x[i];
+            for (int j = 0; j < m; j++)
+                acc = acc + (T->a[m][j] * dt) * K[j][i];
+            xtmp[i] = acc;
+        }
+        orc_rhs(pb, xtmp, p, t + T->c[m] * dt, K[m]);
+    }
+    for (int i = 0; i < n; i++) {
+        double acc = x[i];
+        for (int j = 0; j < T->s; j++)
+            if (T->b[j] != 0.0)
+                acc = acc + (T->b[j] * dt) * K[j][i];
+        out[i] = acc;
+    }
+    if (T->fsal)
+        orc_rhs(pb, out, p, t + dt, dxdt_new);
+    for (int i = 0; i < n; i++) {
+        double acc = 0.0;
+        int first = 1;
+        for (int j = 0; j < T->s; j++) {
+            if (T->e[j] == 0.0)
+                continue; /* an exact zero term leaves the sum unchanged */
+            double term = (T->e[j] * dt) * K[j][i];
+            acc = first ? term : acc + term;
+            first = 0;
+        }
+        if (T->fsal)
+            acc = acc + (T->e_new * dt) * dxdt_new[i];
+        xerr[i] = acc;
+    }
+}
+
+/* default_error_checker::error with a_x = a_dxdt = 1: max-norm of
+ * |err_i| / (atol + rtol (|x_i| + |dt| |dxdt_i|)) at the step start. */
+static double error_norm(const orc_problem *pb, const double *x, const double *dxdt,
+                         const double *xerr, double dt)
+{
+    double m = 0.0;
+    double adt = fabs(dt);
+    for (int i = 0; i < pb->n; i++) {
+        double r = fabs(xerr[i]) / (pb->atol + pb->rtol * (1.0 * fabs(x[i]) + adt * fabs(dxdt[i])));
+        if (isnan(r))
+            return r;
+        if (r > m)
+            m = r;
+    }
+    return m;
+}
+
+/* default_step_adjuster::decrease_step / increase_step */
+static double decrease_step(double dt, double err, int error_order)
+{
+    double f = 9.0 / 10.0 * pow(err, -1.0 / (error_order - 1));
+    double lo = 1.0 / 5.0;
+    return dt * (f > lo ? f : lo);
+}
+
+static double increase_step(double dt, double err, int stepper_order)
+{
+    if (err < 0.5) {
+        double floor_ = pow(5.0, -(double)stepper_order);
+        if (err < floor_)
+            err = floor_;
+        dt *= 9.0 / 10.0 * pow(err, -1.0 / stepper_order);
+    }
+    return dt;
+}
+
+int orc_forward(const orc_problem *pb, const double *y0, const double *p, double t0, double t1,
+                long cap, double *times, double *states, double *dt_trial, double *yT,
+                long *n_acc, long *n_rej)
+{
+    tableau T;
+    int n = pb->n;
+    if (n < 1 || n > 64 || get_tableau(pb->tableau, &T) != 0)
+        return ORC_BAD_ARGS;
+    double y[64], dxdt[64], dxdt_new[64], out[64], xerr[64], xtmp[64];
+    double K[SMAX][64];
+    memcpy(y, y0, sizeof(double) * n);
+    double t = t0, dt = pb->dt0;
+    long count = 0, rej = 0;
+    int status = ORC_OK;
+    int first_call = 1;
+    int max_fail = pb->max_fail > 0 ? pb->max_fail : 500;
+
+    while (less_with_sign(t, t1)) {
+        if (count >= cap) {
+            status = ORC_MAX_STEPS;
+            break;
+        }
+        times[count] = t;
+        memcpy(states + (size_t)count * n, y, sizeof(double) * n);
+        if (dt_trial)
+            dt_trial[count] = dt;
+        if (less_with_sign(t1, t + dt))
+            dt = t1 - t;
+        int fails = 0;
+        for (;;) {
+            /* try_step: CK54 recomputes dxdt on every attempt; DOPRI5
+             * computes it on the first call and then carries it (FSAL). */
+            if (!T.fsal || first_call) {
+                orc_rhs(pb, y, p, t, dxdt);
+                first_call = 0;
+            }
+            memcpy(K[0], dxdt, sizeof(double) * n);
+            rk_error_step(pb, &T, y, t, dt, p, K, out, dxdt_new, xerr, xtmp);
+            double err = error_norm(pb, y, dxdt, xerr, dt);
+            int ok;
+            if (isnan(err)) {
+                status = ORC_NONFINITE;
+                break;
+            }
+            if (err > 1.0) {
+                dt = decrease_step(dt, err, T.error_order);
+                ok = 0;
+                rej++;
+            } else {
+                t += dt;
+                dt = increase_step(dt, err, T.stepper_order);
+                memcpy(y, out, sizeof(double) * n);
+                if (T.fsal)
+                    memcpy(dxdt, dxdt_new, sizeof(double) * n);
+                ok = 1;
+            }
+            /* failed_step_checker::operator(): throws once m_steps reaches max */
+            if (fails >= max_fail) {
+                status = ORC_MAX_REJECTS;
+                break;
+            }
+            fails++;
+            if (ok)
+                break;
+            if (!isfinite(dt) || dt == 0.0) {
+                status = ORC_NONFINITE;
+                break;
+            }
+        }
+        if (status != ORC_OK)
+            break;
+        count++;
+    }
+    if (status == ORC_OK) {
+        times[count] = t;
+        memcpy(states + (size_t)count * n, y, sizeof(double) * n);
+        for (int i = 0; i < n; i++)
+            if (!isfinite(y[i]))
+                status = ORC_NONFINITE;
+    }
+    if (yT)
+        memcpy(yT, y, sizeof(double) * n);
+    if (n_acc)
+        *n_acc = count;
+    if (n_rej)
+        *n_rej = rej;
+    return status;
+}
+
+void orc_forward_frozen(const orc_problem *pb, const double *y0, const double *p, long T,
+                        const double *times, double *yT)
+{
+    tableau tab;
+    int n = pb->n;
+    get_tableau(pb->tableau, &tab);
+    double y[64], xtmp[64], K[SMAX][64];
+    memcpy(y, y0, sizeof(double) * n);
+    for (long k = 0; k < T; k++) {
+        double t = times[k], h = times[k + 1] - times[k];
+        orc_rhs(pb, y, p, t, K[0]);
+        for (int m = 1; m < tab.s; m++) {
+            for (int i = 0; i < n; i++) {
+                double acc = y[i];
+                for (int j = 0; j < m; j++)
+                    acc = acc + (tab.a[m][j] * h) * K[j][i];
+                xtmp[i] = acc;
+            }
+            orc_rhs(pb, xtmp, p, t + tab.c[m] * h, K[m]);
+        }
+        for (int i = 0; i < n; i++) {
+            double acc = y[i];
+            for (int j = 0; j < tab.s; j++)
+                if (tab.b[j] != 0.0)
+                    acc = acc + (tab.b[j] * h) * K[j][i];
+            y[i] = acc;
+        }
+    }
+    memcpy(yT, y, sizeof(double) * n);
+}
+
+/* ---------------------------------------------------------------- adjoint */
+
+/* back_prop_step (detail/backpropagation.hpp:160-229) for one seed. */
+static void back_prop_step(const orc_problem *pb, const tableau *T, const double *p, double tn,
+                           double h, const double *u, double *lam, double *alphabar,
+                           double *K /* [s][n] */, double *X /* [s][n] */, double *Kbar /* [s][n] */,
+                           double *ybar, double *gx, double *gp)
+{
+    int n = pb->n, s = T->s, np = pb->npar;
+    /* compute_intermediate_states (:24-64): X_m = u + sum_{j<m} (h a_mj) K_j */
+    for (int m = 0; m < s; m++) {
+        for (int i = 0; i < n; i++) {
+            double acc = u[i];
+            for (int j = 0; j < m; j++)
+                acc += h * T->a[m][j] * K[j * n + i];
+            X[m * n + i] = acc;
+        }
+        orc_rhs(pb, X + m * n, p, tn + T->c[m] * h, K + m * n);
+    }
+    /* step s+1 (:178-184): ybar = lambda, Kbar_m = b_m h lambda */
+    for (int i = 0; i < n; i++) {
+        ybar[i] = 0.0 + lam[i];
+        for (int m = 0; m < s; m++)
+            Kbar[m * n + i] = 0.0 + T->b[m] * h * lam[i];
+    }
+    /* steps s..1 (:196-224) */
+    for (int m = s - 1; m >= 0; m--) {
+        orc_vjp(pb, Kbar + m * n, X + m * n, p, tn + T->c[m] * h, gx, gp);
+        for (int i = 0; i < n; i++) {
+            ybar[i] += gx[i];
+            for (int k = 0; k < m; k++)
+                Kbar[k * n + i] += gx[i] * T->a[m][k] * h;
+        }
+        for (int k = 0; k < np; k++)
+            alphabar[k] += gp[k];
+    }
+    for (int i = 0; i < n; i++)
+        lam[i] = ybar[i];
+}
+
+int orc_adjoint(const orc_problem *pb, const double *p, long T, const double *times,
+                const double *states, int nout, double *lambda, double *mu)
+{
+    tableau tab;
+    if (get_tableau(pb->tableau, &tab) != 0 || pb->n < 1 || pb->n > 64 || nout < 1)
+        return ORC_BAD_ARGS;
+    int n = pb->n, np = pb->npar, s = tab.s;
+    double *work = (double *)malloc(sizeof(double) * ((size_t)4 * s * n + 2 * n + 2 * (size_t)np));
+    if (!work)
+        return ORC_BAD_ARGS;
+    double *K = work, *X = K + s * n, *Kbar = X + s * n, *ybar = Kbar + s * n;
+    double *gx = ybar + n, *gp = gx + n, *alphabar = gp + np;
+    int status = ORC_OK;
+    for (int q = 0; q < nout; q++) {
+        double *lam = lambda + (size_t)q * n;
+        for (int k = 0; k < np; k++)
+            alphabar[k] = 0.0;
+        /* back_prop (:256-278): n = T-1 .. 0 */
+        for (long k = T - 1; k >= 0; k--) {
+            double tn = times[k];
+            double h = times[k + 1] - times[k];
+            back_prop_step(pb, &tab, p, tn, h, states + (size_t)k * n, lam, alphabar, K, X, Kbar,
+                           ybar, gx, gp);
+        }
+        /* write-back (:317-321): mu += alphabar */
+        for (int k = 0; k < np; k++)
+            mu[(size_t)q * np + k] += alphabar[k];
+        for (int i = 0; i < n; i++)
+            if (!isfinite(lam[i]))
+                status = ORC_NONFINITE;
+    }
+    free(work);
+    return status;
+}
+
+/* --------------------------------------------------------------- gradient */
+
+int orc_gradient(const orc_problem *pb, int cost, const double *y0, const double *p, double t0,
+                 double t1, double *yT, double *dy0, double *dp, long *n_acc, long *n_rej)
+{
+    int n = pb->n;
+    long cap = pb->max_steps > 0 ? pb->max_steps : 100000;
+    double *times = (double *)malloc(sizeof(double) * (size_t)(cap + 1));
+    double *states = (double *)malloc(sizeof(double) * (size_t)(cap + 1) * n);
+    if (!times || !states) {
+        free(times);
+        free(states);
+        return ORC_BAD_ARGS;
+    }
+    double yT_local[64];
+    long T = 0;
+    int st = orc_forward(pb, y0, p, t0, t1, cap, times, states, NULL, yT_local, &T, n_rej);
+    if (yT)
+        memcpy(yT, yT_local, sizeof(double) * n);
+    if (n_acc)
+        *n_acc = T;
+    if (st == ORC_OK) {
+        for (int i = 0; i < n; i++)
+            dy0[i] = cost == ORC_COST_SUMSQ ? 2.0 * yT_local[i] : 1.0;
+        for (int k = 0; k < pb->npar; k++)
+            dp[k] = 0.0;
+        st = orc_adjoint(pb, p, T, times, states, 1, dy0, dp);
+    }
+    free(times);
+    free(states);
+    return st;
+}
+
+typedef struct {
+    const orc_problem *pb;
+    int cost;
+    long lo, hi;
+    const double *y0, *p, *t0, *t1;
+    double *yT, *dy0, *dp;
+    long *n_acc, *n_rej;
+    int *status;
+} batch_job;
+
+static void *batch_worker(void *arg)
+{
+    batch_job *J = (batch_job *)arg;
+    int n = J->pb->n, np = J->pb->npar;
+    for (long b = J->lo; b < J->hi; b++) {
+        long na = 0, nr = 0;
+        int st = orc_gradient(J->pb, J->cost, J->y0 + b * n, J->p + b * np, J->t0[b], J->t1[b],
+                              J->yT ? J->yT + b * n : NULL, J->dy0 + b * n, J->dp + b * np, &na,
+                              &nr);
+        if (J->n_acc)
+            J->n_acc[b] = na;
+        if (J->n_rej)
+            J->n_rej[b] = nr;
+        if (J->status)
+            J->status[b] = st;
+    }
+    return NULL;
+}
+
+int orc_gradient_batch(const orc_problem *pb, int cost, long B, const double *y0, const double *p,
+                       const double *t0, const double *t1, int nthreads, double *yT, double *dy0,
+                       double *dp, long *n_acc, long *n_rej, int *status)
+{
+    if (nthreads < 1)
+        nthreads = 1;
+    if (nthreads > 256)
+        nthreads = 256;
+    pthread_t th[256];
+    int created[256];
+    batch_job jobs[256];
+    long per = (B + nthreads - 1) / nthreads;
+    for (int k = 0; k < nthreads; k++) {
+        long lo = k * per, hi = lo + per < B ? lo + per : B;
+        batch_job J = {pb, cost, lo, lo < hi ? hi : lo, y0, p, t0, t1, yT, dy0, dp, n_acc, n_rej, status};
+        jobs[k] = J;
+        created[k] = 0;
+    }
+    for (int k = 0; k < nthreads; k++) {
+        if (jobs[k].lo >= jobs[k].hi)
+            continue;
+        if (pthread_create(&th[k], NULL, batch_worker, &jobs[k]) == 0)
+            created[k] = 1;
+        else
+            batch_worker(&jobs[k]);
+    }
+    for (int k = 0; k < nthreads; k++)
+        if (created[k])
+            pthread_join(th[k], NULL);
+    return ORC_OK;
+}

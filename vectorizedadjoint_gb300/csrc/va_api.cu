@@ -1,0 +1,660 @@
+// C ABI of the discrete-adjoint library (include/va.h): handle, checkpoint
+// pool, launch configuration, CUDA-graph capture of forward+backward and the
+// host-buffer entry point.  Replaces the reference's Driver
+// (lib/include/Driver.hpp), runge_kutta (lib/include/runge_kutta.hpp) and
+// adjointSolve (lib/include/backpropagation.hpp) for built-in models.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/va.h"
+#include "va_kernels.cuh"
+#include "va_registry.h"
+
+namespace {
+
+constexpr int64_t kDefaultBudget = 16LL << 30; // 16 GiB of checkpoints
+
+struct GraphKey {
+    int cost = -2;
+    const void *ptrs[10] = {};
+    void *stream = nullptr;
+    bool operator==(const GraphKey &o) const
+    {
+        if (cost != o.cost || stream != o.stream)
+            return false;
+        for (int i = 0; i < 10; i++)
+            if (ptrs[i] != o.ptrs[i])
+                return false;
+        return true;
+    }
+};
+
+} // namespace
+
+struct va_handle {
+    va_problem prob{};
+    va_options opt{};
+    int device = 0;
+    int sm_count = 0;
+    const va::KernelSet *ks = nullptr;
+    int N = 0, P = 0, RS = 0;
+
+    // checkpoint pool and per-instance metadata
+    double *pool_rec = nullptr;
+    int *chunk_prev = nullptr;
+    int n_chunks = 0;
+    int chunk_len = 64;
+    int *inst_T = nullptr, *inst_last = nullptr, *inst_status = nullptr;
+    va::Control *ctl = nullptr;
+
+    // staging buffers of the host entry point
+    double *s_y0 = nullptr, *s_par = nullptr, *s_t0 = nullptr, *s_t1 = nullptr;
+    double *s_yT = nullptr, *s_dy0 = nullptr, *s_dpar = nullptr;
+    int *s_nacc = nullptr, *s_status = nullptr;
+
+    int fwd_block = 128, fwd_grid = 0, bwd_block = 128, bwd_grid = 0;
+    bool forward_done = false;
+    std::string err;
+
+    cudaGraphExec_t graph = nullptr;
+    GraphKey graph_key;
+};
+
+namespace {
+
+va_status fail(va_handle *h, va_status st, const char *fmt, const char *detail = "")
+{
+    if (h) {
+        char buf[512];
+        std::snprintf(buf, sizeof(buf), fmt, detail);
+        h->err = buf;
+    }
+    return st;
+}
+
+va_status cuda_fail(va_handle *h, cudaError_t e, const char *where)
+{
+    if (h) {
+        h->err = std::string(where) + ": " + cudaGetErrorString(e);
+    }
+    return VA_CUDA_ERROR;
+}
+
+#define VA_CUDA(h, call)                                                                           \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return cuda_fail((h), e_, #call);                                                      \
+    } while (0)
+
+const va::KernelSet *kernel_set(const va_problem &p)
+{
+    switch (p.model) {
+    case VA_MODEL_VDP:
+        return va::kernels_vdp();
+    case VA_MODEL_VDP_PETSC:
+        return va::kernels_vdp_petsc();
+    case VA_MODEL_DHO:
+        return va::kernels_dho();
+    case VA_MODEL_DECAY:
+        return va::kernels_decay();
+    case VA_MODEL_GLV:
+        return va::kernels_glv(p.n);
+    default:
+        return nullptr;
+    }
+}
+
+int grid_for(va_handle *h, const void *fn, int block, int instances)
+{
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, block, 0) != cudaSuccess || occ < 1)
+        occ = 1;
+    int bps = h->opt.blocks_per_sm > 0 ? std::min(h->opt.blocks_per_sm, occ) : occ;
+    long need = ((long)instances * h->ks->tpi + block - 1) / block;
+    long g = (long)h->sm_count * bps;
+    return (int)std::max(1L, std::min(g, need));
+}
+
+va_status ensure_buffers(va_handle *h)
+{
+    if (h->pool_rec)
+        return VA_OK;
+    const int B = h->prob.batch;
+    const size_t rec_bytes = (size_t)h->RS * sizeof(double);
+    const size_t chunk_bytes = rec_bytes * h->chunk_len;
+    int64_t budget = h->opt.ckpt_budget_bytes > 0 ? h->opt.ckpt_budget_bytes : kDefaultBudget;
+    const int64_t per_inst_chunks = ((int64_t)h->opt.max_steps + 1 + h->chunk_len - 1) / h->chunk_len;
+    int64_t worst = per_inst_chunks * B;
+    int64_t by_budget = budget / (int64_t)chunk_bytes;
+    int64_t nch = std::min(worst, by_budget);
+    nch = std::max<int64_t>(nch, 1);
+    if (nch > 0x7fffffff)
+        nch = 0x7fffffff;
+    h->n_chunks = (int)nch;
+    VA_CUDA(h, cudaMalloc(&h->pool_rec, (size_t)nch * chunk_bytes));
+    VA_CUDA(h, cudaMalloc(&h->chunk_prev, (size_t)nch * sizeof(int)));
+    VA_CUDA(h, cudaMalloc(&h->inst_T, (size_t)B * sizeof(int)));
+    VA_CUDA(h, cudaMalloc(&h->inst_last, (size_t)B * sizeof(int)));
+    VA_CUDA(h, cudaMalloc(&h->inst_status, (size_t)B * sizeof(int)));
+    VA_CUDA(h, cudaMalloc(&h->ctl, sizeof(va::Control)));
+    VA_CUDA(h, cudaMemset(h->ctl, 0, sizeof(va::Control)));
+    return VA_OK;
+}
+
+va_status ensure_staging(va_handle *h)
+{
+    if (h->s_y0)
+        return VA_OK;
+    const size_t B = h->prob.batch, N = h->N, P = h->P, Q = h->prob.nout;
+    VA_CUDA(h, cudaMalloc(&h->s_y0, B * N * sizeof(double)));
+    VA_CUDA(h, cudaMalloc(&h->s_par, B * P * sizeof(double)));
+    VA_CUDA(h, cudaMalloc(&h->s_t0, B * sizeof(double)));
+    VA_CUDA(h, cudaMalloc(&h->s_t1, B * sizeof(double)));
+    VA_CUDA(h, cudaMalloc(&h->s_yT, B * N * sizeof(double)));
+    VA_CUDA(h, cudaMalloc(&h->s_dy0, B * Q * N * sizeof(double)));
+    VA_CUDA(h, cudaMalloc(&h->s_dpar, B * Q * P * sizeof(double)));
+    VA_CUDA(h, cudaMalloc(&h->s_nacc, B * sizeof(int)));
+    VA_CUDA(h, cudaMalloc(&h->s_status, B * sizeof(int)));
+    return VA_OK;
+}
+
+va::Pool pool_of(va_handle *h)
+{
+    va::Pool p;
+    p.rec = h->pool_rec;
+    p.chunk_prev = h->chunk_prev;
+    p.n_chunks = h->n_chunks;
+    p.chunk_len = h->chunk_len;
+    return p;
+}
+
+cudaError_t launch(const void *fn, int grid, int block, void *params, cudaStream_t s)
+{
+    void *args[] = {params};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, s);
+}
+
+va_status enqueue_forward(va_handle *h, const double *y0, const double *params, const double *t0,
+                          const double *t1, double *yT, int32_t *n_acc, int32_t *n_rej,
+                          int32_t *status, cudaStream_t s)
+{
+    va::FwdParams a{};
+    a.B = h->prob.batch;
+    a.y0 = y0;
+    a.par = params;
+    a.t0 = t0;
+    a.t1 = t1;
+    a.atol = h->opt.atol;
+    a.rtol = h->opt.rtol;
+    a.dt0 = h->opt.dt0;
+    a.max_steps = h->opt.max_steps;
+    a.max_fail = h->opt.max_rejects;
+    a.yT = yT;
+    a.n_acc_out = n_acc;
+    a.n_rej_out = n_rej;
+    a.status_out = status;
+    a.inst_T = h->inst_T;
+    a.inst_last = h->inst_last;
+    a.inst_status = h->inst_status;
+    a.pool = pool_of(h);
+    a.ctl = h->ctl;
+    const void *fn = h->ks->fwd[h->opt.tableau][h->opt.precision];
+    if (h->fwd_grid <= 0)
+        h->fwd_grid = grid_for(h, fn, h->fwd_block, a.B);
+    VA_CUDA(h, cudaMemsetAsync(h->ctl, 0, sizeof(va::Control), s));
+    VA_CUDA(h, launch(fn, h->fwd_grid, h->fwd_block, &a, s));
+    return VA_OK;
+}
+
+va_status enqueue_backward(va_handle *h, const double *params, const double *lambdaT,
+                           const double *mu_direct, int cost, double *dy0, double *dparams,
+                           int32_t *status, cudaStream_t s)
+{
+    va::AdjParams a{};
+    a.B = h->prob.batch;
+    a.nout = h->prob.nout;
+    a.par = params;
+    a.lambdaT = lambdaT;
+    a.mu_direct = mu_direct;
+    a.cost = cost;
+    a.dy0 = dy0;
+    a.dpar = dparams;
+    a.status_out = status;
+    a.order = nullptr;
+    a.inst_T = h->inst_T;
+    a.inst_last = h->inst_last;
+    a.inst_status = h->inst_status;
+    a.pool = pool_of(h);
+    a.ctl = h->ctl;
+    const void *fn = h->ks->bwd[h->opt.tableau][h->opt.precision];
+    if (h->bwd_grid <= 0)
+        h->bwd_grid = grid_for(h, fn, h->bwd_block, a.B);
+    VA_CUDA(h, cudaMemsetAsync(&h->ctl->adj_next, 0, sizeof(unsigned int), s));
+    VA_CUDA(h, launch(fn, h->bwd_grid, h->bwd_block, &a, s));
+    return VA_OK;
+}
+
+void drop_graph(va_handle *h)
+{
+    if (h->graph) {
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    h->graph_key = GraphKey{};
+}
+
+} // namespace
+
+extern "C" {
+
+const char *va_status_string(int32_t s)
+{
+    switch (s) {
+    case VA_OK:
+        return "VA_OK";
+    case VA_MAX_REJECTS:
+        return "VA_MAX_REJECTS";
+    case VA_MAX_STEPS:
+        return "VA_MAX_STEPS";
+    case VA_NONFINITE:
+        return "VA_NONFINITE";
+    case VA_CKPT_BUDGET:
+        return "VA_CKPT_BUDGET";
+    case VA_BAD_ARGS:
+        return "VA_BAD_ARGS";
+    case VA_CUDA_ERROR:
+        return "VA_CUDA_ERROR";
+    case VA_NOT_READY:
+        return "VA_NOT_READY";
+    case VA_RECOMPUTE_MISMATCH:
+        return "VA_RECOMPUTE_MISMATCH";
+    case VA_NOT_RUN:
+        return "VA_NOT_RUN";
+    default:
+        return "VA_UNKNOWN";
+    }
+}
+
+const char *va_last_error(const va_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+va_status va_default_options(va_options *o)
+{
+    if (!o)
+        return VA_BAD_ARGS;
+    std::memset(o, 0, sizeof(*o));
+    o->tableau = VA_TAB_DOPRI5;
+    o->precision = VA_PREC_FP64;
+    o->atol = 1e-6;
+    o->rtol = 1e-6;
+    o->dt0 = 1e-3;
+    o->max_steps = 1000000;
+    o->max_rejects = 500;
+    o->ckpt_budget_bytes = 0;
+    o->ckpt_stride = 0;
+    o->block_size = 0;
+    o->blocks_per_sm = 0;
+    o->chunk_len = 0;
+    return VA_OK;
+}
+
+va_status va_create(const va_problem *prob, const va_options *opt, va_handle **out)
+{
+    if (!prob || !out)
+        return VA_BAD_ARGS;
+    *out = nullptr;
+    va_options o;
+    if (opt)
+        o = *opt;
+    else
+        va_default_options(&o);
+    if (prob->batch < 1 || prob->nout < 1 || prob->n < 1)
+        return VA_BAD_ARGS;
+    if (o.tableau != VA_TAB_DOPRI5 && o.tableau != VA_TAB_CK54)
+        return VA_BAD_ARGS;
+    if (o.precision != VA_PREC_FP64 && o.precision != VA_PREC_MIXED)
+        return VA_BAD_ARGS;
+    if (!(o.atol >= 0.0) || !(o.rtol >= 0.0) || !(o.atol + o.rtol > 0.0) || !(o.dt0 > 0.0))
+        return VA_BAD_ARGS;
+    if (o.max_steps < 1 || o.max_rejects < 1)
+        return VA_BAD_ARGS;
+    const va::KernelSet *ks = kernel_set(*prob);
+    if (!ks)
+        return VA_BAD_ARGS;
+    const int N = ks->N > 0 ? ks->N : prob->n;
+    const int P = ks->P > 0 ? ks->P : prob->npar;
+    if (prob->n != N || prob->npar != P)
+        return VA_BAD_ARGS;
+    if (o.ckpt_stride > 1)
+        return VA_BAD_ARGS; // two-level checkpointing is handled by the segment path
+    va_handle *h = new va_handle();
+    h->prob = *prob;
+    h->opt = o;
+    h->ks = ks;
+    h->N = N;
+    h->P = P;
+    h->RS = va::record_doubles(N);
+    h->chunk_len = o.chunk_len > 0 ? o.chunk_len : 64;
+    if (o.block_size > 0) {
+        h->fwd_block = h->bwd_block = o.block_size;
+    }
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device);
+    if (e != cudaSuccess) {
+        delete h;
+        return VA_CUDA_ERROR;
+    }
+    *out = h;
+    return VA_OK;
+}
+
+va_status va_destroy(va_handle *h)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    drop_graph(h);
+    void *ptrs[] = {h->pool_rec, h->chunk_prev, h->inst_T,  h->inst_last, h->inst_status,
+                    h->ctl,      h->s_y0,       h->s_par,   h->s_t0,      h->s_t1,
+                    h->s_yT,     h->s_dy0,      h->s_dpar,  h->s_nacc,    h->s_status};
+    for (void *p : ptrs)
+        if (p)
+            cudaFree(p);
+    delete h;
+    return VA_OK;
+}
+
+va_status va_forward(va_handle *h, const double *y0, const double *params, const double *t0,
+                     const double *t1, double *yT, int32_t *n_acc, int32_t *n_rej, int32_t *status,
+                     void *stream)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    if (!y0 || !params || !t0 || !t1)
+        return fail(h, VA_BAD_ARGS, "va_forward: null input pointer%s");
+    va_status st = ensure_buffers(h);
+    if (st != VA_OK)
+        return st;
+    st = enqueue_forward(h, y0, params, t0, t1, yT, n_acc, n_rej, status, (cudaStream_t)stream);
+    if (st == VA_OK)
+        h->forward_done = true;
+    return st;
+}
+
+va_status va_backward(va_handle *h, const double *params, const double *lambdaT,
+                      const double *mu_direct, double *dy0, double *dparams, int32_t *status,
+                      void *stream)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    if (!h->forward_done)
+        return fail(h, VA_NOT_READY, "va_backward: no forward sweep has run on this handle%s");
+    if (!params || !lambdaT || !dy0 || !dparams)
+        return fail(h, VA_BAD_ARGS, "va_backward: null pointer%s");
+    return enqueue_backward(h, params, lambdaT, mu_direct, VA_COST_SEEDS, dy0, dparams, status,
+                            (cudaStream_t)stream);
+}
+
+va_status va_gradient(va_handle *h, int32_t cost, const double *y0, const double *params,
+                      const double *t0, const double *t1, double *yT, double *dy0, double *dparams,
+                      int32_t *n_acc, int32_t *status, void *stream)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    if (cost != VA_COST_SUMSQ && cost != VA_COST_SUM)
+        return fail(h, VA_BAD_ARGS, "va_gradient: cost must be VA_COST_SUMSQ or VA_COST_SUM%s");
+    if (h->prob.nout != 1)
+        return fail(h, VA_BAD_ARGS, "va_gradient: built-in costs need nout == 1%s");
+    if (!y0 || !params || !t0 || !t1 || !dy0 || !dparams)
+        return fail(h, VA_BAD_ARGS, "va_gradient: null pointer%s");
+    va_status st = ensure_buffers(h);
+    if (st != VA_OK)
+        return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    GraphKey key;
+    key.cost = cost;
+    const void *ptrs[10] = {y0, params, t0, t1, yT, dy0, dparams, n_acc, status, nullptr};
+    std::memcpy(key.ptrs, ptrs, sizeof(ptrs));
+    key.stream = stream;
+    // The legacy default stream cannot be captured: launch directly there.
+    if (s == nullptr) {
+        st = enqueue_forward(h, y0, params, t0, t1, yT, n_acc, nullptr, status, s);
+        if (st != VA_OK)
+            return st;
+        h->forward_done = true;
+        return enqueue_backward(h, params, nullptr, nullptr, cost, dy0, dparams, status, s);
+    }
+    if (!h->graph || !(h->graph_key == key)) {
+        drop_graph(h);
+        // size the persistent grids before capture (occupancy queries)
+        if (h->fwd_grid <= 0)
+            h->fwd_grid = grid_for(h, h->ks->fwd[h->opt.tableau][h->opt.precision], h->fwd_block,
+                                   h->prob.batch);
+        if (h->bwd_grid <= 0)
+            h->bwd_grid = grid_for(h, h->ks->bwd[h->opt.tableau][h->opt.precision], h->bwd_block,
+                                   h->prob.batch);
+        VA_CUDA(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        va_status s1 = enqueue_forward(h, y0, params, t0, t1, yT, n_acc, nullptr, status, s);
+        va_status s2 = s1 == VA_OK
+                           ? enqueue_backward(h, params, nullptr, nullptr, cost, dy0, dparams, status, s)
+                           : s1;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (s2 != VA_OK) {
+            if (g)
+                cudaGraphDestroy(g);
+            return s2;
+        }
+        if (e != cudaSuccess)
+            return cuda_fail(h, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&h->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            h->graph = nullptr;
+            return cuda_fail(h, e, "cudaGraphInstantiate");
+        }
+        h->graph_key = key;
+    }
+    VA_CUDA(h, cudaGraphLaunch(h->graph, s));
+    h->forward_done = true;
+    return VA_OK;
+}
+
+va_status va_gradient_host(va_handle *h, int32_t cost, const double *y0, const double *params,
+                           const double *t0, const double *t1, double *yT, double *dy0,
+                           double *dparams, int32_t *n_acc, int32_t *status, void *stream)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    if (!y0 || !params || !t0 || !t1)
+        return fail(h, VA_BAD_ARGS, "va_gradient_host: null input pointer%s");
+    va_status st = ensure_staging(h);
+    if (st != VA_OK)
+        return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t B = h->prob.batch, N = h->N, P = h->P;
+    VA_CUDA(h, cudaMemcpyAsync(h->s_y0, y0, B * N * sizeof(double), cudaMemcpyHostToDevice, s));
+    VA_CUDA(h, cudaMemcpyAsync(h->s_par, params, B * P * sizeof(double), cudaMemcpyHostToDevice, s));
+    VA_CUDA(h, cudaMemcpyAsync(h->s_t0, t0, B * sizeof(double), cudaMemcpyHostToDevice, s));
+    VA_CUDA(h, cudaMemcpyAsync(h->s_t1, t1, B * sizeof(double), cudaMemcpyHostToDevice, s));
+    st = va_gradient(h, cost, h->s_y0, h->s_par, h->s_t0, h->s_t1, h->s_yT, h->s_dy0, h->s_dpar,
+                     h->s_nacc, h->s_status, stream);
+    if (st != VA_OK)
+        return st;
+    if (yT)
+        VA_CUDA(h, cudaMemcpyAsync(yT, h->s_yT, B * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (dy0)
+        VA_CUDA(h, cudaMemcpyAsync(dy0, h->s_dy0, B * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (dparams)
+        VA_CUDA(h, cudaMemcpyAsync(dparams, h->s_dpar, B * P * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (n_acc)
+        VA_CUDA(h, cudaMemcpyAsync(n_acc, h->s_nacc, B * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (status)
+        VA_CUDA(h, cudaMemcpyAsync(status, h->s_status, B * sizeof(int), cudaMemcpyDeviceToHost, s));
+    VA_CUDA(h, cudaStreamSynchronize(s));
+    return VA_OK;
+}
+
+va_status va_get_launch(const va_handle *h, int32_t *fwd_block, int32_t *fwd_grid,
+                        int32_t *bwd_block, int32_t *bwd_grid)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    if (fwd_block)
+        *fwd_block = h->fwd_block;
+    if (fwd_grid)
+        *fwd_grid = h->fwd_grid;
+    if (bwd_block)
+        *bwd_block = h->bwd_block;
+    if (bwd_grid)
+        *bwd_grid = h->bwd_grid;
+    return VA_OK;
+}
+
+va_status va_checkpoint_info(const va_handle *h, int64_t *capacity_bytes, int64_t *used_bytes,
+                             int32_t *stride)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    const int64_t chunk_bytes = (int64_t)h->RS * sizeof(double) * h->chunk_len;
+    if (capacity_bytes)
+        *capacity_bytes = (int64_t)h->n_chunks * chunk_bytes;
+    if (used_bytes) {
+        *used_bytes = 0;
+        if (h->ctl) {
+            va::Control c{};
+            if (cudaMemcpy(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost) == cudaSuccess)
+                *used_bytes = (int64_t)std::min<unsigned>(c.pool_next, (unsigned)h->n_chunks) * chunk_bytes;
+        }
+    }
+    if (stride)
+        *stride = 1;
+    return VA_OK;
+}
+
+va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double *t, double *dt,
+                        double *y, int32_t *n_records)
+{
+    if (!h || instance < 0 || instance >= h->prob.batch || capacity < 0)
+        return VA_BAD_ARGS;
+    if (!h->forward_done || !h->inst_T)
+        return fail(h, VA_NOT_READY, "va_trajectory: no forward sweep has run%s");
+    VA_CUDA(h, cudaDeviceSynchronize());
+    int T = 0, last = -1, st = 0;
+    VA_CUDA(h, cudaMemcpy(&T, h->inst_T + instance, sizeof(int), cudaMemcpyDeviceToHost));
+    VA_CUDA(h, cudaMemcpy(&last, h->inst_last + instance, sizeof(int), cudaMemcpyDeviceToHost));
+    VA_CUDA(h, cudaMemcpy(&st, h->inst_status + instance, sizeof(int), cudaMemcpyDeviceToHost));
+    if (n_records)
+        *n_records = T + 1;
+    if (st != VA_OK || last < 0)
+        return fail(h, (va_status)st, "va_trajectory: instance has no complete record%s");
+    const int CH = h->chunk_len, RS = h->RS, N = h->N;
+    std::vector<double> buf((size_t)CH * RS);
+    int chunk = last;
+    int first_in_chunk = (T / CH) * CH; // record index at slot 0 of the last chunk
+    while (chunk >= 0 && first_in_chunk >= 0) {
+        const int cnt = std::min(CH, T + 1 - first_in_chunk);
+        VA_CUDA(h, cudaMemcpy(buf.data(), h->pool_rec + (size_t)chunk * CH * RS,
+                              (size_t)cnt * RS * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int k = 0; k < cnt; k++) {
+            const int j = first_in_chunk + k;
+            if (j >= capacity)
+                continue;
+            if (t)
+                t[j] = buf[(size_t)k * RS];
+            if (dt)
+                dt[j] = buf[(size_t)k * RS + 1];
+            if (y)
+                for (int i = 0; i < N; i++)
+                    y[(size_t)j * N + i] = buf[(size_t)k * RS + 2 + i];
+        }
+        int prev = -1;
+        VA_CUDA(h, cudaMemcpy(&prev, h->chunk_prev + chunk, sizeof(int), cudaMemcpyDeviceToHost));
+        chunk = prev;
+        first_in_chunk -= CH;
+    }
+    return VA_OK;
+}
+
+va_status va_autotune(va_handle *h, int32_t cost, const double *y0, const double *params,
+                      const double *t0, const double *t1, void *stream)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    va_status st = ensure_buffers(h);
+    if (st != VA_OK)
+        return st;
+    st = ensure_staging(h);
+    if (st != VA_OK)
+        return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    const void *ffn = h->ks->fwd[h->opt.tableau][h->opt.precision];
+    const void *bfn = h->ks->bwd[h->opt.tableau][h->opt.precision];
+    cudaEvent_t e0, e1, e2;
+    VA_CUDA(h, cudaEventCreate(&e0));
+    VA_CUDA(h, cudaEventCreate(&e1));
+    VA_CUDA(h, cudaEventCreate(&e2));
+    float best_f = 1e30f, best_b = 1e30f;
+    int bf_block = h->fwd_block, bf_grid = h->fwd_grid, bb_block = h->bwd_block, bb_grid = h->bwd_grid;
+    const int blocks[] = {64, 128, 256};
+    for (int blk : blocks) {
+        int occf = 0, occb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occf, ffn, blk, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occb, bfn, blk, 0);
+        int maxocc = std::max(1, std::max(occf, occb));
+        std::vector<int> cands;
+        for (int c = 1; c < maxocc; c *= 2)
+            cands.push_back(c);
+        cands.push_back(maxocc);
+        for (int bps : cands) {
+            h->fwd_block = h->bwd_block = blk;
+            long need = ((long)h->prob.batch * h->ks->tpi + blk - 1) / blk;
+            h->fwd_grid = (int)std::max(1L, std::min((long)h->sm_count * std::min(bps, std::max(occf, 1)), need));
+            h->bwd_grid = (int)std::max(1L, std::min((long)h->sm_count * std::min(bps, std::max(occb, 1)), need));
+            for (int rep = 0; rep < 2; rep++) {
+                VA_CUDA(h, cudaEventRecord(e0, s));
+                st = enqueue_forward(h, y0, params, t0, t1, h->s_yT, nullptr, nullptr, h->s_status, s);
+                if (st != VA_OK)
+                    return st;
+                VA_CUDA(h, cudaEventRecord(e1, s));
+                st = enqueue_backward(h, params, nullptr, nullptr, cost, h->s_dy0, h->s_dpar, h->s_status, s);
+                if (st != VA_OK)
+                    return st;
+                VA_CUDA(h, cudaEventRecord(e2, s));
+                VA_CUDA(h, cudaEventSynchronize(e2));
+                float tf = 0, tb = 0;
+                cudaEventElapsedTime(&tf, e0, e1);
+                cudaEventElapsedTime(&tb, e1, e2);
+                if (rep == 1) {
+                    if (tf < best_f) {
+                        best_f = tf;
+                        bf_block = blk;
+                        bf_grid = h->fwd_grid;
+                    }
+                    if (tb < best_b) {
+                        best_b = tb;
+                        bb_block = blk;
+                        bb_grid = h->bwd_grid;
+                    }
+                }
+            }
+        }
+    }
+    h->fwd_block = bf_block;
+    h->fwd_grid = bf_grid;
+    h->bwd_block = bb_block;
+    h->bwd_grid = bb_grid;
+    drop_graph(h);
+    h->forward_done = true;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    return VA_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,646 @@
+// Persistent forward and backward sweeps for models whose whole state fits in
+// one thread (VdP, DHO, decay): one thread owns one instance at a time and,
+// when that instance is done, takes the next one from a global counter, so a
+// lane never waits for the slowest instance of its warp.
+//
+// Forward sweep  = the reference's controlled loop
+//   (lib/include/detail/runge_kutta.hpp:137-180) with odeint 1.74's
+//   controlled_runge_kutta::try_step, default_error_checker and
+//   default_step_adjuster run on the device.  Every accepted (t_n, dt_n, y_n)
+//   is written to a chunked checkpoint pool in HBM (StateStorage.hpp:23-35).
+// Backward sweep = back_prop / back_prop_step
+//   (lib/include/detail/backpropagation.hpp:160-278): h_n = t_{n+1} - t_n
+//   (StateStorage.hpp:22), stages recomputed from y_n, seeds b_m h lambda,
+//   transposed-tableau accumulation, mu += J_p^T Kbar.
+//
+// S is the stage type: double (FP64 path, the reference's arithmetic order)
+// or float (mixed path: stages and VJPs in FP32; t, h, y, the error norm,
+// the controller and the gradient accumulators stay FP64).
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+
+#include "va_tableau.cuh"
+
+namespace va {
+
+enum : int32_t {
+    ST_OK = 0,
+    ST_MAX_REJECTS = 1,
+    ST_MAX_STEPS = 2,
+    ST_NONFINITE = 3,
+    ST_CKPT_BUDGET = 4,
+    ST_BAD_ARGS = 5,
+    ST_RECOMPUTE_MISMATCH = 8,
+    ST_NOT_RUN = 9
+};
+
+constexpr double kDblEps = 2.220446049250313080847e-16; // std::numeric_limits<double>::epsilon()
+
+// Device control block, cleared before every launch.
+struct Control {
+    unsigned int fwd_next;  // next instance for the forward sweep
+    unsigned int adj_next;  // next position in the backward work order
+    unsigned int pool_next; // next free checkpoint chunk
+    unsigned int pool_fail; // set when the pool ran out
+};
+
+// Checkpoint pool: chunks of `chunk_len` records of `rs` doubles.
+// Record layout: [t_n, dt_n (trial step at the top of step n), y_n[0..N)].
+struct Pool {
+    double *rec;
+    int *chunk_prev;
+    int n_chunks;
+    int chunk_len;
+};
+
+struct FwdParams {
+    int B;
+    const double *y0;  // [B][N]
+    const double *par; // [B][P]
+    const double *t0;  // [B]
+    const double *t1;  // [B]
+    double atol, rtol, dt0;
+    int max_steps, max_fail;
+    double *yT;      // [B][N] (may be null)
+    int *n_acc_out;  // [B] (may be null)
+    int *n_rej_out;  // [B] (may be null)
+    int *status_out; // [B] (may be null)
+    int *inst_T;     // [B] accepted steps
+    int *inst_last;  // [B] last checkpoint chunk
+    int *inst_status;// [B]
+    Pool pool;
+    Control *ctl;
+};
+
+struct AdjParams {
+    int B;
+    int nout;
+    const double *par;       // [B][P]
+    const double *lambdaT;   // [B][nout][N]  (null when cost >= 0)
+    const double *mu_direct; // [B][nout][P]  (may be null)
+    int cost;                // -1 seeds from lambdaT; 0: g = sum y(T)^2; 1: g = sum y(T)
+    double *dy0;             // [B][nout][N]
+    double *dpar;            // [B][nout][P]
+    int *status_out;         // [B] (may be null)
+    const int *order;        // [B] work order (may be null = identity)
+    const int *inst_T;
+    const int *inst_last;
+    const int *inst_status;
+    Pool pool;
+    Control *ctl;
+};
+
+__host__ __device__ constexpr int record_doubles(int n) { return (2 + n + 1) & ~1; }
+
+// ---------------------------------------------------------------- controller
+
+// odeint default_step_adjuster::decrease_step:
+//   dt *= max(0.9 err^(-1/(q-1)), 0.2)
+template <class Tab>
+__device__ __forceinline__ double decrease_step(double dt, double err)
+{
+    double f = 9.0 / 10.0 * pow(err, -1.0 / (Tab::ERROR_ORDER - 1));
+    return dt * fmax(f, 1.0 / 5.0);
+}
+
+// odeint default_step_adjuster::increase_step:
+//   if err < 0.5: dt *= 0.9 max(err, 5^-p)^(-1/p)
+template <class Tab>
+__device__ __forceinline__ double increase_step(double dt, double err)
+{
+    if (err < 0.5) {
+        // 5^-5 = 1/3125, exactly the rounding of pow(5.0, -5.0)
+        constexpr double floor_err = 1.0 / 3125.0;
+        static_assert(Tab::STEPPER_ORDER == 5, "floor constant assumes a fifth-order stepper");
+        err = fmax(floor_err, err);
+        dt *= 9.0 / 10.0 * pow(err, -1.0 / Tab::STEPPER_ORDER);
+    }
+    return dt;
+}
+
+// ------------------------------------------------------------- stage algebra
+
+// X_m = y + sum_{j<m} (a_mj dt) K_j, in the order odeint's scale_sum
+// evaluates it (and the reference recomputes it, backpropagation.hpp:36-45).
+template <class Tab, int N, class S>
+__device__ __forceinline__ void form_stage(int m, const double (&y)[N], const S (&K)[Tab::S][N],
+                                           double dt, S (&X)[N])
+{
+    if constexpr (std::is_same<S, double>::value) {
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            double acc = y[i];
+#pragma unroll
+            for (int j = 0; j < Tab::S - 1; j++)
+                if (j < m)
+                    acc = acc + (Tab::a(m, j) * dt) * K[j][i];
+            X[i] = acc;
+        }
+    } else {
+        const float fdt = (float)dt;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int j = 0; j < Tab::S - 1; j++)
+                if (j < m)
+                    acc = fmaf((float)Tab::a(m, j), K[j][i], acc);
+            X[i] = fmaf(acc, fdt, (float)y[i]);
+        }
+    }
+}
+
+// One attempted step of the embedded pair from (y, k0 = f(y), t) with step dt:
+// y_new, k_new = f(y_new) (FSAL pairs) and the error norm
+// max_i |err_i| / (atol + rtol (|y_i| + |dt| |k0_i|))  (default_error_checker
+// with a_x = a_dxdt = 1, evaluated at the step start).
+template <class M, class Tab, class S>
+__device__ __forceinline__ double attempt(const double (&y)[M::N], const S (&k0)[M::N],
+                                          const S (&p)[M::P], double t, double dt, double atol,
+                                          double rtol, double (&ynew)[M::N], S (&knew)[M::N])
+{
+    constexpr int N = M::N, NS = Tab::S;
+    S K[NS][N];
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        K[0][i] = k0[i];
+#pragma unroll
+    for (int m = 1; m < NS; m++) {
+        S X[N];
+        form_stage<Tab, N, S>(m, y, K, dt, X);
+        M::template rhs<S>(X, p, S(t + Tab::c(m) * dt), K[m]);
+    }
+    double e[N];
+    if constexpr (std::is_same<S, double>::value) {
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            double acc = y[i];
+#pragma unroll
+            for (int j = 0; j < NS; j++)
+                if (Tab::b(j) != 0.0)
+                    acc = acc + (Tab::b(j) * dt) * K[j][i];
+            ynew[i] = acc;
+        }
+        if constexpr (Tab::FSAL)
+            M::template rhs<S>(ynew, p, t + dt, knew);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            double acc = 0.0;
+            bool first = true;
+#pragma unroll
+            for (int j = 0; j < NS; j++)
+                if (Tab::e(j) != 0.0) {
+                    double term = (Tab::e(j) * dt) * K[j][i];
+                    acc = first ? term : acc + term;
+                    first = false;
+                }
+            if constexpr (Tab::FSAL)
+                acc = acc + (Tab::E_NEW * dt) * knew[i];
+            e[i] = acc;
+        }
+    } else {
+        float dy[N];
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int j = 0; j < NS; j++)
+                if (Tab::b(j) != 0.0)
+                    acc = fmaf((float)Tab::b(j), K[j][i], acc);
+            dy[i] = acc;
+            ynew[i] = fma(dt, (double)acc, y[i]);
+        }
+        if constexpr (Tab::FSAL) {
+            float yf[N];
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                yf[i] = (float)ynew[i];
+            M::template rhs<float>(yf, p, (float)(t + dt), knew);
+        }
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int j = 0; j < NS; j++)
+                if (Tab::e(j) != 0.0)
+                    acc = fmaf((float)Tab::e(j), K[j][i], acc);
+            if constexpr (Tab::FSAL)
+                acc = fmaf((float)Tab::E_NEW, knew[i], acc);
+            e[i] = dt * (double)acc;
+        }
+        (void)dy;
+    }
+    // max-norm with a single division: keep the largest ratio as a fraction
+    const double adt = fabs(dt);
+    double num = fabs(e[0]);
+    double den = atol + rtol * (1.0 * fabs(y[0]) + adt * fabs((double)k0[0]));
+#pragma unroll
+    for (int i = 1; i < N; i++) {
+        double ni = fabs(e[i]);
+        double di = atol + rtol * (1.0 * fabs(y[i]) + adt * fabs((double)k0[i]));
+        if (ni * den > num * di || ni != ni) {
+            num = ni;
+            den = di;
+        }
+    }
+    return num / den;
+}
+
+// Checkpoint pool helpers.  Record j of an instance lives in chunk j / CH of
+// its chain, slot j % CH.
+template <int RS>
+__device__ __forceinline__ double *record_ptr(const Pool &pool, int chunk, int slot)
+{
+    return pool.rec + ((size_t)chunk * pool.chunk_len + slot) * RS;
+}
+
+template <int N>
+__device__ __forceinline__ void write_record(double *r, double t, double dt, const double (&y)[N])
+{
+    constexpr int RS = record_doubles(N);
+    double v[RS];
+    v[0] = t;
+    v[1] = dt;
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        v[2 + i] = y[i];
+#pragma unroll
+    for (int i = 2 + N; i < RS; i++)
+        v[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < RS; i += 2)
+        *reinterpret_cast<double2 *>(r + i) = make_double2(v[i], v[i + 1]);
+}
+
+template <int N>
+__device__ __forceinline__ void read_record(const double *r, double &t, double (&y)[N])
+{
+    constexpr int RS = record_doubles(N);
+    double v[RS];
+#pragma unroll
+    for (int i = 0; i < RS; i += 2) {
+        double2 q = __ldcs(reinterpret_cast<const double2 *>(r + i));
+        v[i] = q.x;
+        v[i + 1] = q.y;
+    }
+    t = v[0];
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        y[i] = v[2 + i];
+}
+
+// ------------------------------------------------------------ forward sweep
+
+template <class M, class Tab, class S>
+__global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
+{
+    constexpr int N = M::N, P = M::P;
+    constexpr int RS = record_doubles(N);
+    const int CH = a.pool.chunk_len;
+
+    int b = -1;
+    double y[N], t = 0.0, t1 = 0.0, dt = 0.0;
+    S k0[N], p[P];
+    int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
+    bool at_top = true;
+
+    // Take the next instance; false when the batch is exhausted.
+    auto fetch = [&]() -> bool {
+        b = (int)atomicAdd(&a.ctl->fwd_next, 1u);
+        if (b >= a.B)
+            return false;
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            y[i] = a.y0[(size_t)b * N + i];
+#pragma unroll
+        for (int k = 0; k < P; k++)
+            p[k] = (S)a.par[(size_t)b * P + k];
+        t = a.t0[b];
+        t1 = a.t1[b];
+        dt = a.dt0;
+        count = rej = fails = 0;
+        status = ST_OK;
+        at_top = true;
+        slot = 0;
+        chunk = (int)atomicAdd(&a.ctl->pool_next, 1u);
+        if (chunk >= a.pool.n_chunks) {
+            status = ST_CKPT_BUDGET;
+            chunk = -1;
+            atomicOr(&a.ctl->pool_fail, 1u);
+        } else {
+            a.pool.chunk_prev[chunk] = -1;
+        }
+        // k_1 = f(y_0): odeint computes it on the first call (FSAL) or on
+        // every attempt (non-FSAL, same value for the same y, t).
+        if constexpr (std::is_same<S, double>::value) {
+            M::template rhs<S>(y, p, t, k0);
+        } else {
+            float yf[N];
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                yf[i] = (float)y[i];
+            M::template rhs<float>(yf, p, (float)t, k0);
+        }
+        return true;
+    };
+
+    // Reserve the slot of record `count`; false if the pool ran out.
+    auto reserve = [&]() -> bool {
+        if (chunk < 0)
+            return false;
+        if (count > 0 && slot == CH) {
+            int c = (int)atomicAdd(&a.ctl->pool_next, 1u);
+            if (c >= a.pool.n_chunks) {
+                atomicOr(&a.ctl->pool_fail, 1u);
+                return false;
+            }
+            a.pool.chunk_prev[c] = chunk;
+            chunk = c;
+            slot = 0;
+        }
+        return true;
+    };
+
+    auto finish = [&]() {
+        if (status == ST_OK) {
+            if (reserve()) {
+                write_record<N>(record_ptr<RS>(a.pool, chunk, slot), t, dt, y);
+                slot++;
+            } else {
+                status = ST_CKPT_BUDGET;
+            }
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                if (!isfinite(y[i]))
+                    status = ST_NONFINITE;
+        }
+        if (a.yT) {
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                a.yT[(size_t)b * N + i] = y[i];
+        }
+        a.inst_T[b] = count;
+        a.inst_last[b] = chunk;
+        a.inst_status[b] = status;
+        if (a.n_acc_out)
+            a.n_acc_out[b] = count;
+        if (a.n_rej_out)
+            a.n_rej_out[b] = rej;
+        if (a.status_out)
+            a.status_out[b] = status;
+    };
+
+    bool alive = fetch();
+    while (alive) {
+        if (status != ST_OK) {
+            finish();
+            alive = fetch();
+            continue;
+        }
+        if (at_top) {
+            // while (less_with_sign(t, t1, dt))  (runge_kutta.hpp:155)
+            if (!(t1 - t > kDblEps)) {
+                finish();
+                alive = fetch();
+                continue;
+            }
+            if (count >= a.max_steps) {
+                status = ST_MAX_STEPS;
+                continue;
+            }
+            if (!reserve()) {
+                status = ST_CKPT_BUDGET;
+                continue;
+            }
+            write_record<N>(record_ptr<RS>(a.pool, chunk, slot), t, dt, y);
+            slot++;
+            // end clamp (runge_kutta.hpp:160-163)
+            if ((t + dt) - t1 > kDblEps)
+                dt = t1 - t;
+            fails = 0;
+            at_top = false;
+        }
+        double ynew[N];
+        S knew[N];
+        const double err = attempt<M, Tab, S>(y, k0, p, t, dt, a.atol, a.rtol, ynew, knew);
+        bool ok;
+        if (err != err) {
+            status = ST_NONFINITE;
+            continue;
+        }
+        if (err > 1.0) {
+            dt = decrease_step<Tab>(dt, err);
+            rej++;
+            ok = false;
+        } else {
+            t += dt;
+            dt = increase_step<Tab>(dt, err);
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                y[i] = ynew[i];
+            if constexpr (Tab::FSAL) {
+#pragma unroll
+                for (int i = 0; i < N; i++)
+                    k0[i] = knew[i];
+            } else {
+                if constexpr (std::is_same<S, double>::value) {
+                    M::template rhs<S>(y, p, t, k0);
+                } else {
+                    float yf[N];
+#pragma unroll
+                    for (int i = 0; i < N; i++)
+                        yf[i] = (float)y[i];
+                    M::template rhs<float>(yf, p, (float)t, k0);
+                }
+            }
+            ok = true;
+        }
+        // failed_step_checker: at most max_fail attempts per accepted step
+        if (fails >= a.max_fail) {
+            status = ST_MAX_REJECTS;
+            continue;
+        }
+        fails++;
+        if (ok) {
+            count++;
+            at_top = true;
+        } else if (!(dt > 0.0) || !isfinite(dt)) {
+            status = ST_NONFINITE;
+        }
+    }
+}
+
+// ----------------------------------------------------------- backward sweep
+
+// One back_prop_step (backpropagation.hpp:160-229) for step n with state y_n,
+// start time tn and h = t_{n+1} - t_n.  lam: in lambda_{n+1}, out lambda_n.
+template <class M, class Tab, class S>
+__device__ __forceinline__ void back_step(const double (&y)[M::N], double tn, double h,
+                                          const S (&p)[M::P], double (&lam)[M::N],
+                                          double (&mu)[M::P])
+{
+    constexpr int N = M::N, P = M::P, NS = Tab::S;
+    S K[NS][N];
+    S X[NS][N];
+    // recompute the stages from y_n (compute_intermediate_states, :24-64)
+#pragma unroll
+    for (int m = 0; m < NS; m++) {
+        form_stage<Tab, N, S>(m, y, K, h, X[m]);
+        M::template rhs<S>(X[m], p, S(tn + Tab::c(m) * h), K[m]);
+    }
+    // seeds: ybar = lambda, Kbar_m = (b_m h) lambda  (:178-184)
+    S Kbar[NS][N];
+    double ybar[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        ybar[i] = lam[i];
+#pragma unroll
+        for (int m = 0; m < NS; m++) {
+            if constexpr (std::is_same<S, double>::value)
+                Kbar[m][i] = (Tab::b(m) * h) * lam[i];
+            else
+                Kbar[m][i] = ((float)Tab::b(m) * (float)h) * (float)lam[i];
+        }
+    }
+    // stages s..1 (:196-224)
+#pragma unroll
+    for (int m = NS - 1; m >= 0; m--) {
+        S gx[N], gp[P];
+        M::template vjp<S>(Kbar[m], X[m], p, S(tn + Tab::c(m) * h), gx, gp);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            ybar[i] += (double)gx[i];
+#pragma unroll
+            for (int k = 0; k < NS - 1; k++)
+                if (k < m) {
+                    if constexpr (std::is_same<S, double>::value)
+                        Kbar[k][i] += gx[i] * Tab::a(m, k) * h;
+                    else
+                        Kbar[k][i] = fmaf(gx[i] * (float)Tab::a(m, k), (float)h, Kbar[k][i]);
+                }
+        }
+#pragma unroll
+        for (int k = 0; k < P; k++)
+            mu[k] += (double)gp[k];
+    }
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        lam[i] = ybar[i];
+}
+
+template <class M, class Tab, class S>
+__global__ void __launch_bounds__(256) backward_kernel(AdjParams a)
+{
+    constexpr int N = M::N, P = M::P;
+    constexpr int RS = record_doubles(N);
+    const int CH = a.pool.chunk_len;
+
+    int b = -1, q = 0, j = -1, chunk = -1, slot = 0, T = 0, last = -1;
+    double lam[N], mu[P], t_next = 0.0;
+    S p[P];
+    bool alive = true, live = false;
+
+    // Position the walk on record T of instance b and seed cost q.
+    auto start_seed = [&]() {
+        chunk = last;
+        slot = T % a.pool.chunk_len;
+        double yTl[N];
+        read_record<N>(record_ptr<RS>(a.pool, chunk, slot), t_next, yTl);
+        const size_t o = ((size_t)b * a.nout + q);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            if (a.cost == 0)
+                lam[i] = 2.0 * yTl[i];
+            else if (a.cost == 1)
+                lam[i] = 1.0;
+            else
+                lam[i] = a.lambdaT[o * N + i];
+        }
+#pragma unroll
+        for (int k = 0; k < P; k++)
+            mu[k] = 0.0;
+        j = T - 1;
+    };
+
+    auto fetch = [&]() -> bool {
+        for (;;) {
+            unsigned w = atomicAdd(&a.ctl->adj_next, 1u);
+            if ((int)w >= a.B)
+                return false;
+            b = a.order ? a.order[w] : (int)w;
+            const int st = a.inst_status[b];
+            if (st != ST_OK) {
+                // no trajectory to differentiate: report the forward status
+                for (int qq = 0; qq < a.nout; qq++) {
+                    const size_t o = ((size_t)b * a.nout + qq);
+                    for (int i = 0; i < N; i++)
+                        a.dy0[o * N + i] = __longlong_as_double(0x7ff8000000000000ll);
+                    for (int k = 0; k < P; k++)
+                        a.dpar[o * P + k] = __longlong_as_double(0x7ff8000000000000ll);
+                }
+                if (a.status_out)
+                    a.status_out[b] = st;
+                continue;
+            }
+#pragma unroll
+            for (int k = 0; k < P; k++)
+                p[k] = (S)a.par[(size_t)b * P + k];
+            T = a.inst_T[b];
+            last = a.inst_last[b];
+            q = 0;
+            start_seed();
+            return true;
+        }
+    };
+
+    auto finish_seed = [&]() {
+        const size_t o = ((size_t)b * a.nout + q);
+        bool finite = true;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            a.dy0[o * N + i] = lam[i];
+            finite = finite && isfinite(lam[i]);
+        }
+#pragma unroll
+        for (int k = 0; k < P; k++) {
+            // mu_direct + accumulated alphabar (backpropagation.hpp:317-321)
+            const double d = a.mu_direct ? a.mu_direct[o * P + k] : 0.0;
+            a.dpar[o * P + k] = d + mu[k];
+            finite = finite && isfinite(mu[k]);
+        }
+        if (a.status_out && (q == a.nout - 1 || !finite))
+            a.status_out[b] = finite ? ST_OK : ST_NONFINITE;
+    };
+
+    live = fetch();
+    alive = live;
+    while (alive) {
+        if (j < 0) {
+            finish_seed();
+            if (q + 1 < a.nout) {
+                q++;
+                start_seed();
+            } else {
+                alive = fetch();
+            }
+            continue;
+        }
+        // step back to record j
+        if (slot == 0) {
+            chunk = a.pool.chunk_prev[chunk];
+            slot = CH - 1;
+        } else {
+            slot--;
+        }
+        double y[N], tn;
+        read_record<N>(record_ptr<RS>(a.pool, chunk, slot), tn, y);
+        const double h = t_next - tn;
+        back_step<M, Tab, S>(y, tn, h, p, lam, mu);
+        t_next = tn;
+        j--;
+    }
+}
+
+} // namespace va

@@ -1,0 +1,90 @@
+// Butcher tableaux of the embedded explicit Runge-Kutta pairs, as
+// compile-time constants that fold into the unrolled stage loops.
+//
+// Cash-Karp 5(4) (Cash & Karp 1990) is the pair the reference reads from
+// odeint in lib/include/ButcherTable.hpp:259-308.  Dormand-Prince 5(4)
+// (Dormand & Prince 1980) is not in the reference's ButcherTable
+// (ButcherTable.hpp:365-368 rejects it); it is added here from the published
+// tableau.  Each coefficient is the IEEE quotient of its two integers, and
+// each error weight the difference of two such quotients, the same values
+// odeint 1.74's rk54_ck_coefficients_* and runge_kutta_dopri5 compute.
+#pragma once
+
+namespace va {
+
+struct TabDopri5 {
+    static constexpr int S = 6;           // stages feeding y_{n+1}
+    static constexpr bool FSAL = true;    // f(y_{n+1}) is the next k_1
+    static constexpr int ERROR_ORDER = 4; // odeint error_order_value
+    static constexpr int STEPPER_ORDER = 5;
+    __host__ __device__ static constexpr double a(int i, int j)
+    {
+        return i == 1 ? (j == 0 ? 1.0 / 5.0 : 0.0)
+             : i == 2 ? (j == 0 ? 3.0 / 40.0 : j == 1 ? 9.0 / 40.0 : 0.0)
+             : i == 3 ? (j == 0 ? 44.0 / 45.0 : j == 1 ? -56.0 / 15.0 : j == 2 ? 32.0 / 9.0 : 0.0)
+             : i == 4 ? (j == 0 ? 19372.0 / 6561.0 : j == 1 ? -25360.0 / 2187.0
+                         : j == 2 ? 64448.0 / 6561.0 : j == 3 ? -212.0 / 729.0 : 0.0)
+             : i == 5 ? (j == 0 ? 9017.0 / 3168.0 : j == 1 ? -355.0 / 33.0 : j == 2 ? 46732.0 / 5247.0
+                         : j == 3 ? 49.0 / 176.0 : j == 4 ? -5103.0 / 18656.0 : 0.0)
+             : 0.0;
+    }
+    __host__ __device__ static constexpr double b(int j)
+    {
+        return j == 0 ? 35.0 / 384.0 : j == 2 ? 500.0 / 1113.0 : j == 3 ? 125.0 / 192.0
+             : j == 4 ? -2187.0 / 6784.0 : j == 5 ? 11.0 / 84.0 : 0.0;
+    }
+    __host__ __device__ static constexpr double c(int j)
+    {
+        return j == 1 ? 1.0 / 5.0 : j == 2 ? 3.0 / 10.0 : j == 3 ? 4.0 / 5.0 : j == 4 ? 8.0 / 9.0
+             : j == 5 ? 1.0 : 0.0;
+    }
+    // b - b_hat on k_1..k_6, and on f(y_{n+1})
+    __host__ __device__ static constexpr double e(int j)
+    {
+        return j == 0 ? 35.0 / 384.0 - 5179.0 / 57600.0
+             : j == 2 ? 500.0 / 1113.0 - 7571.0 / 16695.0
+             : j == 3 ? 125.0 / 192.0 - 393.0 / 640.0
+             : j == 4 ? -2187.0 / 6784.0 - -92097.0 / 339200.0
+             : j == 5 ? 11.0 / 84.0 - 187.0 / 2100.0 : 0.0;
+    }
+    static constexpr double E_NEW = -1.0 / 40.0;
+};
+
+struct TabCK54 {
+    static constexpr int S = 6;
+    static constexpr bool FSAL = false;
+    static constexpr int ERROR_ORDER = 4;
+    static constexpr int STEPPER_ORDER = 5;
+    __host__ __device__ static constexpr double a(int i, int j)
+    {
+        return i == 1 ? (j == 0 ? 1.0 / 5.0 : 0.0)
+             : i == 2 ? (j == 0 ? 3.0 / 40.0 : j == 1 ? 9.0 / 40.0 : 0.0)
+             : i == 3 ? (j == 0 ? 3.0 / 10.0 : j == 1 ? -9.0 / 10.0 : j == 2 ? 6.0 / 5.0 : 0.0)
+             : i == 4 ? (j == 0 ? -11.0 / 54.0 : j == 1 ? 5.0 / 2.0 : j == 2 ? -70.0 / 27.0
+                         : j == 3 ? 35.0 / 27.0 : 0.0)
+             : i == 5 ? (j == 0 ? 1631.0 / 55296.0 : j == 1 ? 175.0 / 512.0 : j == 2 ? 575.0 / 13824.0
+                         : j == 3 ? 44275.0 / 110592.0 : j == 4 ? 253.0 / 4096.0 : 0.0)
+             : 0.0;
+    }
+    __host__ __device__ static constexpr double b(int j)
+    {
+        return j == 0 ? 37.0 / 378.0 : j == 2 ? 250.0 / 621.0 : j == 3 ? 125.0 / 594.0
+             : j == 5 ? 512.0 / 1771.0 : 0.0;
+    }
+    __host__ __device__ static constexpr double c(int j)
+    {
+        return j == 1 ? 1.0 / 5.0 : j == 2 ? 3.0 / 10.0 : j == 3 ? 3.0 / 5.0 : j == 4 ? 1.0
+             : j == 5 ? 7.0 / 8.0 : 0.0;
+    }
+    __host__ __device__ static constexpr double e(int j)
+    {
+        return j == 0 ? 37.0 / 378.0 - 2825.0 / 27648.0
+             : j == 2 ? 250.0 / 621.0 - 18575.0 / 48384.0
+             : j == 3 ? 125.0 / 594.0 - 13525.0 / 55296.0
+             : j == 4 ? -277.0 / 14336.0
+             : j == 5 ? 512.0 / 1771.0 - 1.0 / 4.0 : 0.0;
+    }
+    static constexpr double E_NEW = 0.0;
+};
+
+} // namespace va

@@ -1,0 +1,150 @@
+"""Batched solver over the C ABI (include/va.h).
+
+`Solver` wraps one va_handle: a batch of B instances of one built-in model.
+Inputs and outputs are CUDA tensors (torch provides device memory and
+streams only; all arithmetic runs in the library's CUDA kernels).  The
+forward/backward pair maps one-to-one onto va_forward / va_backward, so a
+torch.autograd.Function can wrap it.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class Solver:
+    """One batch of B independent instances of a built-in model.
+
+    model     : 'vdp' | 'vdp_petsc' | 'dho' | 'glv' | 'decay'
+    n, npar   : state and per-instance parameter counts
+    batch     : B
+    nout      : cost functions (seed rows) per instance
+    tableau   : 'dopri5' | 'ck54'
+    precision : 'fp64' | 'mixed'
+    """
+
+    def __init__(self, model, n, npar, batch, nout=1, tableau="dopri5", precision="fp64",
+                 atol=1e-6, rtol=1e-6, dt0=1e-3, max_steps=1000000, max_rejects=500,
+                 ckpt_budget_bytes=0, ckpt_stride=0, block_size=0, blocks_per_sm=0, chunk_len=0):
+        self.L = _lib.load()
+        if not torch.cuda.is_available():
+            raise RuntimeError("vectorizedadjoint_gb300 needs a CUDA device (no CPU fallback)")
+        self.model, self.n, self.npar, self.batch, self.nout = model, n, npar, batch, nout
+        self.tableau, self.precision = tableau, precision
+        prob = _lib.VaProblem(_lib.MODELS[model], n, npar, batch, nout)
+        opt = _lib.VaOptions()
+        self.L.va_default_options(ctypes.byref(opt))
+        opt.tableau = _lib.TABLEAUX[tableau]
+        opt.precision = _lib.PRECISIONS[precision]
+        opt.atol, opt.rtol, opt.dt0 = atol, rtol, dt0
+        opt.max_steps, opt.max_rejects = max_steps, max_rejects
+        opt.ckpt_budget_bytes, opt.ckpt_stride = ckpt_budget_bytes, ckpt_stride
+        opt.block_size, opt.blocks_per_sm, opt.chunk_len = block_size, blocks_per_sm, chunk_len
+        torch.cuda.init()
+        self.h = ctypes.c_void_p()
+        st = self.L.va_create(ctypes.byref(prob), ctypes.byref(opt), ctypes.byref(self.h))
+        if st != _lib.VA_OK:
+            raise _lib.VaError(st, f"va_create({model}, n={n}, npar={npar}, B={batch})")
+
+    def _check(self, st, what):
+        if st != _lib.VA_OK:
+            raise _lib.VaError(st, f"{what}: {self.L.va_last_error(self.h).decode()}")
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.va_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- device-tensor entry points -------------------------------------------------
+    def _alloc(self, *shape, dtype=torch.float64):
+        return torch.empty(*shape, dtype=dtype, device="cuda")
+
+    def forward(self, y0, params, t0, t1):
+        """va_forward.  Returns dict(yT, n_acc, n_rej, status) of CUDA tensors."""
+        B, n = self.batch, self.n
+        yT = self._alloc(B, n)
+        n_acc = self._alloc(B, dtype=torch.int32)
+        n_rej = self._alloc(B, dtype=torch.int32)
+        status = self._alloc(B, dtype=torch.int32)
+        self._inputs = (y0, params, t0, t1)
+        self._check(self.L.va_forward(self.h, _ptr(y0), _ptr(params), _ptr(t0), _ptr(t1), _ptr(yT),
+                                      _ptr(n_acc), _ptr(n_rej), _ptr(status), _stream()), "va_forward")
+        return dict(yT=yT, n_acc=n_acc, n_rej=n_rej, status=status)
+
+    def backward(self, params, lambdaT, mu_direct=None):
+        """va_backward.  lambdaT [B, nout, n], mu_direct [B, nout, npar] or None."""
+        B, n, P, Q = self.batch, self.n, self.npar, self.nout
+        dy0 = self._alloc(B, Q, n)
+        dp = self._alloc(B, Q, P)
+        status = self._alloc(B, dtype=torch.int32)
+        self._check(self.L.va_backward(self.h, _ptr(params), _ptr(lambdaT), _ptr(mu_direct), _ptr(dy0),
+                                       _ptr(dp), _ptr(status), _stream()), "va_backward")
+        return dict(dy0=dy0, dp=dp, status=status)
+
+    def gradient(self, cost, y0, params, t0, t1, out=None):
+        """va_gradient (forward + backward, graph-captured).  cost 'sumsq' | 'sum'."""
+        B, n, P = self.batch, self.n, self.npar
+        if out is None:
+            out = dict(yT=self._alloc(B, n), dy0=self._alloc(B, n), dp=self._alloc(B, P),
+                       n_acc=self._alloc(B, dtype=torch.int32), status=self._alloc(B, dtype=torch.int32))
+        self._check(self.L.va_gradient(self.h, _lib.COSTS[cost], _ptr(y0), _ptr(params), _ptr(t0), _ptr(t1),
+                                       _ptr(out["yT"]), _ptr(out["dy0"]), _ptr(out["dp"]), _ptr(out["n_acc"]),
+                                       _ptr(out["status"]), _stream()), "va_gradient")
+        return out
+
+    def gradient_host(self, cost, y0, params, t0, t1, out=None):
+        """va_gradient_host: host (numpy / CPU tensor) buffers in and out."""
+        import numpy as np
+        B, n, P = self.batch, self.n, self.npar
+
+        def hp(a):
+            return ctypes.c_void_p(a.ctypes.data) if isinstance(a, np.ndarray) else ctypes.c_void_p(a.data_ptr())
+        if out is None:
+            out = dict(yT=np.empty((B, n)), dy0=np.empty((B, n)), dp=np.empty((B, P)),
+                       n_acc=np.empty(B, np.int32), status=np.empty(B, np.int32))
+        self._check(self.L.va_gradient_host(self.h, _lib.COSTS[cost], hp(y0), hp(params), hp(t0), hp(t1),
+                                            hp(out["yT"]), hp(out["dy0"]), hp(out["dp"]), hp(out["n_acc"]),
+                                            hp(out["status"]), _stream()), "va_gradient_host")
+        return out
+
+    def autotune(self, cost, y0, params, t0, t1):
+        self._check(self.L.va_autotune(self.h, _lib.COSTS[cost], _ptr(y0), _ptr(params), _ptr(t0), _ptr(t1),
+                                       _stream()), "va_autotune")
+        return self.launch()
+
+    def launch(self):
+        v = [ctypes.c_int32() for _ in range(4)]
+        self.L.va_get_launch(self.h, *[ctypes.byref(x) for x in v])
+        return dict(fwd_block=v[0].value, fwd_grid=v[1].value, bwd_block=v[2].value, bwd_grid=v[3].value)
+
+    def trajectory(self, instance, capacity=None):
+        """Accepted-step record of one instance: (t[T+1], dt[T+1], y[T+1, n]) as numpy arrays."""
+        import numpy as np
+        nrec = ctypes.c_int32()
+        self.L.va_trajectory(self.h, instance, 0, None, None, None, ctypes.byref(nrec))
+        cap = nrec.value if capacity is None else capacity
+        t, dt, y = np.zeros(cap), np.zeros(cap), np.zeros((cap, self.n))
+        self._check(self.L.va_trajectory(self.h, instance, cap, ctypes.c_void_p(t.ctypes.data),
+                                         ctypes.c_void_p(dt.ctypes.data), ctypes.c_void_p(y.ctypes.data),
+                                         ctypes.byref(nrec)), "va_trajectory")
+        return t[:nrec.value], dt[:nrec.value], y[:nrec.value]
+
+    def checkpoint_info(self):
+        cap, used, stride = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()
+        self.L.va_checkpoint_info(self.h, ctypes.byref(cap), ctypes.byref(used), ctypes.byref(stride))
+        return dict(capacity_bytes=cap.value, used_bytes=used.value, stride=stride.value)
