@@ -173,7 +173,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default="vdpb")
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed_dw", choices=["mixed_dw", "mixed", "fp64"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
@@ -266,31 +266,46 @@ def _bench(args, rank, world, local, torch, dist):
     dom = ("forward", fl_f, fms) if fms >= bms else ("backward", fl_b, bms)
     achieved = dom[1] / (dom[2] * 1e-3) / 1e12
 
-    # FP64 reference gradients on the same batch: error of this run against FP64
-    err = None
-    if args.precision == "mixed":
-        s64 = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision="fp64",
-                     atol=c["tol"], rtol=c["tol"], ckpt_budget_bytes=c.get("budget", 0))
-        o64 = s64.gradient(c["cost"], y0, par, t0, t1)
-        torch.cuda.synchronize()
-        t64 = []
+    # the other precision modes on the same batch: throughput and gradient error vs FP64
+    def run_mode(precision):
+        sm = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision=precision,
+                    atol=c["tol"], rtol=c["tol"], ckpt_budget_bytes=c.get("budget", 0))
+        sm.autotune(c["cost"], y0, par, t0, t1)
+        o = sm.gradient(c["cost"], y0, par, t0, t1)
+        tt = []
         for _ in range(3):
+            flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            s64.gradient(c["cost"], y0, par, t0, t1, out=o64)
+            sm.gradient(c["cost"], y0, par, t0, t1, out=o)
             e1.record(stream)
             e1.synchronize()
-            t64.append(e0.elapsed_time(e1))
-        g = torch.cat([out["dy0"], out["dp"]], 1)
+            tt.append(e0.elapsed_time(e1))
+        sm.close()
+        return B / (float(np.median(tt)) * 1e-3), o
+
+    def grad_err(o, o64):
+        g = torch.cat([o["dy0"], o["dp"]], 1)
         g64 = torch.cat([o64["dy0"], o64["dp"]], 1)
         rel = ((g - g64).abs().amax(1) / g64.abs().amax(1).clamp_min(1e-300)).cpu().numpy()
-        ok = (status == 0) & (o64["status"].cpu().numpy() == 0)
-        err = {"median": float(np.median(rel[ok])), "p99": float(np.quantile(rel[ok], 0.99)),
-               "max": float(rel[ok].max()), "vs": "FP64 path of this library (oracle-checked)"}
-        fp64_value = B / (float(np.median(t64)) * 1e-3)
-        s64.close()
+        ok = (o["status"].cpu().numpy() == 0) & (o64["status"].cpu().numpy() == 0)
+        same = float((o["n_acc"] == o64["n_acc"]).float().mean().item())
+        return {"median": float(np.median(rel[ok])), "p99": float(np.quantile(rel[ok], 0.99)),
+                "max": float(rel[ok].max()), "same_step_count": same,
+                "vs": "FP64 path of this library (oracle-checked in tests)"}
+
+    modes = {}
+    if args.precision == "fp64":
+        fp64_value, o64 = value, out
     else:
-        fp64_value = value
+        fp64_value, o64 = run_mode("fp64")
+    modes["fp64"] = {"gradients_per_s": fp64_value}
+    modes[args.precision] = {"gradients_per_s": value, "grad_err_vs_fp64": grad_err(out, o64)}
+    for other in ("mixed_dw", "mixed"):
+        if other not in modes:
+            v, o = run_mode(other)
+            modes[other] = {"gradients_per_s": v, "grad_err_vs_fp64": grad_err(o, o64)}
+    err = modes[args.precision].get("grad_err_vs_fp64")
 
     # plain drop-in: the FP64 path called once per instance through the host entry point
     M = 64
@@ -332,7 +347,8 @@ def _bench(args, rank, world, local, torch, dist):
             "metric": "adjoint gradients/s", "value": value, "unit": "gradients/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 stages / f64 controller+accumulators" if args.precision == "mixed" else "f64",
+            "dtype": {"mixed_dw": "f32x2 (double-word) stages / f64 controller+accumulators",
+                      "mixed": "f32 stages / f64 controller+accumulators", "fp64": "f64"}[args.precision],
             "data": "synthetic (seeded PCG64)",
             "config": {"workload": f"{args.config}: {c['model']} B={B} {c['tableau']} tol={c['tol']}",
                        "batch": B, "precision": args.precision, "cost": c["cost"],
@@ -347,6 +363,7 @@ def _bench(args, rank, world, local, torch, dist):
                          "flops_per_launch": dom[1], "launch_ms": dom[2], "traffic": None,
                          "forward_ms": fms, "backward_ms": bms},
             "fp64_batched": fp64_value,
+            "modes": modes,
             "plain_fp64_per_instance": plain,
             "batched_vs_plain": value / plain,
             "grad_err_vs_fp64": err,

@@ -61,8 +61,10 @@ typedef enum { VA_TAB_DOPRI5 = 0, VA_TAB_CK54 = 1 } va_tableau;
 
 typedef enum {
     VA_PREC_FP64 = 0, /* all arithmetic FP64: the drop-in path                          */
-    VA_PREC_MIXED = 1 /* FP32 stages and VJPs; FP64 t, h, y, error norm, controller and
-                         gradient accumulators                                           */
+    VA_PREC_MIXED = 1, /* FP32 stages and VJPs; FP64 t, h, y, error norm, controller and
+                          gradient accumulators                                          */
+    VA_PREC_MIXED_DW = 2 /* as VA_PREC_MIXED, but stages and VJPs in double-word arithmetic
+                            (pairs of FP32, ~48-bit significand) on the FP32 pipe         */
 } va_precision;
 
 typedef enum { VA_COST_SEEDS = -1, VA_COST_SUMSQ = 0, VA_COST_SUM = 1 } va_cost;

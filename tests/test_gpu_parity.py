@@ -63,7 +63,9 @@ def test_fp64_gradients_match_oracle(oracle, cuda, name, B):
     for b, g in zip(idx, ref):
         assert g["status"] == 0
         assert int(r["n_acc"][b]) == g["n_acc"], (b, int(r["n_acc"][b]), g["n_acc"])
-        assert rel_err(r["yT"][b], g["yT"], 1e-8) < REL_Y * 100, b
+        # relative to the trajectory's scale: a decayed oscillator ends near 0
+        yscale = max(np.abs(w["y0"][b]).max(), np.abs(g["yT"]).max())
+        assert np.abs(r["yT"][b] - g["yT"]).max() / yscale < REL_Y * 100, b
         assert grad_rel(r["dy0"][b], g["dy0"]) < REL_G, b
         assert grad_rel(r["dp"][b], g["dp"]) < REL_G, b
     s.close()
@@ -159,13 +161,29 @@ def test_host_entry_point_matches_device(cuda):
 
 @pytest.mark.parametrize("name,B,bound", [("vdp1", 1, 1e-5), ("dho", 256, 1e-5), ("vdpb", 512, 1e-4)])
 def test_mixed_precision_error_vs_fp64(oracle, cuda, name, B, bound):
-    """Mixed path (FP32 stages/VJPs, FP64 controller and accumulators): gradient
-    error against the FP64 oracle, bounded per config (measured values are
-    reported by bench.py)."""
+    """Plain FP32 stages/VJPs (FP64 controller and accumulators): median
+    gradient error against the FP64 oracle, bounded per config."""
     s, w, r = run_gpu(name, B, precision="mixed")
     assert (r["status"] == 0).all()
     idx = list(range(0, B, max(1, B // 32)))
     pb, ref = oracle_batch(oracle, w, idx)
     errs = [max(grad_rel(r["dy0"][b], g["dy0"]), grad_rel(r["dp"][b], g["dp"])) for b, g in zip(idx, ref)]
     assert np.median(errs) < bound, (np.median(errs), max(errs))
+    s.close()
+
+
+@pytest.mark.parametrize("name,B", [("vdp1", 1), ("dho", 256), ("vdpb", 512)])
+def test_mixed_dw_error_vs_fp64(oracle, cuda, name, B):
+    """Double-word stages/VJPs on the FP32 pipe: gradient error against the FP64
+    oracle at most 1e-6 for every instance (the mixed-path target), median
+    below 1e-9, and the same accepted-step counts."""
+    s, w, r = run_gpu(name, B, precision="mixed_dw")
+    assert (r["status"] == 0).all()
+    idx = list(range(0, B, max(1, B // 32)))
+    pb, ref = oracle_batch(oracle, w, idx)
+    errs = [max(grad_rel(r["dy0"][b], g["dy0"]), grad_rel(r["dp"][b], g["dp"])) for b, g in zip(idx, ref)]
+    assert max(errs) <= 1e-6, (np.median(errs), max(errs))
+    assert np.median(errs) < 1e-9, np.median(errs)
+    same = [int(r["n_acc"][b]) == g["n_acc"] for b, g in zip(idx, ref)]
+    assert np.mean(same) >= 0.95
     s.close()

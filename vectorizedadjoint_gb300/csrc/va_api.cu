@@ -317,7 +317,7 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
         return VA_BAD_ARGS;
     if (o.tableau != VA_TAB_DOPRI5 && o.tableau != VA_TAB_CK54)
         return VA_BAD_ARGS;
-    if (o.precision != VA_PREC_FP64 && o.precision != VA_PREC_MIXED)
+    if (o.precision != VA_PREC_FP64 && o.precision != VA_PREC_MIXED && o.precision != VA_PREC_MIXED_DW)
         return VA_BAD_ARGS;
     if (!(o.atol >= 0.0) || !(o.rtol >= 0.0) || !(o.atol + o.rtol > 0.0) || !(o.dt0 > 0.0))
         return VA_BAD_ARGS;

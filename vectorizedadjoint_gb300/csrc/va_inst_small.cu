@@ -16,6 +16,10 @@ static KernelSet make_set()
     k.fwd[0][1] = (const void *)forward_kernel<M, TabDopri5, float>;
     k.fwd[1][0] = (const void *)forward_kernel<M, TabCK54, double>;
     k.fwd[1][1] = (const void *)forward_kernel<M, TabCK54, float>;
+    k.fwd[0][2] = (const void *)forward_kernel<M, TabDopri5, dword>;
+    k.fwd[1][2] = (const void *)forward_kernel<M, TabCK54, dword>;
+    k.bwd[0][2] = (const void *)backward_kernel<M, TabDopri5, dword>;
+    k.bwd[1][2] = (const void *)backward_kernel<M, TabCK54, dword>;
     k.bwd[0][0] = (const void *)backward_kernel<M, TabDopri5, double>;
     k.bwd[0][1] = (const void *)backward_kernel<M, TabDopri5, float>;
     k.bwd[1][0] = (const void *)backward_kernel<M, TabCK54, double>;

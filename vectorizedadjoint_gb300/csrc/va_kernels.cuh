@@ -21,6 +21,7 @@
 #include <cstdint>
 #include <type_traits>
 
+#include "va_dword.cuh"
 #include "va_tableau.cuh"
 
 namespace va {
@@ -94,28 +95,76 @@ struct AdjParams {
 
 __host__ __device__ constexpr int record_doubles(int n) { return (2 + n + 1) & ~1; }
 
+// Stage-type helpers for the reduced-precision paths (S = float or dword).
+template <class S>
+__host__ __device__ __forceinline__ S from_d(double v)
+{
+    return S(v);
+}
+__host__ __device__ __forceinline__ double to_d(double v) { return v; }
+__host__ __device__ __forceinline__ double to_d(float v) { return (double)v; }
+__host__ __device__ __forceinline__ double to_d(dword v) { return (double)v; }
+// a * b + c
+__host__ __device__ __forceinline__ float madd(float a, float b, float c) { return fmaf(a, b, c); }
+__host__ __device__ __forceinline__ dword madd(dword a, dword b, dword c) { return a * b + c; }
+template <class S>
+__host__ __device__ __forceinline__ S fromf(float v)
+{
+    return S(v, 0.0f);
+}
+template <>
+__host__ __device__ __forceinline__ float fromf<float>(float v)
+{
+    return v;
+}
+
 // ---------------------------------------------------------------- controller
+
+// a^(-1/K) for a > 0 in FP64 without a double-precision pow (FP64 issues at
+// 1/61 of the FP32 rate on this part): an FP32 seed, then two steps of
+// Newton's iteration for the inverse K-th root, x <- x + x (1 - a x^K) / K,
+// which converges quadratically (seed error ~1e-7 -> ~1e-14 -> rounding).
+// Inputs beyond the FP32 range seed x = 0 (a huge) or inf (a tiny); callers
+// only pass a in [5^-5, 0.5) (increase) or a > 1 (decrease, where x = 0
+// lands on the 0.2 limiter exactly as pow would).
+template <int K>
+__host__ __device__ __forceinline__ double inv_root(double a)
+{
+    double x = (double)powf((float)a, -1.0f / (float)K);
+    if (!(x > 0.0) || !isfinite(x))
+        return x;
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        double xk = x;
+#pragma unroll
+        for (int k = 1; k < K; k++)
+            xk *= x;
+        const double r = fma(-a, xk, 1.0);
+        x = fma(x * r, 1.0 / K, x);
+    }
+    return x;
+}
 
 // odeint default_step_adjuster::decrease_step:
 //   dt *= max(0.9 err^(-1/(q-1)), 0.2)
 template <class Tab>
-__device__ __forceinline__ double decrease_step(double dt, double err)
+__host__ __device__ __forceinline__ double decrease_step(double dt, double err)
 {
-    double f = 9.0 / 10.0 * pow(err, -1.0 / (Tab::ERROR_ORDER - 1));
+    double f = 9.0 / 10.0 * inv_root<Tab::ERROR_ORDER - 1>(err);
     return dt * fmax(f, 1.0 / 5.0);
 }
 
 // odeint default_step_adjuster::increase_step:
 //   if err < 0.5: dt *= 0.9 max(err, 5^-p)^(-1/p)
 template <class Tab>
-__device__ __forceinline__ double increase_step(double dt, double err)
+__host__ __device__ __forceinline__ double increase_step(double dt, double err)
 {
     if (err < 0.5) {
-        // 5^-5 = 1/3125, exactly the rounding of pow(5.0, -5.0)
+        // 5^-5 = 1/3125, the rounding of pow(5.0, -5.0)
         constexpr double floor_err = 1.0 / 3125.0;
         static_assert(Tab::STEPPER_ORDER == 5, "floor constant assumes a fifth-order stepper");
         err = fmax(floor_err, err);
-        dt *= 9.0 / 10.0 * pow(err, -1.0 / Tab::STEPPER_ORDER);
+        dt *= 9.0 / 10.0 * inv_root<Tab::STEPPER_ORDER>(err);
     }
     return dt;
 }
@@ -125,7 +174,7 @@ __device__ __forceinline__ double increase_step(double dt, double err)
 // X_m = y + sum_{j<m} (a_mj dt) K_j, in the order odeint's scale_sum
 // evaluates it (and the reference recomputes it, backpropagation.hpp:36-45).
 template <class Tab, int N, class S>
-__device__ __forceinline__ void form_stage(int m, const double (&y)[N], const S (&K)[Tab::S][N],
+__host__ __device__ __forceinline__ void form_stage(int m, const double (&y)[N], const S (&K)[Tab::S][N],
                                            double dt, S (&X)[N])
 {
     if constexpr (std::is_same<S, double>::value) {
@@ -139,15 +188,16 @@ __device__ __forceinline__ void form_stage(int m, const double (&y)[N], const S 
             X[i] = acc;
         }
     } else {
-        const float fdt = (float)dt;
+        // X = y + dt * sum_{j<m} a_mj K_j  (float or double-word stages)
+        const S sdt = from_d<S>(dt);
 #pragma unroll
         for (int i = 0; i < N; i++) {
-            float acc = 0.0f;
+            S acc = S(0);
 #pragma unroll
             for (int j = 0; j < Tab::S - 1; j++)
                 if (j < m)
-                    acc = fmaf((float)Tab::a(m, j), K[j][i], acc);
-            X[i] = fmaf(acc, fdt, (float)y[i]);
+                    acc = madd(S(Tab::a(m, j)), K[j][i], acc);
+            X[i] = madd(acc, sdt, from_d<S>(y[i]));
         }
     }
 }
@@ -157,7 +207,7 @@ __device__ __forceinline__ void form_stage(int m, const double (&y)[N], const S 
 // max_i |err_i| / (atol + rtol (|y_i| + |dt| |k0_i|))  (default_error_checker
 // with a_x = a_dxdt = 1, evaluated at the step start).
 template <class M, class Tab, class S>
-__device__ __forceinline__ double attempt(const double (&y)[M::N], const S (&k0)[M::N],
+__host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], const S (&k0)[M::N],
                                           const S (&p)[M::P], double t, double dt, double atol,
                                           double rtol, double (&ynew)[M::N], S (&knew)[M::N])
 {
@@ -201,51 +251,66 @@ __device__ __forceinline__ double attempt(const double (&y)[M::N], const S (&k0)
             e[i] = acc;
         }
     } else {
-        float dy[N];
+        // y_new = y + dt * sum_j b_j K_j: an FP64 update of an FP32 increment
+        // (float stages) or a double-word sum rounded once to FP64.
+        const S sdt = from_d<S>(dt);
 #pragma unroll
         for (int i = 0; i < N; i++) {
-            float acc = 0.0f;
+            S acc = S(0);
 #pragma unroll
             for (int j = 0; j < NS; j++)
                 if (Tab::b(j) != 0.0)
-                    acc = fmaf((float)Tab::b(j), K[j][i], acc);
-            dy[i] = acc;
-            ynew[i] = fma(dt, (double)acc, y[i]);
+                    acc = madd(S(Tab::b(j)), K[j][i], acc);
+            if constexpr (std::is_same<S, float>::value)
+                ynew[i] = fma(dt, (double)acc, y[i]);
+            else
+                ynew[i] = to_d(madd(acc, sdt, from_d<S>(y[i])));
         }
         if constexpr (Tab::FSAL) {
-            float yf[N];
+            S ys[N];
 #pragma unroll
             for (int i = 0; i < N; i++)
-                yf[i] = (float)ynew[i];
-            M::template rhs<float>(yf, p, (float)(t + dt), knew);
+                ys[i] = from_d<S>(ynew[i]);
+            M::template rhs<S>(ys, p, from_d<S>(t + dt), knew);
         }
 #pragma unroll
         for (int i = 0; i < N; i++) {
-            float acc = 0.0f;
+            S acc = S(0);
 #pragma unroll
             for (int j = 0; j < NS; j++)
                 if (Tab::e(j) != 0.0)
-                    acc = fmaf((float)Tab::e(j), K[j][i], acc);
+                    acc = madd(S(Tab::e(j)), K[j][i], acc);
             if constexpr (Tab::FSAL)
-                acc = fmaf((float)Tab::E_NEW, knew[i], acc);
-            e[i] = dt * (double)acc;
+                acc = madd(S(Tab::E_NEW), knew[i], acc);
+            e[i] = dt * to_d(acc);
         }
-        (void)dy;
     }
     // max-norm with a single division: keep the largest ratio as a fraction
     const double adt = fabs(dt);
     double num = fabs(e[0]);
-    double den = atol + rtol * (1.0 * fabs(y[0]) + adt * fabs((double)k0[0]));
+    double den = atol + rtol * (1.0 * fabs(y[0]) + adt * fabs(to_d(k0[0])));
 #pragma unroll
     for (int i = 1; i < N; i++) {
         double ni = fabs(e[i]);
-        double di = atol + rtol * (1.0 * fabs(y[i]) + adt * fabs((double)k0[i]));
+        double di = atol + rtol * (1.0 * fabs(y[i]) + adt * fabs(to_d(k0[i])));
         if (ni * den > num * di || ni != ni) {
             num = ni;
             den = di;
         }
     }
     return num / den;
+}
+
+// k = f(y) at an FP64 state, in stage precision.
+template <class M, class S>
+__host__ __device__ __forceinline__ void eval_rhs(const double (&y)[M::N], const S (&p)[M::P], double t,
+                                                  S (&k)[M::N])
+{
+    S ys[M::N];
+#pragma unroll
+    for (int i = 0; i < M::N; i++)
+        ys[i] = from_d<S>(y[i]);
+    M::template rhs<S>(ys, p, from_d<S>(t), k);
 }
 
 // Checkpoint pool helpers.  Record j of an instance lives in chunk j / CH of
@@ -316,7 +381,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
             y[i] = a.y0[(size_t)b * N + i];
 #pragma unroll
         for (int k = 0; k < P; k++)
-            p[k] = (S)a.par[(size_t)b * P + k];
+            p[k] = from_d<S>(a.par[(size_t)b * P + k]);
         t = a.t0[b];
         t1 = a.t1[b];
         dt = a.dt0;
@@ -334,15 +399,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
         }
         // k_1 = f(y_0): odeint computes it on the first call (FSAL) or on
         // every attempt (non-FSAL, same value for the same y, t).
-        if constexpr (std::is_same<S, double>::value) {
-            M::template rhs<S>(y, p, t, k0);
-        } else {
-            float yf[N];
-#pragma unroll
-            for (int i = 0; i < N; i++)
-                yf[i] = (float)y[i];
-            M::template rhs<float>(yf, p, (float)t, k0);
-        }
+        eval_rhs<M, S>(y, p, t, k0);
         return true;
     };
 
@@ -445,15 +502,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
                 for (int i = 0; i < N; i++)
                     k0[i] = knew[i];
             } else {
-                if constexpr (std::is_same<S, double>::value) {
-                    M::template rhs<S>(y, p, t, k0);
-                } else {
-                    float yf[N];
-#pragma unroll
-                    for (int i = 0; i < N; i++)
-                        yf[i] = (float)y[i];
-                    M::template rhs<float>(yf, p, (float)t, k0);
-                }
+                eval_rhs<M, S>(y, p, t, k0);
             }
             ok = true;
         }
@@ -477,7 +526,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
 // One back_prop_step (backpropagation.hpp:160-229) for step n with state y_n,
 // start time tn and h = t_{n+1} - t_n.  lam: in lambda_{n+1}, out lambda_n.
 template <class M, class Tab, class S>
-__device__ __forceinline__ void back_step(const double (&y)[M::N], double tn, double h,
+__host__ __device__ __forceinline__ void back_step(const double (&y)[M::N], double tn, double h,
                                           const S (&p)[M::P], double (&lam)[M::N],
                                           double (&mu)[M::P])
 {
@@ -488,46 +537,78 @@ __device__ __forceinline__ void back_step(const double (&y)[M::N], double tn, do
 #pragma unroll
     for (int m = 0; m < NS; m++) {
         form_stage<Tab, N, S>(m, y, K, h, X[m]);
-        M::template rhs<S>(X[m], p, S(tn + Tab::c(m) * h), K[m]);
+        M::template rhs<S>(X[m], p, from_d<S>(tn + Tab::c(m) * h), K[m]);
     }
-    // seeds: ybar = lambda, Kbar_m = (b_m h) lambda  (:178-184)
     S Kbar[NS][N];
-    double ybar[N];
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-        ybar[i] = lam[i];
-#pragma unroll
-        for (int m = 0; m < NS; m++) {
-            if constexpr (std::is_same<S, double>::value)
-                Kbar[m][i] = (Tab::b(m) * h) * lam[i];
-            else
-                Kbar[m][i] = ((float)Tab::b(m) * (float)h) * (float)lam[i];
-        }
-    }
-    // stages s..1 (:196-224)
-#pragma unroll
-    for (int m = NS - 1; m >= 0; m--) {
-        S gx[N], gp[P];
-        M::template vjp<S>(Kbar[m], X[m], p, S(tn + Tab::c(m) * h), gx, gp);
+    if constexpr (std::is_same<S, double>::value) {
+        // seeds: ybar = lambda, Kbar_m = (b_m h) lambda  (:178-184)
+        double ybar[N];
 #pragma unroll
         for (int i = 0; i < N; i++) {
-            ybar[i] += (double)gx[i];
+            ybar[i] = lam[i];
 #pragma unroll
-            for (int k = 0; k < NS - 1; k++)
-                if (k < m) {
-                    if constexpr (std::is_same<S, double>::value)
+            for (int m = 0; m < NS; m++)
+                Kbar[m][i] = (Tab::b(m) * h) * lam[i];
+        }
+        // stages s..1 (:196-224)
+#pragma unroll
+        for (int m = NS - 1; m >= 0; m--) {
+            S gx[N], gp[P];
+            M::template vjp<S>(Kbar[m], X[m], p, S(tn + Tab::c(m) * h), gx, gp);
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+                ybar[i] += gx[i];
+#pragma unroll
+                for (int k = 0; k < NS - 1; k++)
+                    if (k < m)
                         Kbar[k][i] += gx[i] * Tab::a(m, k) * h;
-                    else
-                        Kbar[k][i] = fmaf(gx[i] * (float)Tab::a(m, k), (float)h, Kbar[k][i]);
-                }
+            }
+#pragma unroll
+            for (int k = 0; k < P; k++)
+                mu[k] += gp[k];
         }
 #pragma unroll
-        for (int k = 0; k < P; k++)
-            mu[k] += (double)gp[k];
-    }
+        for (int i = 0; i < N; i++)
+            lam[i] = ybar[i];
+    } else {
+        // Same recurrence with stage-precision seeds and VJPs; the per-step
+        // sums of J^T Kbar are added to the FP64 lambda / mu once per step.
+        const S sdt = from_d<S>(h);
+        S sl[N];
 #pragma unroll
-    for (int i = 0; i < N; i++)
-        lam[i] = ybar[i];
+        for (int i = 0; i < N; i++)
+            sl[i] = from_d<S>(lam[i]);
+#pragma unroll
+        for (int m = 0; m < NS; m++) {
+            const S bh = S(Tab::b(m)) * sdt;
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                Kbar[m][i] = bh * sl[i];
+        }
+        S dx[N], dp[P];
+#pragma unroll
+        for (int m = NS - 1; m >= 0; m--) {
+            S gx[N], gp[P];
+            M::template vjp<S>(Kbar[m], X[m], p, from_d<S>(tn + Tab::c(m) * h), gx, gp);
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+                dx[i] = m == NS - 1 ? gx[i] : dx[i] + gx[i];
+#pragma unroll
+                for (int k = 0; k < NS - 1; k++)
+                    if (k < m)
+                        Kbar[k][i] = madd(gx[i] * S(Tab::a(m, k)), sdt, Kbar[k][i]);
+            }
+#pragma unroll
+            for (int k = 0; k < P; k++)
+                dp[k] = m == NS - 1 ? gp[k] : dp[k] + gp[k];
+        }
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            lam[i] += to_d(dx[i]);
+#pragma unroll
+        for (int k = 0; k < P; k++)
+            mu[k] += to_d(dp[k]);
+    }
 }
 
 template <class M, class Tab, class S>
@@ -586,7 +667,7 @@ __global__ void __launch_bounds__(256) backward_kernel(AdjParams a)
             }
 #pragma unroll
             for (int k = 0; k < P; k++)
-                p[k] = (S)a.par[(size_t)b * P + k];
+                p[k] = from_d<S>(a.par[(size_t)b * P + k]);
             T = a.inst_T[b];
             last = a.inst_last[b];
             q = 0;

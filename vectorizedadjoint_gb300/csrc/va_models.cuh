@@ -16,14 +16,14 @@ namespace va {
 struct ModelVdP {
     static constexpr int N = 2, P = 1;
     template <class S>
-    __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
+    __host__ __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
     {
         (void)t;
         f[0] = x[1];
         f[1] = p[0] * (S(1) - x[0] * x[0]) * x[1] - x[0];
     }
     template <class S>
-    __device__ __forceinline__ static void vjp(const S *w, const S *x, const S *p, S t, S *gx, S *gp)
+    __host__ __device__ __forceinline__ static void vjp(const S *w, const S *x, const S *p, S t, S *gx, S *gp)
     {
         (void)t;
         const S mu = p[0];
@@ -38,14 +38,14 @@ struct ModelVdP {
 struct ModelVdPPetsc {
     static constexpr int N = 2, P = 1;
     template <class S>
-    __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
+    __host__ __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
     {
         (void)t;
         f[0] = x[1];
         f[1] = p[0] * ((S(1) - x[0] * x[0]) * x[1] - x[0]);
     }
     template <class S>
-    __device__ __forceinline__ static void vjp(const S *w, const S *x, const S *p, S t, S *gx, S *gp)
+    __host__ __device__ __forceinline__ static void vjp(const S *w, const S *x, const S *p, S t, S *gx, S *gp)
     {
         (void)t;
         const S mu = p[0];
@@ -62,14 +62,14 @@ struct ModelVdPPetsc {
 struct ModelDHO {
     static constexpr int N = 2, P = 2;
     template <class S>
-    __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
+    __host__ __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
     {
         (void)t;
         f[0] = x[1];
         f[1] = -p[0] * p[0] * x[0] - S(2) * p[1] * p[0] * x[1];
     }
     template <class S>
-    __device__ __forceinline__ static void vjp(const S *w, const S *x, const S *p, S t, S *gx, S *gp)
+    __host__ __device__ __forceinline__ static void vjp(const S *w, const S *x, const S *p, S t, S *gx, S *gp)
     {
         (void)t;
         const S om = p[0], ze = p[1];
@@ -85,13 +85,13 @@ struct ModelDHO {
 struct ModelDecay {
     static constexpr int N = 1, P = 1;
     template <class S>
-    __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
+    __host__ __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
     {
         (void)t;
         f[0] = -p[0] * x[0];
     }
     template <class S>
-    __device__ __forceinline__ static void vjp(const S *w, const S *x, const S *p, S t, S *gx, S *gp)
+    __host__ __device__ __forceinline__ static void vjp(const S *w, const S *x, const S *p, S t, S *gx, S *gp)
     {
         (void)t;
         gx[0] = -p[0] * w[0];

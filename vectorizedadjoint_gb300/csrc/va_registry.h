@@ -8,8 +8,8 @@ namespace va {
 struct KernelSet {
     int N, P;          // state and parameter counts (0 = runtime n)
     int tpi;           // threads that carry one instance
-    const void *fwd[2][2]; // [tableau][precision] -> __global__ void(FwdParams)
-    const void *bwd[2][2]; // [tableau][precision] -> __global__ void(AdjParams)
+    const void *fwd[2][3]; // [tableau][precision] -> __global__ void(FwdParams)
+    const void *bwd[2][3]; // [tableau][precision] -> __global__ void(AdjParams)
 };
 
 const KernelSet *kernels_vdp();

@@ -29,7 +29,7 @@ class Solver:
     batch     : B
     nout      : cost functions (seed rows) per instance
     tableau   : 'dopri5' | 'ck54'
-    precision : 'fp64' | 'mixed'
+    precision : 'fp64' | 'mixed' (FP32 stages) | 'mixed_dw' (double-word FP32-pair stages)
     """
 
     def __init__(self, model, n, npar, batch, nout=1, tableau="dopri5", precision="fp64",
