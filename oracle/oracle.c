@@ -7,6 +7,7 @@
 #include "oracle.h"
 
 #include <float.h>
+#include <stdint.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
@@ -285,21 +286,61 @@ static double error_norm(const orc_problem *pb, const double *x, const double *d
     return m;
 }
 
-/* default_step_adjuster::decrease_step / increase_step */
-static double decrease_step(double dt, double err, int error_order)
+/* err^(-1/k).  pow_mode 1: the C library's pow, as odeint calls std::pow.
+ * pow_mode 0: a fixed IEEE-only scheme -- Newton's iteration for the inverse
+ * k-th root x <- x + x (1 - a x^k) / k from a seed read off the float bit
+ * pattern (exponent field scaled by -1/k), four FP32 steps then two FP64
+ * steps -- whose result is the same bits on every IEEE machine, so step
+ * sequences can be compared bit for bit with the CUDA library, which uses
+ * the same scheme.  The two modes differ in the last bit of some factors. */
+static double inv_root(double a, int k, int pow_mode)
 {
-    double f = 9.0 / 10.0 * pow(err, -1.0 / (error_order - 1));
+    if (pow_mode == 1)
+        return pow(a, -1.0 / k);
+    if (!(a < 1e30))
+        return 0.0;
+    float af = (float)a;
+    int32_t bits;
+    memcpy(&bits, &af, 4);
+    int32_t c = (int32_t)(((int64_t)(k + 1) * 0x3F800000LL) / k);
+    int32_t xb = c - bits / k;
+    float x;
+    memcpy(&x, &xb, 4);
+    const float rk = 1.0f / (float)k;
+    for (int it = 0; it < 4; it++) {
+        float xk = x;
+        for (int j = 1; j < k; j++)
+            xk = xk * x;
+        float r = fmaf(-af, xk, 1.0f);
+        x = fmaf(x * r, rk, x);
+    }
+    double xd = (double)x;
+    for (int it = 0; it < 2; it++) {
+        double xk = xd;
+        for (int j = 1; j < k; j++)
+            xk = xk * xd;
+        double r = fma(-a, xk, 1.0);
+        xd = fma(xd * r, 1.0 / k, xd);
+    }
+    return xd;
+}
+
+/* default_step_adjuster::decrease_step / increase_step */
+static double decrease_step(double dt, double err, int error_order, int pow_mode)
+{
+    double f = 9.0 / 10.0 * inv_root(err, error_order - 1, pow_mode);
     double lo = 1.0 / 5.0;
     return dt * (f > lo ? f : lo);
 }
 
-static double increase_step(double dt, double err, int stepper_order)
+static double increase_step(double dt, double err, int stepper_order, int pow_mode)
 {
     if (err < 0.5) {
-        double floor_ = pow(5.0, -(double)stepper_order);
+        /* pow(5.0, -5.0): 5^-5 = 1/3125 rounded */
+        double floor_ = stepper_order == 5 ? 1.0 / 3125.0 : pow(5.0, -(double)stepper_order);
         if (err < floor_)
             err = floor_;
-        dt *= 9.0 / 10.0 * pow(err, -1.0 / stepper_order);
+        dt *= 9.0 / 10.0 * inv_root(err, stepper_order, pow_mode);
     }
     return dt;
 }
@@ -349,12 +390,12 @@ int orc_forward(const orc_problem *pb, const double *y0, const double *p, double
                 break;
             }
             if (err > 1.0) {
-                dt = decrease_step(dt, err, T.error_order);
+                dt = decrease_step(dt, err, T.error_order, pb->pow_mode);
                 ok = 0;
                 rej++;
             } else {
                 t += dt;
-                dt = increase_step(dt, err, T.stepper_order);
+                dt = increase_step(dt, err, T.stepper_order, pb->pow_mode);
                 memcpy(y, out, sizeof(double) * n);
                 if (T.fsal)
                     memcpy(dxdt, dxdt_new, sizeof(double) * n);

@@ -72,6 +72,9 @@ typedef struct {
     double dt0;    /* initial step                            */
     long max_steps;/* accepted-step capacity                  */
     int max_fail;  /* consecutive failed attempts (odeint 500) */
+    int pow_mode;  /* step-size factor err^(-1/k): 0 = fixed IEEE-only Newton
+                      scheme shared with the CUDA library (bit-comparable),
+                      1 = the C library's pow (as odeint's std::pow) */
 } orc_problem;
 
 /* Right-hand side and vector-Jacobian product of the built-in models. */

@@ -33,6 +33,7 @@ class Problem(ctypes.Structure):
         ("dt0", ctypes.c_double),
         ("max_steps", ctypes.c_long),
         ("max_fail", ctypes.c_int),
+        ("pow_mode", ctypes.c_int),
     ]
 
 
@@ -77,8 +78,10 @@ def _d(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-def problem(model, tableau, n, npar, atol, rtol, dt0=1e-3, max_steps=200000, max_fail=500):
-    return Problem(MODEL[model], TABLEAU[tableau], n, npar, atol, rtol, dt0, max_steps, max_fail)
+def problem(model, tableau, n, npar, atol, rtol, dt0=1e-3, max_steps=200000, max_fail=500, pow_mode=0):
+    """pow_mode 0: the IEEE-only step-factor power shared with the CUDA library
+    (bit-comparable step sequences); 1: the C library's pow, as odeint calls it."""
+    return Problem(MODEL[model], TABLEAU[tableau], n, npar, atol, rtol, dt0, max_steps, max_fail, pow_mode)
 
 
 def forward(pb, y0, p, t0, t1, cap=None):

@@ -1,11 +1,17 @@
 """GPU parity through the C ABI against the CPU oracle.
 
-FP64 path (the drop-in): per instance the same accepted-step count, the
-accepted (t_n, y_n) within 1e-12 relative, y(T) within 1e-12 and gradients
-within 1e-9 relative (tolerances of the drop-in contract; the GPU contracts
-products into FMAs, the oracle does not, so results agree to rounding, not
-bit for bit).  Mixed path: gradient error against the FP64 oracle stated per
-config.
+FP64 path (the drop-in): the CUDA FP64 sweeps are built without FMA
+contraction and evaluate every expression in the oracle's order, and both
+compute the controller's err^(-1/k) with the same IEEE-only scheme, so the
+accepted-step sequence (count, t_n, h_n, y_n), y(T) and the gradients are
+compared BIT FOR BIT.  Against the oracle's libm-pow mode (odeint calls
+std::pow), the last-bit differences of some step factors are amplified by the
+error estimate's cancellation into ~1e-9 relative differences of later h_n;
+gradients then agree to 1e-9 relative.
+
+Reduced precision: gradient error against the FP64 oracle, relative to the
+instance's gradient scale with a floor of 1e-8 max|y0| (damped oscillators
+decay to |y(T)| << 1e-10, where no precision gives relative digits).
 """
 import numpy as np
 import pytest
@@ -16,25 +22,16 @@ from vectorizedadjoint_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
-REL_Y = 1e-12
-REL_G = 1e-9
-
 
 def dev(a, dtype=torch.float64):
     return torch.tensor(np.ascontiguousarray(a), dtype=dtype, device="cuda")
 
 
-def rel_err(a, b, floor=1e-12):
-    a, b = np.asarray(a), np.asarray(b)
-    scale = np.maximum(np.abs(b), floor)
-    return float(np.max(np.abs(a - b) / scale)) if a.size else 0.0
-
-
-def grad_rel(a, b):
-    """max |a-b| / max|b| per instance (gradient components share a scale)."""
-    a, b = np.atleast_2d(a), np.atleast_2d(b)
-    s = np.maximum(np.abs(b).max(axis=1, keepdims=True), 1e-300)
-    return float(np.max(np.abs(a - b) / s))
+def grad_rel(a, b, floor=0.0):
+    """max |a-b| / max(max|b|, floor) for one instance."""
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    s = max(np.abs(b).max(), floor, 1e-300)
+    return float(np.max(np.abs(a - b)) / s)
 
 
 def run_gpu(name, B, precision="fp64", **kw):
@@ -48,32 +45,34 @@ def run_gpu(name, B, precision="fp64", **kw):
     return s, w, res
 
 
-def oracle_batch(oracle, w, idx):
+def oracle_runs(oracle, w, idx, pow_mode=0):
     c = w["cfg"]
-    pb = oracle.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"])
+    pb = oracle.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"], pow_mode=pow_mode)
     return pb, [oracle.gradient(pb, c["cost"], w["y0"][b], w["params"][b], 0.0, w["t1"][b]) for b in idx]
 
 
-@pytest.mark.parametrize("name,B", [("vdp1", 1), ("dho", 256), ("vdpb", 512)])
-def test_fp64_gradients_match_oracle(oracle, cuda, name, B):
+CASES = [("vdp1", 1), ("dho", 256), ("vdpb", 512), ("glv10", 96)]
+
+
+@pytest.mark.parametrize("name,B", CASES)
+def test_fp64_bit_exact_with_oracle(oracle, cuda, name, B):
+    """Step counts, y(T) and gradients identical to the oracle's bits."""
     s, w, r = run_gpu(name, B)
     assert (r["status"] == 0).all()
-    idx = list(range(0, B, max(1, B // 64)))
-    pb, ref = oracle_batch(oracle, w, idx)
+    idx = list(range(0, B, max(1, B // 48)))
+    _, ref = oracle_runs(oracle, w, idx)
     for b, g in zip(idx, ref):
         assert g["status"] == 0
-        assert int(r["n_acc"][b]) == g["n_acc"], (b, int(r["n_acc"][b]), g["n_acc"])
-        # relative to the trajectory's scale: a decayed oscillator ends near 0
-        yscale = max(np.abs(w["y0"][b]).max(), np.abs(g["yT"]).max())
-        assert np.abs(r["yT"][b] - g["yT"]).max() / yscale < REL_Y * 100, b
-        assert grad_rel(r["dy0"][b], g["dy0"]) < REL_G, b
-        assert grad_rel(r["dp"][b], g["dp"]) < REL_G, b
+        assert int(r["n_acc"][b]) == g["n_acc"], b
+        np.testing.assert_array_equal(r["yT"][b], g["yT"], err_msg=f"y(T) instance {b}")
+        np.testing.assert_array_equal(r["dy0"][b], g["dy0"], err_msg=f"dy0 instance {b}")
+        np.testing.assert_array_equal(r["dp"][b], g["dp"], err_msg=f"dp instance {b}")
     s.close()
 
 
-@pytest.mark.parametrize("name,B", [("vdp1", 1), ("dho", 64), ("vdpb", 64)])
+@pytest.mark.parametrize("name,B", [("vdp1", 1), ("dho", 64), ("vdpb", 64), ("glv10", 32)])
 def test_fp64_accepted_step_sequence(oracle, cuda, name, B):
-    """Same accepted steps: count, t_n (hence h_n) and y_n within 1e-12 relative."""
+    """The checkpointed (t_n, dt_n, y_n) equal the oracle's, bit for bit."""
     w = W.make(name, batch=B)
     c = w["cfg"]
     s = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision="fp64",
@@ -81,27 +80,40 @@ def test_fp64_accepted_step_sequence(oracle, cuda, name, B):
     f = s.forward(dev(w["y0"]), dev(w["params"]), dev(w["t0"]), dev(w["t1"]))
     torch.cuda.synchronize()
     pb = oracle.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"])
-    worst_t = worst_y = 0.0
+    n_rej = f["n_rej"].cpu().numpy()
     for b in range(0, B, max(1, B // 16)):
         fw = oracle.forward(pb, w["y0"][b], w["params"][b], 0.0, w["t1"][b])
         t, dt, y = s.trajectory(b)
         assert len(t) == fw["n_acc"] + 1
-        h_gpu, h_ref = np.diff(t), np.diff(fw["times"])
-        worst_t = max(worst_t, rel_err(h_gpu, h_ref))
-        scale = np.maximum(np.abs(fw["states"]), 1e-3)
-        worst_y = max(worst_y, float(np.max(np.abs(y - fw["states"]) / scale)))
-        assert int(f["n_rej"][b]) == fw["n_rej"]
-    # h_n = t_{n+1} - t_n inherits the absolute error of t, so compare on t's scale
-    assert worst_t < 1e-9, worst_t
-    assert worst_y < 1e-11, worst_y
+        np.testing.assert_array_equal(t, fw["times"])
+        np.testing.assert_array_equal(dt[:-1], fw["dt_trial"])
+        np.testing.assert_array_equal(y, fw["states"])
+        assert int(n_rej[b]) == fw["n_rej"]
     s.close()
 
 
-def test_forward_backward_pair_equals_gradient(oracle, cuda):
+@pytest.mark.parametrize("name,B", [("vdp1", 1), ("dho", 64), ("vdpb", 64), ("glv10", 16)])
+def test_fp64_vs_libm_pow_controller(oracle, cuda, name, B):
+    """Against the oracle with the C library's pow (odeint's std::pow): same
+    step counts on (nearly) all instances, gradients within 1e-9 relative."""
+    s, w, r = run_gpu(name, B)
+    idx = list(range(0, B, max(1, B // 16)))
+    _, ref = oracle_runs(oracle, w, idx, pow_mode=1)
+    same = 0
+    for b, g in zip(idx, ref):
+        floor = 1e-8 * np.abs(w["y0"][b]).max()
+        if int(r["n_acc"][b]) == g["n_acc"]:
+            same += 1
+            assert grad_rel(r["dy0"][b], g["dy0"], floor) < 1e-9, b
+            assert grad_rel(r["dp"][b], g["dp"], floor) < 1e-9, b
+    assert same >= 0.9 * len(idx)
+    s.close()
+
+
+def test_forward_backward_pair_equals_gradient(cuda):
     """va_forward + va_backward with explicit seeds == va_gradient (cost sumsq)."""
     B = 128
     w = W.make("dho", batch=B)
-    c = w["cfg"]
     s = Solver("dho", 2, 2, B, tableau="ck54", atol=1e-8, rtol=1e-8)
     P = dev(w["params"])
     f = s.forward(dev(w["y0"]), P, dev(w["t0"]), dev(w["t1"]))
@@ -116,37 +128,58 @@ def test_forward_backward_pair_equals_gradient(oracle, cuda):
     s2.close()
 
 
-def test_multi_cost_seeds(oracle, cuda):
-    """nout > 1 (the reference's seed lanes): each row equals the oracle's."""
-    B, Q = 32, 3
-    w = W.make("vdpb", batch=B)
-    s = Solver("vdp", 2, 1, B, nout=Q, tableau="dopri5", atol=1e-6, rtol=1e-6)
+@pytest.mark.parametrize("name,B,Q", [("vdpb", 32, 3), ("glv10", 8, 10)])
+def test_multi_cost_seeds(oracle, cuda, name, B, Q):
+    """nout > 1 cost rows (the reference's seed lanes, identity seeds in its GLV
+    example): each row equals the oracle's, bit for bit."""
+    w = W.make(name, batch=B)
+    c = w["cfg"]
+    s = Solver(c["model"], c["n"], c["npar"], B, nout=Q, tableau=c["tableau"], atol=c["tol"], rtol=c["tol"])
     P = dev(w["params"])
     s.forward(dev(w["y0"]), P, dev(w["t0"]), dev(w["t1"]))
     rng = np.random.default_rng(3)
-    lam = rng.normal(size=(B, Q, 2))
-    mu = rng.normal(size=(B, Q, 1))
+    lam = rng.normal(size=(B, Q, c["n"]))
+    mu = rng.normal(size=(B, Q, c["npar"]))
     bw = s.backward(P, dev(lam), dev(mu))
     torch.cuda.synchronize()
     dy0, dp = bw["dy0"].cpu().numpy(), bw["dp"].cpu().numpy()
-    pb = oracle.problem("vdp", "dopri5", 2, 1, 1e-6, 1e-6)
-    for b in range(0, B, 5):
+    pb = oracle.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"])
+    for b in range(0, B, 3):
         fw = oracle.forward(pb, w["y0"][b], w["params"][b], 0.0, w["t1"][b])
         L, M, st = oracle.adjoint(pb, w["params"][b], fw["times"], fw["states"], lam[b], mu[b])
-        assert grad_rel(dy0[b], L) < REL_G
-        assert grad_rel(dp[b], M) < REL_G
+        np.testing.assert_array_equal(dy0[b], L)
+        np.testing.assert_array_equal(dp[b], M)
     s.close()
 
 
 def test_deterministic_repeat(cuda):
-    """No atomics on the result path: two runs are bitwise equal."""
-    s, w, r1 = run_gpu("vdpb", 4096)
+    """No atomics on the result path: two runs are bitwise equal (mixed_dw)."""
+    s, w, r1 = run_gpu("vdpb", 4096, precision="mixed_dw")
     c = w["cfg"]
     out = s.gradient(c["cost"], dev(w["y0"]), dev(w["params"]), dev(w["t0"]), dev(w["t1"]))
     torch.cuda.synchronize()
     np.testing.assert_array_equal(out["dp"].cpu().numpy(), r1["dp"])
     np.testing.assert_array_equal(out["dy0"].cpu().numpy(), r1["dy0"])
     s.close()
+
+
+def test_graph_replay_on_side_stream(cuda):
+    """va_gradient on a non-default stream captures both sweeps in a CUDA graph;
+    replays give the direct-launch results."""
+    B = 512
+    w = W.make("vdpb", batch=B)
+    s0, _, r = run_gpu("vdpb", B)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        s = Solver("vdp", 2, 1, B, atol=1e-6, rtol=1e-6)
+        args = [dev(w["y0"]), dev(w["params"]), dev(w["t0"]), dev(w["t1"])]
+        out = s.gradient("sumsq", *args)
+        for _ in range(3):
+            out = s.gradient("sumsq", *args, out=out)
+        side.synchronize()
+    np.testing.assert_array_equal(out["dp"].cpu().numpy(), r["dp"])
+    s.close()
+    s0.close()
 
 
 def test_host_entry_point_matches_device(cuda):
@@ -159,31 +192,35 @@ def test_host_entry_point_matches_device(cuda):
     s.close()
 
 
-@pytest.mark.parametrize("name,B,bound", [("vdp1", 1, 1e-5), ("dho", 256, 1e-5), ("vdpb", 512, 1e-4)])
-def test_mixed_precision_error_vs_fp64(oracle, cuda, name, B, bound):
-    """Plain FP32 stages/VJPs (FP64 controller and accumulators): median
-    gradient error against the FP64 oracle, bounded per config."""
-    s, w, r = run_gpu(name, B, precision="mixed")
-    assert (r["status"] == 0).all()
-    idx = list(range(0, B, max(1, B // 32)))
-    pb, ref = oracle_batch(oracle, w, idx)
-    errs = [max(grad_rel(r["dy0"][b], g["dy0"]), grad_rel(r["dp"][b], g["dp"])) for b, g in zip(idx, ref)]
-    assert np.median(errs) < bound, (np.median(errs), max(errs))
-    s.close()
-
-
-@pytest.mark.parametrize("name,B", [("vdp1", 1), ("dho", 256), ("vdpb", 512)])
+@pytest.mark.parametrize("name,B", [("vdp1", 1), ("dho", 256), ("vdpb", 512), ("glv10", 96)])
 def test_mixed_dw_error_vs_fp64(oracle, cuda, name, B):
     """Double-word stages/VJPs on the FP32 pipe: gradient error against the FP64
-    oracle at most 1e-6 for every instance (the mixed-path target), median
-    below 1e-9, and the same accepted-step counts."""
+    oracle at most 1e-6 for every instance (the mixed-path target)."""
     s, w, r = run_gpu(name, B, precision="mixed_dw")
     assert (r["status"] == 0).all()
     idx = list(range(0, B, max(1, B // 32)))
-    pb, ref = oracle_batch(oracle, w, idx)
-    errs = [max(grad_rel(r["dy0"][b], g["dy0"]), grad_rel(r["dp"][b], g["dp"])) for b, g in zip(idx, ref)]
+    _, ref = oracle_runs(oracle, w, idx)
+    errs = []
+    for b, g in zip(idx, ref):
+        floor = 1e-8 * np.abs(w["y0"][b]).max()
+        errs.append(max(grad_rel(r["dy0"][b], g["dy0"], floor), grad_rel(r["dp"][b], g["dp"], floor)))
     assert max(errs) <= 1e-6, (np.median(errs), max(errs))
     assert np.median(errs) < 1e-9, np.median(errs)
-    same = [int(r["n_acc"][b]) == g["n_acc"] for b, g in zip(idx, ref)]
-    assert np.mean(same) >= 0.95
+    s.close()
+
+
+@pytest.mark.parametrize("name,B,bound", [("vdp1", 1, 1e-5), ("dho", 256, 1e-4), ("vdpb", 512, 1e-4),
+                                          ("glv10", 96, 1e-4)])
+def test_mixed_fp32_error_vs_fp64(oracle, cuda, name, B, bound):
+    """Plain FP32 stages/VJPs (FP64 controller and accumulators): median
+    gradient error against the FP64 oracle below a per-config bound."""
+    s, w, r = run_gpu(name, B, precision="mixed")
+    assert (r["status"] == 0).all()
+    idx = list(range(0, B, max(1, B // 32)))
+    _, ref = oracle_runs(oracle, w, idx)
+    errs = []
+    for b, g in zip(idx, ref):
+        floor = 1e-8 * np.abs(w["y0"][b]).max()
+        errs.append(max(grad_rel(r["dy0"][b], g["dy0"], floor), grad_rel(r["dp"][b], g["dp"], floor)))
+    assert np.median(errs) < bound, (np.median(errs), max(errs))
     s.close()

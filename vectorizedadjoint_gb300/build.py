@@ -36,7 +36,9 @@ def build(verbose=False):
         obj = os.path.join(OUT_DIR, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if _stale(obj, src):
-            cmd = [NVCC, *FLAGS, "-c", src, "-o", obj]
+            # FP64 sweeps: no FMA contraction, so they round like the oracle
+            extra = ["-fmad=false"] if src.endswith("_fp64.cu") else []
+            cmd = [NVCC, *FLAGS, *extra, "-c", src, "-o", obj]
             if verbose:
                 print(" ".join(cmd))
             procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))

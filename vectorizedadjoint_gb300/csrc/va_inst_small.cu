@@ -1,50 +1,54 @@
-// Kernel instantiations for the one-thread-per-instance models.
+// Kernel tables of the one-thread-per-instance models.  This unit holds the
+// reduced-precision sweeps (float and double-word stages); the FP64 sweeps
+// come from va_inst_small_fp64.cu, which is built without FMA contraction.
 #include "va_kernels.cuh"
 #include "va_models.cuh"
 #include "va_registry.h"
 
 namespace va {
 
+void fill_fp64_vdp(KernelSet &k);
+void fill_fp64_vdp_petsc(KernelSet &k);
+void fill_fp64_dho(KernelSet &k);
+void fill_fp64_decay(KernelSet &k);
+
 template <class M>
-static KernelSet make_set()
+static KernelSet make_set(void (*fill_fp64)(KernelSet &))
 {
     KernelSet k{};
     k.N = M::N;
     k.P = M::P;
     k.tpi = 1;
-    k.fwd[0][0] = (const void *)forward_kernel<M, TabDopri5, double>;
+    fill_fp64(k);
     k.fwd[0][1] = (const void *)forward_kernel<M, TabDopri5, float>;
-    k.fwd[1][0] = (const void *)forward_kernel<M, TabCK54, double>;
     k.fwd[1][1] = (const void *)forward_kernel<M, TabCK54, float>;
     k.fwd[0][2] = (const void *)forward_kernel<M, TabDopri5, dword>;
     k.fwd[1][2] = (const void *)forward_kernel<M, TabCK54, dword>;
+    k.bwd[0][1] = (const void *)backward_kernel<M, TabDopri5, float>;
+    k.bwd[1][1] = (const void *)backward_kernel<M, TabCK54, float>;
     k.bwd[0][2] = (const void *)backward_kernel<M, TabDopri5, dword>;
     k.bwd[1][2] = (const void *)backward_kernel<M, TabCK54, dword>;
-    k.bwd[0][0] = (const void *)backward_kernel<M, TabDopri5, double>;
-    k.bwd[0][1] = (const void *)backward_kernel<M, TabDopri5, float>;
-    k.bwd[1][0] = (const void *)backward_kernel<M, TabCK54, double>;
-    k.bwd[1][1] = (const void *)backward_kernel<M, TabCK54, float>;
     return k;
 }
 
 const KernelSet *kernels_vdp()
 {
-    static const KernelSet k = make_set<ModelVdP>();
+    static const KernelSet k = make_set<ModelVdP>(fill_fp64_vdp);
     return &k;
 }
 const KernelSet *kernels_vdp_petsc()
 {
-    static const KernelSet k = make_set<ModelVdPPetsc>();
+    static const KernelSet k = make_set<ModelVdPPetsc>(fill_fp64_vdp_petsc);
     return &k;
 }
 const KernelSet *kernels_dho()
 {
-    static const KernelSet k = make_set<ModelDHO>();
+    static const KernelSet k = make_set<ModelDHO>(fill_fp64_dho);
     return &k;
 }
 const KernelSet *kernels_decay()
 {
-    static const KernelSet k = make_set<ModelDecay>();
+    static const KernelSet k = make_set<ModelDecay>(fill_fp64_decay);
     return &k;
 }
 

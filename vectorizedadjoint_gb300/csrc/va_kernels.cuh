@@ -19,6 +19,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 #include <type_traits>
 
 #include "va_dword.cuh"
@@ -104,7 +105,9 @@ __host__ __device__ __forceinline__ S from_d(double v)
 __host__ __device__ __forceinline__ double to_d(double v) { return v; }
 __host__ __device__ __forceinline__ double to_d(float v) { return (double)v; }
 __host__ __device__ __forceinline__ double to_d(dword v) { return (double)v; }
-// a * b + c
+// a * b + c (for double: fused only where the translation unit contracts;
+// the FP64 kernels are built without contraction)
+__host__ __device__ __forceinline__ double madd(double a, double b, double c) { return a * b + c; }
 __host__ __device__ __forceinline__ float madd(float a, float b, float c) { return fmaf(a, b, c); }
 __host__ __device__ __forceinline__ dword madd(dword a, dword b, dword c) { return a * b + c; }
 template <class S>
@@ -120,29 +123,66 @@ __host__ __device__ __forceinline__ float fromf<float>(float v)
 
 // ---------------------------------------------------------------- controller
 
-// a^(-1/K) for a > 0 in FP64 without a double-precision pow (FP64 issues at
-// 1/61 of the FP32 rate on this part): an FP32 seed, then two steps of
-// Newton's iteration for the inverse K-th root, x <- x + x (1 - a x^K) / K,
-// which converges quadratically (seed error ~1e-7 -> ~1e-14 -> rounding).
-// Inputs beyond the FP32 range seed x = 0 (a huge) or inf (a tiny); callers
-// only pass a in [5^-5, 0.5) (increase) or a > 1 (decrease, where x = 0
-// lands on the 0.2 limiter exactly as pow would).
+__host__ __device__ __forceinline__ int32_t f32_bits(float f)
+{
+#ifdef __CUDA_ARCH__
+    return __float_as_int(f);
+#else
+    int32_t i;
+    memcpy(&i, &f, 4);
+    return i;
+#endif
+}
+__host__ __device__ __forceinline__ float f32_from_bits(int32_t i)
+{
+#ifdef __CUDA_ARCH__
+    return __int_as_float(i);
+#else
+    float f;
+    memcpy(&f, &i, 4);
+    return f;
+#endif
+}
+
+// a^(-1/K) for the step-size controller, without a double-precision pow
+// (FP64 issues at 1/61 of the FP32 rate on this part).  Newton's iteration
+// for the inverse K-th root, x <- x + x (1 - a x^K) / K, from a seed built on
+// the float bit pattern (log2 read off the exponent field and scaled by
+// -1/K, the idea of the classic fast inverse square root): four FP32 steps
+// (seed error ~6% -> ~1e-7), two FP64 steps (-> ~1e-14 -> rounding).  Only
+// IEEE adds, multiplies and fused multiply-adds, in a fixed order: the
+// result has the same bits on any IEEE machine, which the oracle relies on
+// for a bit-exact comparison of step sequences.  a >= 1e30 (decrease only)
+// returns 0, which the 0.2 limiter turns into the same factor pow would.
 template <int K>
 __host__ __device__ __forceinline__ double inv_root(double a)
 {
-    double x = (double)powf((float)a, -1.0f / (float)K);
-    if (!(x > 0.0) || !isfinite(x))
-        return x;
+    if (!(a < 1e30))
+        return 0.0;
+    const float af = (float)a;
+    constexpr int32_t c = (int32_t)(((int64_t)(K + 1) * 0x3F800000LL) / K);
+    float x = f32_from_bits(c - f32_bits(af) / K);
+    const float rk = 1.0f / (float)K;
 #pragma unroll
-    for (int it = 0; it < 2; it++) {
-        double xk = x;
+    for (int it = 0; it < 4; it++) {
+        float xk = x;
 #pragma unroll
         for (int k = 1; k < K; k++)
-            xk *= x;
-        const double r = fma(-a, xk, 1.0);
-        x = fma(x * r, 1.0 / K, x);
+            xk = xk * x;
+        const float r = fmaf(-af, xk, 1.0f);
+        x = fmaf(x * r, rk, x);
     }
-    return x;
+    double xd = (double)x;
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        double xk = xd;
+#pragma unroll
+        for (int k = 1; k < K; k++)
+            xk = xk * xd;
+        const double r = fma(-a, xk, 1.0);
+        xd = fma(xd * r, 1.0 / K, xd);
+    }
+    return xd;
 }
 
 // odeint default_step_adjuster::decrease_step:
@@ -285,8 +325,21 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
             e[i] = dt * to_d(acc);
         }
     }
-    // max-norm with a single division: keep the largest ratio as a fraction
     const double adt = fabs(dt);
+    if constexpr (std::is_same<S, double>::value) {
+        // odeint's rel_error + norm_inf: one quotient per component, then max
+        double m = 0.0;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const double r = fabs(e[i]) / (atol + rtol * (1.0 * fabs(y[i]) + adt * fabs(k0[i])));
+            if (r != r)
+                return r;
+            if (r > m)
+                m = r;
+        }
+        return m;
+    }
+    // reduced paths: max-norm with one division, the largest ratio kept as a fraction
     double num = fabs(e[0]);
     double den = atol + rtol * (1.0 * fabs(y[0]) + adt * fabs(to_d(k0[0])));
 #pragma unroll
@@ -528,9 +581,9 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
 template <class M, class Tab, class S>
 __host__ __device__ __forceinline__ void back_step(const double (&y)[M::N], double tn, double h,
                                           const S (&p)[M::P], double (&lam)[M::N],
-                                          double (&mu)[M::P])
+                                          double (&mu)[M::PG])
 {
-    constexpr int N = M::N, P = M::P, NS = Tab::S;
+    constexpr int N = M::N, P = M::PG, NS = Tab::S;
     S K[NS][N];
     S X[NS][N];
     // recompute the stages from y_n (compute_intermediate_states, :24-64)

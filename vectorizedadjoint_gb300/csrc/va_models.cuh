@@ -1,5 +1,5 @@
 // Right-hand sides and hand-written vector-Jacobian products of the built-in
-// models.  They take the place of the user functor the reference records
+// models (N states, P parameters read by the RHS, PG parameter gradients).  They take the place of the user functor the reference records
 // with AADC (lib/include/AadData.hpp:124-171) and of the JIT reverse code it
 // replays in AadData::VectorTimesJacobians (AadData.hpp:291-330): every
 // model gives f(x, p, t) and (J_x^T w, J_p^T w) at the same point.
@@ -14,7 +14,7 @@ namespace va {
 
 // Van der Pol, Lienard form: x0' = x1, x1' = mu (1 - x0^2) x1 - x0.  p = (mu).
 struct ModelVdP {
-    static constexpr int N = 2, P = 1;
+    static constexpr int N = 2, P = 1, PG = 1;
     template <class S>
     __host__ __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
     {
@@ -36,7 +36,7 @@ struct ModelVdP {
 // Van der Pol as in the reference example (examples/VanDerPol/main.cpp:41-42):
 // x0' = x1, x1' = mu ((1 - x0^2) x1 - x0).
 struct ModelVdPPetsc {
-    static constexpr int N = 2, P = 1;
+    static constexpr int N = 2, P = 1, PG = 1;
     template <class S>
     __host__ __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
     {
@@ -60,7 +60,7 @@ struct ModelVdPPetsc {
 // examples/HarmonicOscillator/main.cpp:11-30 uses fixed k = 1 and a friction
 // parameter; this is the (omega, zeta) form of the same family.)
 struct ModelDHO {
-    static constexpr int N = 2, P = 2;
+    static constexpr int N = 2, P = 2, PG = 2;
     template <class S>
     __host__ __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
     {
@@ -83,7 +83,7 @@ struct ModelDHO {
 // Exponential decay y' = -k y; p = (k).  Its discrete adjoint has a closed
 // form for a frozen step sequence, which the tests use.
 struct ModelDecay {
-    static constexpr int N = 1, P = 1;
+    static constexpr int N = 1, P = 1, PG = 1;
     template <class S>
     __host__ __device__ __forceinline__ static void rhs(const S *x, const S *p, S t, S *f)
     {
