@@ -154,6 +154,17 @@ VA_API va_status va_gradient_host(va_handle *h, int32_t cost, const double *y0, 
                            const double *t0, const double *t1, double *yT, double *dy0,
                            double *dparams, int32_t *n_acc, int32_t *status, void *stream);
 
+/* va_forward with HOST buffers (synchronous; device staging owned by the
+ * handle).  The single-instance C++ facade (va_driver.hpp) runs on this. */
+VA_API va_status va_forward_host(va_handle *h, const double *y0, const double *params,
+                                 const double *t0, const double *t1, double *yT, int32_t *n_acc,
+                                 int32_t *n_rej, int32_t *status);
+
+/* va_backward with HOST buffers (synchronous). */
+VA_API va_status va_backward_host(va_handle *h, const double *params, const double *lambdaT,
+                                  const double *mu_direct, double *dy0, double *dparams,
+                                  int32_t *status);
+
 /* Picks the block size and resident blocks per SM of both sweeps by timing
  * candidate launches on the given inputs (device pointers); the choice is
  * kept in the handle.  Runs forward+backward several times. */

@@ -55,7 +55,8 @@ struct va_handle {
     // staging buffers of the host entry point
     double *s_y0 = nullptr, *s_par = nullptr, *s_t0 = nullptr, *s_t1 = nullptr;
     double *s_yT = nullptr, *s_dy0 = nullptr, *s_dpar = nullptr;
-    int *s_nacc = nullptr, *s_status = nullptr;
+    int *s_nacc = nullptr, *s_status = nullptr, *s_nrej = nullptr;
+    double *s_lam = nullptr, *s_mu = nullptr;
 
     int fwd_block = 128, fwd_grid = 0, bwd_block = 128, bwd_grid = 0;
     bool forward_done = false;
@@ -161,6 +162,9 @@ va_status ensure_staging(va_handle *h)
     VA_CUDA(h, cudaMalloc(&h->s_dpar, B * Q * P * sizeof(double)));
     VA_CUDA(h, cudaMalloc(&h->s_nacc, B * sizeof(int)));
     VA_CUDA(h, cudaMalloc(&h->s_status, B * sizeof(int)));
+    VA_CUDA(h, cudaMalloc(&h->s_nrej, B * sizeof(int)));
+    VA_CUDA(h, cudaMalloc(&h->s_lam, B * Q * N * sizeof(double)));
+    VA_CUDA(h, cudaMalloc(&h->s_mu, B * Q * P * sizeof(double)));
     return VA_OK;
 }
 
@@ -361,7 +365,8 @@ va_status va_destroy(va_handle *h)
     drop_graph(h);
     void *ptrs[] = {h->pool_rec, h->chunk_prev, h->inst_T,  h->inst_last, h->inst_status,
                     h->ctl,      h->s_y0,       h->s_par,   h->s_t0,      h->s_t1,
-                    h->s_yT,     h->s_dy0,      h->s_dpar,  h->s_nacc,    h->s_status};
+                    h->s_yT,     h->s_dy0,      h->s_dpar,  h->s_nacc,    h->s_status,
+                    h->s_nrej,   h->s_lam,      h->s_mu};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -497,6 +502,66 @@ va_status va_gradient_host(va_handle *h, int32_t cost, const double *y0, const d
     if (status)
         VA_CUDA(h, cudaMemcpyAsync(status, h->s_status, B * sizeof(int), cudaMemcpyDeviceToHost, s));
     VA_CUDA(h, cudaStreamSynchronize(s));
+    return VA_OK;
+}
+
+va_status va_forward_host(va_handle *h, const double *y0, const double *params, const double *t0,
+                          const double *t1, double *yT, int32_t *n_acc, int32_t *n_rej, int32_t *status)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    if (!y0 || !params || !t0 || !t1)
+        return fail(h, VA_BAD_ARGS, "va_forward_host: null input pointer%s");
+    va_status st = ensure_staging(h);
+    if (st != VA_OK)
+        return st;
+    const size_t B = h->prob.batch, N = h->N, P = h->P;
+    VA_CUDA(h, cudaMemcpy(h->s_y0, y0, B * N * sizeof(double), cudaMemcpyHostToDevice));
+    VA_CUDA(h, cudaMemcpy(h->s_par, params, B * P * sizeof(double), cudaMemcpyHostToDevice));
+    VA_CUDA(h, cudaMemcpy(h->s_t0, t0, B * sizeof(double), cudaMemcpyHostToDevice));
+    VA_CUDA(h, cudaMemcpy(h->s_t1, t1, B * sizeof(double), cudaMemcpyHostToDevice));
+    st = va_forward(h, h->s_y0, h->s_par, h->s_t0, h->s_t1, h->s_yT, h->s_nacc, h->s_nrej, h->s_status,
+                    nullptr);
+    if (st != VA_OK)
+        return st;
+    VA_CUDA(h, cudaDeviceSynchronize());
+    if (yT)
+        VA_CUDA(h, cudaMemcpy(yT, h->s_yT, B * N * sizeof(double), cudaMemcpyDeviceToHost));
+    if (n_acc)
+        VA_CUDA(h, cudaMemcpy(n_acc, h->s_nacc, B * sizeof(int), cudaMemcpyDeviceToHost));
+    if (n_rej)
+        VA_CUDA(h, cudaMemcpy(n_rej, h->s_nrej, B * sizeof(int), cudaMemcpyDeviceToHost));
+    if (status)
+        VA_CUDA(h, cudaMemcpy(status, h->s_status, B * sizeof(int), cudaMemcpyDeviceToHost));
+    return VA_OK;
+}
+
+va_status va_backward_host(va_handle *h, const double *params, const double *lambdaT,
+                           const double *mu_direct, double *dy0, double *dparams, int32_t *status)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    if (!params || !lambdaT)
+        return fail(h, VA_BAD_ARGS, "va_backward_host: null input pointer%s");
+    va_status st = ensure_staging(h);
+    if (st != VA_OK)
+        return st;
+    const size_t B = h->prob.batch, N = h->N, P = h->P, Q = h->prob.nout;
+    VA_CUDA(h, cudaMemcpy(h->s_par, params, B * P * sizeof(double), cudaMemcpyHostToDevice));
+    VA_CUDA(h, cudaMemcpy(h->s_lam, lambdaT, B * Q * N * sizeof(double), cudaMemcpyHostToDevice));
+    if (mu_direct)
+        VA_CUDA(h, cudaMemcpy(h->s_mu, mu_direct, B * Q * P * sizeof(double), cudaMemcpyHostToDevice));
+    st = va_backward(h, h->s_par, h->s_lam, mu_direct ? h->s_mu : nullptr, h->s_dy0, h->s_dpar,
+                     h->s_status, nullptr);
+    if (st != VA_OK)
+        return st;
+    VA_CUDA(h, cudaDeviceSynchronize());
+    if (dy0)
+        VA_CUDA(h, cudaMemcpy(dy0, h->s_dy0, B * Q * N * sizeof(double), cudaMemcpyDeviceToHost));
+    if (dparams)
+        VA_CUDA(h, cudaMemcpy(dparams, h->s_dpar, B * Q * P * sizeof(double), cudaMemcpyDeviceToHost));
+    if (status)
+        VA_CUDA(h, cudaMemcpy(status, h->s_status, B * sizeof(int), cudaMemcpyDeviceToHost));
     return VA_OK;
 }
 
