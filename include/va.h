@@ -165,6 +165,34 @@ VA_API va_status va_backward_host(va_handle *h, const double *params, const doub
                                   const double *mu_direct, double *dy0, double *dparams,
                                   int32_t *status);
 
+/* Size of the fixed device array va_gradient_noalloc works in. */
+#define VA_NOALLOC_SCRATCH_BYTES (64u << 20)
+
+/* va_gradient without any allocation, for callers that may not allocate
+ * device memory while they run (e.g. a host whose device memory is owned by
+ * another runtime's caching allocator, or a plugin host that forbids
+ * allocation in callbacks).  No counterpart in the reference.  No handle:
+ * the problem and options are arguments; inputs and outputs are the
+ * caller's DEVICE buffers as for va_gradient (nout = 1; yT, n_acc, status
+ * may be NULL).  Models whose state fits one thread only: VA_MODEL_VDP,
+ * VA_MODEL_VDP_PETSC, VA_MODEL_DHO, VA_MODEL_DECAY.
+ * All scratch -- work counters, per-instance metadata and the checkpoint
+ * pool -- lives in one file-scope device array of VA_NOALLOC_SCRATCH_BYTES
+ * (64 MiB) that every GPU loading the library holds until exit.  A batch
+ * whose metadata plus one checkpoint chunk per instance does not fit is
+ * rejected with VA_BAD_ARGS before any GPU work; instances that outgrow the
+ * pool at run time report VA_CKPT_BUDGET in status.
+ * The first call on a device looks up the array's device address (with that
+ * device current): make it before any stream capture.  Calls share the
+ * array and it keeps the last call's contents; calls whose GPU work overlaps
+ * race on it. */
+VA_API va_status va_gradient_noalloc(int32_t model, int32_t tableau, int32_t precision,
+                                     double atol, double rtol, double dt0, int32_t max_steps,
+                                     int32_t max_rejects, int32_t cost, int32_t batch,
+                                     const double *y0, const double *params, const double *t0,
+                                     const double *t1, double *yT, double *dy0, double *dparams,
+                                     int32_t *n_acc, int32_t *status, void *stream);
+
 /* Picks the block size and resident blocks per SM of both sweeps by timing
  * candidate launches on the given inputs (device pointers); the choice is
  * kept in the handle.  Runs forward+backward several times. */

@@ -21,7 +21,8 @@ COSTS = {"seeds": -1, "sumsq": 0, "sum": 1}
 
 # Every symbol include/va.h declares (checked by the CPU test-suite).
 EXPORTS = ["va_default_options", "va_create", "va_destroy", "va_forward", "va_backward",
-           "va_gradient", "va_gradient_host", "va_forward_host", "va_backward_host", "va_autotune",
+           "va_gradient", "va_gradient_host", "va_forward_host", "va_backward_host", "va_gradient_noalloc",
+           "va_autotune",
            "va_get_launch", "va_checkpoint_info",
            "va_trajectory", "va_last_error", "va_status_string"]
 
@@ -70,6 +71,9 @@ def load():
     L.va_gradient_host.argtypes = [H, ctypes.c_int32, dp, dp, dp, dp, dp, dp, dp, ip, ip, vp]
     L.va_forward_host.argtypes = [H, dp, dp, dp, dp, dp, ip, ip, ip]
     L.va_backward_host.argtypes = [H, dp, dp, dp, dp, dp, ip]
+    i32, f64 = ctypes.c_int32, ctypes.c_double
+    L.va_gradient_noalloc.argtypes = [i32, i32, i32, f64, f64, f64, i32, i32, i32, i32,
+                                      dp, dp, dp, dp, dp, dp, dp, ip, ip, vp]
     L.va_autotune.argtypes = [H, ctypes.c_int32, dp, dp, dp, dp, vp]
     L.va_get_launch.argtypes = [H] + [ctypes.POINTER(ctypes.c_int32)] * 4
     L.va_checkpoint_info.argtypes = [H, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
