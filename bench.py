@@ -176,6 +176,11 @@ def main():
     ap.add_argument("--precision", default="mixed_dw", choices=["mixed_dw", "mixed", "fp64"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--quick", action="store_true",
+                    help="only the timed steps of one mode (no autotune sweep, other modes, plain, e2e or CPU "
+                         "legs): the small case used for ncu captures")
+    ap.add_argument("--batch", type=int, default=0, help="override the workload's batch size")
+    ap.add_argument("--budget-gb", type=float, default=0.0, help="checkpoint pool budget (GiB)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", 0))
@@ -202,14 +207,17 @@ def _bench(args, rank, world, local, torch, dist):
     from vectorizedadjoint_gb300 import Solver
     from vectorizedadjoint_gb300 import workloads as W
 
-    w = W.make(args.config)
+    w = W.make(args.config, batch=args.batch or None)
     c = w["cfg"]
     B = c["batch"]
+    if args.budget_gb > 0:
+        c["budget"] = int(args.budget_gb * (1 << 30))
     dev = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")
     y0, par, t0, t1 = dev(w["y0"]), dev(w["params"]), dev(w["t0"]), dev(w["t1"])
     s = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision=args.precision,
                atol=c["tol"], rtol=c["tol"], ckpt_budget_bytes=c.get("budget", 0))
-    s.autotune(c["cost"], y0, par, t0, t1)
+    if not args.quick:
+        s.autotune(c["cost"], y0, par, t0, t1)
     out = s.gradient(c["cost"], y0, par, t0, t1)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     stream = torch.cuda.current_stream()
@@ -237,6 +245,14 @@ def _bench(args, rank, world, local, torch, dist):
     status = out["status"].cpu().numpy()
     n_acc = out["n_acc"].cpu().numpy().astype(np.int64)
     value = world * B / (ms * 1e-3)
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": "adjoint gradients/s", "value": value, "unit": "gradients/s",
+                              "ms_per_step": ms, "quick": True, "precision": args.precision,
+                              "config": {"workload": args.config, "batch": B, "launch": s.launch()},
+                              "status_ok": int((status == 0).sum()), "clocks": clk.summary()}), flush=True)
+        s.close()
+        return
 
     # per-kernel timing (forward / backward launched separately) for the roofline
     lam = None
