@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
 
     int b = -1;
     double y[1], t = 0.0, t1 = 0.0, dt = 0.0;
-    S k0[1], p[P];
+    S ys[1], k0[1], p[P];
     int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
     bool at_top = true;
 
@@ -175,7 +175,8 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
         } else if (li == 0) {
             a.pool.chunk_prev[chunk] = -1;
         }
-        eval_rhs<M, S>(y, p, t, k0);
+        ys[0] = from_d<S>(y[0]);
+        M::template rhs<S>(ys, p, from_d<S>(t), k0);
         return true;
     };
 
@@ -257,25 +258,30 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
             at_top = false;
         }
         double ynew[1];
-        S knew[1];
-        const double err = group_max<G>(attempt<M, Tab, S>(y, k0, p, t, dt, a.atol, a.rtol, ynew, knew), mask);
+        S ynew_s[1], knew[1];
+        const double err = group_max<G>(
+            attempt<M, Tab, S>(y, ys, k0, p, t, dt, a.atol, a.rtol, ynew, ynew_s, knew), mask);
         bool ok;
         if (err != err) {
             status = ST_NONFINITE;
             continue;
         }
         if (err > 1.0) {
-            dt = decrease_step<Tab>(dt, err);
+            dt = decrease_step<Tab, S>(dt, err);
             rej++;
             ok = false;
         } else {
             t += dt;
-            dt = increase_step<Tab>(dt, err);
-            y[0] = ynew[0];
+            dt = increase_step<Tab, S>(dt, err);
+            ys[0] = ynew_s[0];
+            if constexpr (std::is_same<S, dword>::value)
+                y[0] = to_d(ynew_s[0]);
+            else
+                y[0] = ynew[0];
             if constexpr (Tab::FSAL)
                 k0[0] = knew[0];
             else
-                eval_rhs<M, S>(y, p, t, k0);
+                M::template rhs<S>(ys, p, from_d<S>(t), k0);
             ok = true;
         }
         if (fails >= a.max_fail) {

@@ -154,7 +154,7 @@ __host__ __device__ __forceinline__ float f32_from_bits(int32_t i)
 // result has the same bits on any IEEE machine, which the oracle relies on
 // for a bit-exact comparison of step sequences.  a >= 1e30 (decrease only)
 // returns 0, which the 0.2 limiter turns into the same factor pow would.
-template <int K>
+template <int K, int FP64_STEPS = 2>
 __host__ __device__ __forceinline__ double inv_root(double a)
 {
     if (!(a < 1e30))
@@ -174,7 +174,7 @@ __host__ __device__ __forceinline__ double inv_root(double a)
     }
     double xd = (double)x;
 #pragma unroll
-    for (int it = 0; it < 2; it++) {
+    for (int it = 0; it < FP64_STEPS; it++) {
         double xk = xd;
 #pragma unroll
         for (int k = 1; k < K; k++)
@@ -185,18 +185,26 @@ __host__ __device__ __forceinline__ double inv_root(double a)
     return xd;
 }
 
+// FP64 Newton steps of the step-factor root: two on the FP64 path (the
+// scheme the oracle shares), one on the reduced paths (~3e-14 relative,
+// far below the error estimate's own accuracy there).
+template <class S>
+struct RootSteps {
+    static constexpr int value = std::is_same<S, double>::value ? 2 : 1;
+};
+
 // odeint default_step_adjuster::decrease_step:
 //   dt *= max(0.9 err^(-1/(q-1)), 0.2)
-template <class Tab>
+template <class Tab, class S = double>
 __host__ __device__ __forceinline__ double decrease_step(double dt, double err)
 {
-    double f = 9.0 / 10.0 * inv_root<Tab::ERROR_ORDER - 1>(err);
+    double f = 9.0 / 10.0 * inv_root<Tab::ERROR_ORDER - 1, RootSteps<S>::value>(err);
     return dt * fmax(f, 1.0 / 5.0);
 }
 
 // odeint default_step_adjuster::increase_step:
 //   if err < 0.5: dt *= 0.9 max(err, 5^-p)^(-1/p)
-template <class Tab>
+template <class Tab, class S = double>
 __host__ __device__ __forceinline__ double increase_step(double dt, double err)
 {
     if (err < 0.5) {
@@ -204,20 +212,27 @@ __host__ __device__ __forceinline__ double increase_step(double dt, double err)
         constexpr double floor_err = 1.0 / 3125.0;
         static_assert(Tab::STEPPER_ORDER == 5, "floor constant assumes a fifth-order stepper");
         err = fmax(floor_err, err);
-        dt *= 9.0 / 10.0 * inv_root<Tab::STEPPER_ORDER>(err);
+        dt *= 9.0 / 10.0 * inv_root<Tab::STEPPER_ORDER, RootSteps<S>::value>(err);
     }
     return dt;
 }
 
 // ------------------------------------------------------------- stage algebra
 
+__host__ __device__ __forceinline__ double hi_of(double v) { return v; }
+__host__ __device__ __forceinline__ float hi_of(float v) { return v; }
+__host__ __device__ __forceinline__ float hi_of(dword v) { return v.hi; }
+
 // X_m = y + sum_{j<m} (a_mj dt) K_j, in the order odeint's scale_sum
 // evaluates it (and the reference recomputes it, backpropagation.hpp:36-45).
+// ys / sdt: y and dt in stage precision (unused on the FP64 path).
 template <class Tab, int N, class S>
-__host__ __device__ __forceinline__ void form_stage(int m, const double (&y)[N], const S (&K)[Tab::S][N],
-                                           double dt, S (&X)[N])
+__host__ __device__ __forceinline__ void form_stage(int m, const double (&y)[N], const S (&ys)[N],
+                                                   const S (&K)[Tab::S][N], double dt, S sdt, S (&X)[N])
 {
     if constexpr (std::is_same<S, double>::value) {
+        (void)ys;
+        (void)sdt;
 #pragma unroll
         for (int i = 0; i < N; i++) {
             double acc = y[i];
@@ -229,7 +244,8 @@ __host__ __device__ __forceinline__ void form_stage(int m, const double (&y)[N],
         }
     } else {
         // X = y + dt * sum_{j<m} a_mj K_j  (float or double-word stages)
-        const S sdt = from_d<S>(dt);
+        (void)y;
+        (void)dt;
 #pragma unroll
         for (int i = 0; i < N; i++) {
             S acc = S(0);
@@ -237,7 +253,7 @@ __host__ __device__ __forceinline__ void form_stage(int m, const double (&y)[N],
             for (int j = 0; j < Tab::S - 1; j++)
                 if (j < m)
                     acc = madd(S(Tab::a(m, j)), K[j][i], acc);
-            X[i] = madd(acc, sdt, from_d<S>(y[i]));
+            X[i] = madd(acc, sdt, ys[i]);
         }
     }
 }
@@ -246,20 +262,26 @@ __host__ __device__ __forceinline__ void form_stage(int m, const double (&y)[N],
 // y_new, k_new = f(y_new) (FSAL pairs) and the error norm
 // max_i |err_i| / (atol + rtol (|y_i| + |dt| |k0_i|))  (default_error_checker
 // with a_x = a_dxdt = 1, evaluated at the step start).
+// ys is y in stage precision.  Outputs: FP64 and double-word paths give
+// ynew_s (the new state in stage precision; FP64: = ynew); FP64 and float
+// paths give ynew in FP64.  The double-word path leaves ynew to the caller,
+// which rounds ynew_s to FP64 once per accepted step.
 template <class M, class Tab, class S>
-__host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], const S (&k0)[M::N],
-                                          const S (&p)[M::P], double t, double dt, double atol,
-                                          double rtol, double (&ynew)[M::N], S (&knew)[M::N])
+__host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], const S (&ys)[M::N],
+                                                   const S (&k0)[M::N], const S (&p)[M::P], double t,
+                                                   double dt, double atol, double rtol, double (&ynew)[M::N],
+                                                   S (&ynew_s)[M::N], S (&knew)[M::N])
 {
     constexpr int N = M::N, NS = Tab::S;
     S K[NS][N];
+    const S sdt = std::is_same<S, double>::value ? S(dt) : from_d<S>(dt);
 #pragma unroll
     for (int i = 0; i < N; i++)
         K[0][i] = k0[i];
 #pragma unroll
     for (int m = 1; m < NS; m++) {
         S X[N];
-        form_stage<Tab, N, S>(m, y, K, dt, X);
+        form_stage<Tab, N, S>(m, y, ys, K, dt, sdt, X);
         M::template rhs<S>(X, p, S(t + Tab::c(m) * dt), K[m]);
     }
     double e[N];
@@ -272,6 +294,7 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
                 if (Tab::b(j) != 0.0)
                     acc = acc + (Tab::b(j) * dt) * K[j][i];
             ynew[i] = acc;
+            ynew_s[i] = acc;
         }
         if constexpr (Tab::FSAL)
             M::template rhs<S>(ynew, p, t + dt, knew);
@@ -292,8 +315,7 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
         }
     } else {
         // y_new = y + dt * sum_j b_j K_j: an FP64 update of an FP32 increment
-        // (float stages) or a double-word sum rounded once to FP64.
-        const S sdt = from_d<S>(dt);
+        // (float stages) or a double-word sum (rounded to FP64 by the caller).
 #pragma unroll
         for (int i = 0; i < N; i++) {
             S acc = S(0);
@@ -301,18 +323,16 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
             for (int j = 0; j < NS; j++)
                 if (Tab::b(j) != 0.0)
                     acc = madd(S(Tab::b(j)), K[j][i], acc);
-            if constexpr (std::is_same<S, float>::value)
+            if constexpr (std::is_same<S, float>::value) {
                 ynew[i] = fma(dt, (double)acc, y[i]);
-            else
-                ynew[i] = to_d(madd(acc, sdt, from_d<S>(y[i])));
+                ynew_s[i] = (float)ynew[i];
+            } else {
+                ynew_s[i] = madd(acc, sdt, ys[i]);
+            }
         }
-        if constexpr (Tab::FSAL) {
-            S ys[N];
-#pragma unroll
-            for (int i = 0; i < N; i++)
-                ys[i] = from_d<S>(ynew[i]);
-            M::template rhs<S>(ys, p, from_d<S>(t + dt), knew);
-        }
+        if constexpr (Tab::FSAL)
+            M::template rhs<S>(ynew_s, p, from_d<S>(t + dt), knew);
+        // error vector to FP64 from the leading word: an estimate needs no more
 #pragma unroll
         for (int i = 0; i < N; i++) {
             S acc = S(0);
@@ -322,7 +342,7 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
                     acc = madd(S(Tab::e(j)), K[j][i], acc);
             if constexpr (Tab::FSAL)
                 acc = madd(S(Tab::E_NEW), knew[i], acc);
-            e[i] = dt * to_d(acc);
+            e[i] = dt * (double)hi_of(acc);
         }
     }
     const double adt = fabs(dt);
@@ -341,11 +361,11 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
     }
     // reduced paths: max-norm with one division, the largest ratio kept as a fraction
     double num = fabs(e[0]);
-    double den = atol + rtol * (1.0 * fabs(y[0]) + adt * fabs(to_d(k0[0])));
+    double den = atol + rtol * (1.0 * fabs(y[0]) + adt * fabs((double)hi_of(k0[0])));
 #pragma unroll
     for (int i = 1; i < N; i++) {
         double ni = fabs(e[i]);
-        double di = atol + rtol * (1.0 * fabs(y[i]) + adt * fabs(to_d(k0[i])));
+        double di = atol + rtol * (1.0 * fabs(y[i]) + adt * fabs((double)hi_of(k0[i])));
         if (ni * den > num * di || ni != ni) {
             num = ni;
             den = di;
@@ -420,7 +440,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
 
     int b = -1;
     double y[N], t = 0.0, t1 = 0.0, dt = 0.0;
-    S k0[N], p[P];
+    S ys[N], k0[N], p[P]; // ys: y in stage precision, carried across steps
     int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
     bool at_top = true;
 
@@ -452,7 +472,10 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
         }
         // k_1 = f(y_0): odeint computes it on the first call (FSAL) or on
         // every attempt (non-FSAL, same value for the same y, t).
-        eval_rhs<M, S>(y, p, t, k0);
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            ys[i] = from_d<S>(y[i]);
+        M::template rhs<S>(ys, p, from_d<S>(t), k0);
         return true;
     };
 
@@ -533,29 +556,34 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
             at_top = false;
         }
         double ynew[N];
-        S knew[N];
-        const double err = attempt<M, Tab, S>(y, k0, p, t, dt, a.atol, a.rtol, ynew, knew);
+        S ynew_s[N], knew[N];
+        const double err = attempt<M, Tab, S>(y, ys, k0, p, t, dt, a.atol, a.rtol, ynew, ynew_s, knew);
         bool ok;
         if (err != err) {
             status = ST_NONFINITE;
             continue;
         }
         if (err > 1.0) {
-            dt = decrease_step<Tab>(dt, err);
+            dt = decrease_step<Tab, S>(dt, err);
             rej++;
             ok = false;
         } else {
             t += dt;
-            dt = increase_step<Tab>(dt, err);
+            dt = increase_step<Tab, S>(dt, err);
 #pragma unroll
-            for (int i = 0; i < N; i++)
-                y[i] = ynew[i];
+            for (int i = 0; i < N; i++) {
+                ys[i] = ynew_s[i];
+                if constexpr (std::is_same<S, dword>::value)
+                    y[i] = to_d(ynew_s[i]); // the one rounding to FP64 per accepted step
+                else
+                    y[i] = ynew[i];
+            }
             if constexpr (Tab::FSAL) {
 #pragma unroll
                 for (int i = 0; i < N; i++)
                     k0[i] = knew[i];
             } else {
-                eval_rhs<M, S>(y, p, t, k0);
+                M::template rhs<S>(ys, p, from_d<S>(t), k0);
             }
             ok = true;
         }
@@ -586,10 +614,15 @@ __host__ __device__ __forceinline__ void back_step(const double (&y)[M::N], doub
     constexpr int N = M::N, P = M::PG, NS = Tab::S;
     S K[NS][N];
     S X[NS][N];
+    S ys[N];
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        ys[i] = from_d<S>(y[i]);
+    const S shh = from_d<S>(h);
     // recompute the stages from y_n (compute_intermediate_states, :24-64)
 #pragma unroll
     for (int m = 0; m < NS; m++) {
-        form_stage<Tab, N, S>(m, y, K, h, X[m]);
+        form_stage<Tab, N, S>(m, y, ys, K, h, shh, X[m]);
         M::template rhs<S>(X[m], p, from_d<S>(tn + Tab::c(m) * h), K[m]);
     }
     S Kbar[NS][N];
@@ -626,7 +659,7 @@ __host__ __device__ __forceinline__ void back_step(const double (&y)[M::N], doub
     } else {
         // Same recurrence with stage-precision seeds and VJPs; the per-step
         // sums of J^T Kbar are added to the FP64 lambda / mu once per step.
-        const S sdt = from_d<S>(h);
+        const S sdt = shh;
         S sl[N];
 #pragma unroll
         for (int i = 0; i < N; i++)
