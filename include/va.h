@@ -215,6 +215,14 @@ VA_API va_status va_checkpoint_info(const va_handle *h, int64_t *capacity_bytes,
 VA_API va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double *t,
                                double *dt, double *y, int32_t *n_records);
 
+/* Shared parameters of VA_MODEL_GLV_SHARED (n = 64 or 256, npar = n, nout = 1):
+ * A[n][n] row-major (DEVICE, read by every later sweep) and dA[n][n] (DEVICE,
+ * may be NULL), which each backward sweep overwrites with the gradient of
+ * the SUM of the batch's costs with respect to the shared A.  The reference
+ * has no shared-parameter batch; per instance this is its GLV parameter
+ * layout (examples/GeneralizedLotkaVolterra/main.cpp:105-119) with A common. */
+VA_API va_status va_set_shared(va_handle *h, const double *A, double *dA);
+
 /* Message of the last failing call on this handle ("" if none). */
 VA_API const char *va_last_error(const va_handle *h);
 

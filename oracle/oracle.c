@@ -14,6 +14,7 @@
 #include <string.h>
 
 #define SMAX 8
+#define NMAX 256 /* largest state dimension */
 
 typedef struct {
     int s;                 /* stages that feed y_{n+1}                        */
@@ -231,7 +232,7 @@ static int less_with_sign(double t1, double t2) { return t2 - t1 > DBL_EPSILON; 
  * new state, the derivative at the new point (FSAL tableaux only) and the
  * error vector.  K[0] must hold dxdt on entry. */
 static void rk_error_step(const orc_problem *pb, const tableau *T, const double *x, double t,
-                          double dt, const double *p, double K[SMAX][64], double *out,
+                          double dt, const double *p, double K[SMAX][NMAX], double *out,
                           double *dxdt_new, double *xerr, double *xtmp)
 {
     int n = pb->n;
@@ -351,10 +352,10 @@ int orc_forward(const orc_problem *pb, const double *y0, const double *p, double
 {
     tableau T;
     int n = pb->n;
-    if (n < 1 || n > 64 || get_tableau(pb->tableau, &T) != 0)
+    if (n < 1 || n > NMAX || get_tableau(pb->tableau, &T) != 0)
         return ORC_BAD_ARGS;
-    double y[64], dxdt[64], dxdt_new[64], out[64], xerr[64], xtmp[64];
-    double K[SMAX][64];
+    double y[NMAX], dxdt[NMAX], dxdt_new[NMAX], out[NMAX], xerr[NMAX], xtmp[NMAX];
+    double K[SMAX][NMAX];
     memcpy(y, y0, sizeof(double) * n);
     double t = t0, dt = pb->dt0;
     long count = 0, rej = 0;
@@ -440,7 +441,7 @@ void orc_forward_frozen(const orc_problem *pb, const double *y0, const double *p
     tableau tab;
     int n = pb->n;
     get_tableau(pb->tableau, &tab);
-    double y[64], xtmp[64], K[SMAX][64];
+    double y[NMAX], xtmp[NMAX], K[SMAX][NMAX];
     memcpy(y, y0, sizeof(double) * n);
     for (long k = 0; k < T; k++) {
         double t = times[k], h = times[k + 1] - times[k];
@@ -509,7 +510,7 @@ int orc_adjoint(const orc_problem *pb, const double *p, long T, const double *ti
                 const double *states, int nout, double *lambda, double *mu)
 {
     tableau tab;
-    if (get_tableau(pb->tableau, &tab) != 0 || pb->n < 1 || pb->n > 64 || nout < 1)
+    if (get_tableau(pb->tableau, &tab) != 0 || pb->n < 1 || pb->n > NMAX || nout < 1)
         return ORC_BAD_ARGS;
     int n = pb->n, np = pb->npar, s = tab.s;
     double *work = (double *)malloc(sizeof(double) * ((size_t)4 * s * n + 2 * n + 2 * (size_t)np));
@@ -554,7 +555,7 @@ int orc_gradient(const orc_problem *pb, int cost, const double *y0, const double
         free(states);
         return ORC_BAD_ARGS;
     }
-    double yT_local[64];
+    double yT_local[NMAX];
     long T = 0;
     int st = orc_forward(pb, y0, p, t0, t1, cap, times, states, NULL, yT_local, &T, n_rej);
     if (yT)

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/va.h"
+#include "va_bundle.cuh"
 #include "va_kernels.cuh"
 #include "va_registry.h"
 
@@ -23,9 +24,10 @@ struct GraphKey {
     int cost = -2;
     const void *ptrs[10] = {};
     void *stream = nullptr;
+    const void *extra = nullptr;
     bool operator==(const GraphKey &o) const
     {
-        if (cost != o.cost || stream != o.stream)
+        if (cost != o.cost || stream != o.stream || extra != o.extra)
             return false;
         for (int i = 0; i < 10; i++)
             if (ptrs[i] != o.ptrs[i])
@@ -64,6 +66,13 @@ struct va_handle {
 
     cudaGraphExec_t graph = nullptr;
     GraphKey graph_key;
+
+    // shared-matrix bundle path (VA_MODEL_GLV_SHARED)
+    const va::BundleKernelSet *bks = nullptr;
+    const double *shared_A = nullptr;
+    double *shared_dA = nullptr;
+    double *At = nullptr, *dA_part = nullptr;
+    va::dword *Aw = nullptr, *Atw = nullptr;
 };
 
 namespace {
@@ -145,8 +154,37 @@ va_status ensure_buffers(va_handle *h)
     VA_CUDA(h, cudaMalloc(&h->inst_status, (size_t)B * sizeof(int)));
     VA_CUDA(h, cudaMalloc(&h->ctl, sizeof(va::Control)));
     VA_CUDA(h, cudaMemset(h->ctl, 0, sizeof(va::Control)));
+    if (h->bks) {
+        const size_t NN = (size_t)h->N * h->N;
+        const size_t grid = ((size_t)B + h->bks->nb - 1) / h->bks->nb;
+        VA_CUDA(h, cudaMalloc(&h->At, NN * sizeof(double)));
+        VA_CUDA(h, cudaMalloc(&h->Aw, NN * sizeof(va::dword)));
+        VA_CUDA(h, cudaMalloc(&h->Atw, NN * sizeof(va::dword)));
+        VA_CUDA(h, cudaMalloc(&h->dA_part, grid * NN * sizeof(double)));
+        for (int t = 0; t < 2; t++)
+            for (int p = 0; p < 3; p++) {
+                VA_CUDA(h, cudaFuncSetAttribute(h->bks->fwd[t][p], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)h->bks->smem_fwd[p]));
+                VA_CUDA(h, cudaFuncSetAttribute(h->bks->bwd[t][p], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)h->bks->smem_bwd[p]));
+            }
+    }
     return VA_OK;
 }
+
+va::BundleParams bundle_params(va_handle *h)
+{
+    va::BundleParams bp{};
+    bp.A = h->shared_A;
+    bp.At = h->At;
+    bp.Aw = h->Aw;
+    bp.Atw = h->Atw;
+    bp.dA_part = h->dA_part;
+    bp.nb = h->bks->nb;
+    return bp;
+}
+
+int bundle_grid(va_handle *h) { return (h->prob.batch + h->bks->nb - 1) / h->bks->nb; }
 
 va_status ensure_staging(va_handle *h)
 {
@@ -208,6 +246,23 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
     a.inst_status = h->inst_status;
     a.pool = pool_of(h);
     a.ctl = h->ctl;
+    if (h->bks) {
+        if (!h->shared_A)
+            return fail(h, VA_BAD_ARGS, "shared-matrix model: call va_set_shared first%s");
+        const int NN = h->N * h->N;
+        void *pargs[] = {(void *)&h->shared_A, (void *)&h->At, (void *)&h->Aw, (void *)&h->Atw};
+        VA_CUDA(h, cudaMemsetAsync(h->ctl, 0, sizeof(va::Control), s));
+        VA_CUDA(h, cudaLaunchKernel(h->bks->prepare, dim3((NN + 255) / 256), dim3(256), pargs, 0, s));
+        va::BundleParams bp = bundle_params(h);
+        bp.f = a;
+        void *args[] = {&bp};
+        const int p = h->opt.precision;
+        VA_CUDA(h, cudaLaunchKernel(h->bks->fwd[h->opt.tableau][p], dim3(bundle_grid(h)), dim3(h->N), args,
+                                    h->bks->smem_fwd[p], s));
+        h->fwd_grid = bundle_grid(h);
+        h->fwd_block = h->N;
+        return VA_OK;
+    }
     const void *fn = h->ks->fwd[h->opt.tableau][h->opt.precision];
     if (h->fwd_grid <= 0)
         h->fwd_grid = grid_for(h, fn, h->fwd_block, a.B);
@@ -236,6 +291,23 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
     a.inst_status = h->inst_status;
     a.pool = pool_of(h);
     a.ctl = h->ctl;
+    if (h->bks) {
+        va::BundleParams bp = bundle_params(h);
+        bp.g = a;
+        void *args[] = {&bp};
+        const int p = h->opt.precision;
+        const int grid = bundle_grid(h);
+        VA_CUDA(h, cudaLaunchKernel(h->bks->bwd[h->opt.tableau][p], dim3(grid), dim3(h->N), args,
+                                    h->bks->smem_bwd[p], s));
+        if (h->shared_dA) {
+            const int NN = h->N * h->N;
+            void *rargs[] = {(void *)&h->dA_part, (void *)&grid, (void *)&h->shared_dA};
+            VA_CUDA(h, cudaLaunchKernel(h->bks->reduce, dim3((NN + 255) / 256), dim3(256), rargs, 0, s));
+        }
+        h->bwd_grid = grid;
+        h->bwd_block = h->N;
+        return VA_OK;
+    }
     const void *fn = h->ks->bwd[h->opt.tableau][h->opt.precision];
     if (h->bwd_grid <= 0)
         h->bwd_grid = grid_for(h, fn, h->bwd_block, a.B);
@@ -327,11 +399,21 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
         return VA_BAD_ARGS;
     if (o.max_steps < 1 || o.max_rejects < 1)
         return VA_BAD_ARGS;
-    const va::KernelSet *ks = kernel_set(*prob);
-    if (!ks)
-        return VA_BAD_ARGS;
-    const int N = ks->N > 0 ? ks->N : prob->n;
-    const int P = ks->P > 0 ? ks->P : prob->npar;
+    const va::KernelSet *ks = nullptr;
+    const va::BundleKernelSet *bks = nullptr;
+    int N = 0, P = 0;
+    if (prob->model == VA_MODEL_GLV_SHARED) {
+        bks = va::kernels_glv_shared(prob->n);
+        if (!bks || prob->nout != 1)
+            return VA_BAD_ARGS;
+        N = P = prob->n;
+    } else {
+        ks = kernel_set(*prob);
+        if (!ks)
+            return VA_BAD_ARGS;
+        N = ks->N > 0 ? ks->N : prob->n;
+        P = ks->P > 0 ? ks->P : prob->npar;
+    }
     if (prob->n != N || prob->npar != P)
         return VA_BAD_ARGS;
     if (o.ckpt_stride > 1)
@@ -340,6 +422,7 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
     h->prob = *prob;
     h->opt = o;
     h->ks = ks;
+    h->bks = bks;
     h->N = N;
     h->P = P;
     h->RS = va::record_doubles(N);
@@ -366,7 +449,8 @@ va_status va_destroy(va_handle *h)
     void *ptrs[] = {h->pool_rec, h->chunk_prev, h->inst_T,  h->inst_last, h->inst_status,
                     h->ctl,      h->s_y0,       h->s_par,   h->s_t0,      h->s_t1,
                     h->s_yT,     h->s_dy0,      h->s_dpar,  h->s_nacc,    h->s_status,
-                    h->s_nrej,   h->s_lam,      h->s_mu};
+                    h->s_nrej,   h->s_lam,      h->s_mu,    h->At,        h->Aw,
+                    h->Atw,      h->dA_part};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -423,9 +507,10 @@ va_status va_gradient(va_handle *h, int32_t cost, const double *y0, const double
     cudaStream_t s = (cudaStream_t)stream;
     GraphKey key;
     key.cost = cost;
-    const void *ptrs[10] = {y0, params, t0, t1, yT, dy0, dparams, n_acc, status, nullptr};
+    const void *ptrs[10] = {y0, params, t0, t1, yT, dy0, dparams, n_acc, status, h->shared_A};
     std::memcpy(key.ptrs, ptrs, sizeof(ptrs));
     key.stream = stream;
+    key.extra = h->shared_dA;
     // The legacy default stream cannot be captured: launch directly there.
     if (s == nullptr) {
         st = enqueue_forward(h, y0, params, t0, t1, yT, n_acc, nullptr, status, s);
@@ -437,10 +522,10 @@ va_status va_gradient(va_handle *h, int32_t cost, const double *y0, const double
     if (!h->graph || !(h->graph_key == key)) {
         drop_graph(h);
         // size the persistent grids before capture (occupancy queries)
-        if (h->fwd_grid <= 0)
+        if (h->ks && h->fwd_grid <= 0)
             h->fwd_grid = grid_for(h, h->ks->fwd[h->opt.tableau][h->opt.precision], h->fwd_block,
                                    h->prob.batch);
-        if (h->bwd_grid <= 0)
+        if (h->ks && h->bwd_grid <= 0)
             h->bwd_grid = grid_for(h, h->ks->bwd[h->opt.tableau][h->opt.precision], h->bwd_block,
                                    h->prob.batch);
         VA_CUDA(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -646,6 +731,19 @@ va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double
     return VA_OK;
 }
 
+va_status va_set_shared(va_handle *h, const double *A, double *dA)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    if (!h->bks)
+        return fail(h, VA_BAD_ARGS, "va_set_shared: the model has no shared parameters%s");
+    if (!A)
+        return fail(h, VA_BAD_ARGS, "va_set_shared: A is null%s");
+    h->shared_A = A;
+    h->shared_dA = dA;
+    return VA_OK;
+}
+
 va_status va_autotune(va_handle *h, int32_t cost, const double *y0, const double *params,
                       const double *t0, const double *t1, void *stream)
 {
@@ -657,6 +755,8 @@ va_status va_autotune(va_handle *h, int32_t cost, const double *y0, const double
     st = ensure_staging(h);
     if (st != VA_OK)
         return st;
+    if (h->bks)
+        return VA_OK; // bundle kernels: one CTA of N threads per bundle, nothing to tune
     cudaStream_t s = (cudaStream_t)stream;
     const void *ffn = h->ks->fwd[h->opt.tableau][h->opt.precision];
     const void *bfn = h->ks->bwd[h->opt.tableau][h->opt.precision];

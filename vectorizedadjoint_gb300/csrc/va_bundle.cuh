@@ -1,0 +1,691 @@
+// Bundle sweeps for generalized Lotka-Volterra with ONE interaction matrix A
+// shared by the whole batch: x_i' = x_i (r_i + sum_j A_ij x_j), per-instance
+// r and x0.  A CTA of N threads carries a bundle of up to NB instances in
+// lockstep (each instance keeps its own t, dt and controller decisions);
+// thread i owns state component i of every instance in the bundle.
+//
+// Per stage the bundle needs z = A x for each of its instances: thread i
+// forms z_i as a dot product of row i of A (read through the transposed copy
+// At so that consecutive threads read consecutive addresses; A and At stay
+// resident in L2) with the stage vectors, which sit in shared memory and are
+// read as broadcasts.  Sharing each A element across the NB instances of the
+// bundle divides the L2 traffic by NB.  The backward sweep adds
+// A^T (w . x) (read through A itself, again coalesced) and the outer
+// products sum (w . x) x^T that make up dA: those accumulate, once per step,
+// into a private N x N partial of the CTA in global memory, and a final
+// kernel adds the partials in a fixed order -- no atomics on any result.
+//
+// The arithmetic per component follows the reference's GLV functor
+// (examples/GeneralizedLotkaVolterra/main.cpp:109-118: sum_j in ascending
+// order, then x_i (r_i + sum)) and the same back_prop_step recurrence as the
+// other sweeps, so the FP64 build reproduces the oracle's per-instance
+// results bit for bit; dA, a sum over the batch, agrees to rounding.
+#pragma once
+
+#include "va_kernels.cuh"
+
+namespace va {
+
+struct BundleParams {
+    FwdParams f;          // batch, inputs (par = r[B][N]), tolerances, outputs, pool
+    AdjParams g;          // seeds / gradient outputs (par = r)
+    const double *A;      // [N][N] row-major (FP64 path)
+    const double *At;     // [N][N] = A^T row-major
+    const dword *Aw;      // double-word copies (double-word path)
+    const dword *Atw;
+    double *dA_part;      // [gridDim.x][N][N], transposed per CTA: [j][i] += dA_ij
+    int nb;               // instances per CTA (<= NB)
+};
+
+template <class S>
+__device__ __forceinline__ S load_A(const double *A, const dword *Aw, size_t k)
+{
+    if constexpr (std::is_same<S, dword>::value)
+        return Aw[k];
+    else
+        return (S)A[k];
+}
+
+// Block-wide maximum per instance of non-negative values (NaN propagates).
+template <int NT, int NB>
+__device__ __forceinline__ void bundle_max(double (&v)[NB], double *red /* [NT/32][NB] */)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+        double x = v[b];
+        bool nan = x != x;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+        nan = __any_sync(0xffffffffu, nan);
+        if (lane == 0)
+            red[warp * NB + b] = nan ? __longlong_as_double(0x7ff8000000000000ll) : x;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+        double m = 0.0;
+        bool nan = false;
+#pragma unroll
+        for (int w = 0; w < NT / 32; w++) {
+            const double x = red[w * NB + b];
+            nan = nan || x != x;
+            m = fmax(m, x);
+        }
+        v[b] = nan ? __longlong_as_double(0x7ff8000000000000ll) : m;
+    }
+    __syncthreads();
+}
+
+// z_b += sum_j M_ij xs[b][j], j ascending, for the NB vectors in shared
+// memory (thread i).  Mt is the matrix read as Mt[j][i] (consecutive i are
+// consecutive addresses).  One pass over the matrix serves all NB vectors.
+template <int NT, int NB, class S>
+__device__ __forceinline__ void bundle_matvec_acc(const double *Mt, const dword *Mtw,
+                                                  const S *xs /* [NT][NB] */, S (&z)[NB])
+{
+    const int i = threadIdx.x;
+#pragma unroll 4
+    for (int j = 0; j < NT; j++) {
+        const S a = load_A<S>(Mt, Mtw, (size_t)j * NT + i);
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+            z[b] = madd(a, xs[j * NB + b], z[b]);
+    }
+}
+
+template <int NT, int NB, class S>
+__device__ __forceinline__ void bundle_matvec(const double *Mt, const dword *Mtw, const S *xs /* [NT][NB] */,
+                                              S (&z)[NB])
+{
+    const int i = threadIdx.x;
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+        z[b] = S(0);
+#pragma unroll 4
+    for (int j = 0; j < NT; j++) {
+        const S a = load_A<S>(Mt, Mtw, (size_t)j * NT + i);
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+            z[b] = madd(a, xs[j * NB + b], z[b]);
+    }
+}
+
+// ------------------------------------------------------------ forward sweep
+
+template <int NT, int NB, class Tab, class S>
+__global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
+{
+    constexpr int NS = Tab::S;
+    constexpr int RS = record_doubles(NT);
+    const FwdParams &a = bp.f;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    S *xs = reinterpret_cast<S *>(smem_raw);                               // [NT][NB]
+    double *red = reinterpret_cast<double *>(smem_raw + sizeof(S) * NT * NB); // [NT/32][NB]
+    int *ichunk = reinterpret_cast<int *>(red + (NT / 32) * NB);            // [NB]
+    const int i = threadIdx.x;
+    const int CH = a.pool.chunk_len;
+
+    double y[NB], t[NB], t1[NB], dt[NB];
+    S ys[NB], r[NB], K[NS][NB], knew[NB];
+    int count[NB], rej[NB], fails[NB], status[NB], chunk[NB], slot[NB], inst[NB];
+    bool active[NB], at_top[NB];
+
+    // instances of this CTA
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+        inst[b] = blockIdx.x * bp.nb + b;
+        active[b] = b < bp.nb && inst[b] < a.B;
+        count[b] = rej[b] = fails[b] = 0;
+        status[b] = ST_OK;
+        at_top[b] = true;
+        slot[b] = 0;
+        chunk[b] = -1;
+        y[b] = 0.0;
+        t[b] = t1[b] = 0.0;
+        dt[b] = a.dt0;
+        ys[b] = S(0);
+        r[b] = S(0);
+        if (active[b]) {
+            y[b] = a.y0[(size_t)inst[b] * NT + i];
+            r[b] = from_d<S>(a.par[(size_t)inst[b] * NT + i]);
+            ys[b] = from_d<S>(y[b]);
+            t[b] = a.t0[inst[b]];
+            t1[b] = a.t1[inst[b]];
+        }
+    }
+    if (i == 0) {
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            int c = -1;
+            if (active[b]) {
+                c = (int)atomicAdd(&a.ctl->pool_next, 1u);
+                if (c >= a.pool.n_chunks) {
+                    c = -1;
+                    atomicOr(&a.ctl->pool_fail, 1u);
+                } else {
+                    a.pool.chunk_prev[c] = -1;
+                }
+            }
+            ichunk[b] = c;
+        }
+    }
+    // k_1 = f(y_0) for the bundle
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+        xs[i * NB + b] = ys[b];
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+        chunk[b] = ichunk[b];
+        if (active[b] && chunk[b] < 0)
+            status[b] = ST_CKPT_BUDGET;
+    }
+    {
+        S z[NB];
+        bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, z);
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+            K[0][b] = ys[b] * (r[b] + z[b]);
+    }
+    __syncthreads();
+
+    for (;;) {
+        // top of step for every live instance: loop test, record, end clamp.
+        // Chunk allocation needs one thread and a barrier, so it is done for
+        // the whole bundle at once.
+        bool need_chunk = false;
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            if (!active[b] || status[b] != ST_OK || !at_top[b])
+                continue;
+            if (!(t1[b] - t[b] > kDblEps)) {
+                // finished: write the final record, like the single-thread sweep
+                if (slot[b] == CH)
+                    need_chunk = true;
+                continue;
+            }
+            if (count[b] >= a.max_steps) {
+                status[b] = ST_MAX_STEPS;
+                continue;
+            }
+            if (slot[b] == CH)
+                need_chunk = true;
+        }
+        if (need_chunk) {
+            if (i == 0) {
+#pragma unroll
+                for (int b = 0; b < NB; b++) {
+                    int c = chunk[b];
+                    if (active[b] && status[b] == ST_OK && at_top[b] && slot[b] == CH) {
+                        c = (int)atomicAdd(&a.ctl->pool_next, 1u);
+                        if (c >= a.pool.n_chunks) {
+                            c = -1;
+                            atomicOr(&a.ctl->pool_fail, 1u);
+                        } else {
+                            a.pool.chunk_prev[c] = chunk[b];
+                        }
+                    }
+                    ichunk[b] = c;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+                if (active[b] && status[b] == ST_OK && at_top[b] && slot[b] == CH) {
+                    chunk[b] = ichunk[b];
+                    slot[b] = 0;
+                    if (chunk[b] < 0)
+                        status[b] = ST_CKPT_BUDGET;
+                }
+            }
+            __syncthreads();
+        }
+        bool any_attempt = false;
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            if (!active[b] || !at_top[b])
+                continue;
+            if (status[b] == ST_OK) {
+                double *rec = record_ptr<RS>(a.pool, chunk[b], slot[b]);
+                if (i == 0)
+                    *reinterpret_cast<double2 *>(rec) = make_double2(t[b], dt[b]);
+                rec[2 + i] = y[b];
+                slot[b]++;
+            }
+            if (status[b] != ST_OK || !(t1[b] - t[b] > kDblEps)) {
+                // instance done: outputs
+                if (__syncthreads_or(isfinite(y[b]) ? 0 : 1) && status[b] == ST_OK)
+                    status[b] = ST_NONFINITE;
+                if (a.yT)
+                    a.yT[(size_t)inst[b] * NT + i] = y[b];
+                if (i == 0) {
+                    a.inst_T[inst[b]] = count[b];
+                    a.inst_last[inst[b]] = status[b] == ST_OK ? chunk[b] : -1;
+                    a.inst_status[inst[b]] = status[b];
+                    if (a.n_acc_out)
+                        a.n_acc_out[inst[b]] = count[b];
+                    if (a.n_rej_out)
+                        a.n_rej_out[inst[b]] = rej[b];
+                    if (a.status_out)
+                        a.status_out[inst[b]] = status[b];
+                }
+                active[b] = false;
+                continue;
+            }
+            if ((t[b] + dt[b]) - t1[b] > kDblEps)
+                dt[b] = t1[b] - t[b];
+            fails[b] = 0;
+            at_top[b] = false;
+        }
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+            any_attempt = any_attempt || active[b];
+        if (!any_attempt)
+            break;
+
+        // one attempt for every live instance: stages 2..s
+        S sdt[NB];
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+            sdt[b] = from_d<S>(dt[b]);
+#pragma unroll
+        for (int m = 1; m < NS; m++) {
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+                S X;
+                if constexpr (std::is_same<S, double>::value) {
+                    double acc = y[b];
+#pragma unroll
+                    for (int j = 0; j < NS - 1; j++)
+                        if (j < m)
+                            acc = acc + (Tab::a(m, j) * dt[b]) * K[j][b];
+                    X = acc;
+                } else {
+                    S acc = S(0);
+#pragma unroll
+                    for (int j = 0; j < NS - 1; j++)
+                        if (j < m)
+                            acc = madd(S(Tab::a(m, j)), K[j][b], acc);
+                    X = madd(acc, sdt[b], ys[b]);
+                }
+                xs[i * NB + b] = X;
+            }
+            __syncthreads();
+            S z[NB];
+            bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, z);
+#pragma unroll
+            for (int b = 0; b < NB; b++)
+                K[m][b] = xs[i * NB + b] * (r[b] + z[b]);
+            __syncthreads();
+        }
+        // y_new, f(y_new), error estimate
+        S ynew_s[NB];
+        double ynew[NB];
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            if constexpr (std::is_same<S, double>::value) {
+                double acc = y[b];
+#pragma unroll
+                for (int j = 0; j < NS; j++)
+                    if (Tab::b(j) != 0.0)
+                        acc = acc + (Tab::b(j) * dt[b]) * K[j][b];
+                ynew[b] = acc;
+                ynew_s[b] = acc;
+            } else {
+                S acc = S(0);
+#pragma unroll
+                for (int j = 0; j < NS; j++)
+                    if (Tab::b(j) != 0.0)
+                        acc = madd(S(Tab::b(j)), K[j][b], acc);
+                ynew_s[b] = madd(acc, sdt[b], ys[b]);
+                ynew[b] = to_d(ynew_s[b]);
+            }
+            xs[i * NB + b] = ynew_s[b];
+        }
+        if constexpr (Tab::FSAL) {
+            __syncthreads();
+            S z[NB];
+            bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, z);
+#pragma unroll
+            for (int b = 0; b < NB; b++)
+                knew[b] = ynew_s[b] * (r[b] + z[b]);
+            __syncthreads();
+        }
+        double ratio[NB];
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            double e;
+            if constexpr (std::is_same<S, double>::value) {
+                double acc = 0.0;
+                bool first = true;
+#pragma unroll
+                for (int j = 0; j < NS; j++)
+                    if (Tab::e(j) != 0.0) {
+                        const double term = (Tab::e(j) * dt[b]) * K[j][b];
+                        acc = first ? term : acc + term;
+                        first = false;
+                    }
+                if constexpr (Tab::FSAL)
+                    acc = acc + (Tab::E_NEW * dt[b]) * knew[b];
+                e = acc;
+                ratio[b] = fabs(e) / (a.atol + a.rtol * (1.0 * fabs(y[b]) + fabs(dt[b]) * fabs(K[0][b])));
+            } else {
+                S acc = S(0);
+#pragma unroll
+                for (int j = 0; j < NS; j++)
+                    if (Tab::e(j) != 0.0)
+                        acc = madd(S(Tab::e(j)), K[j][b], acc);
+                if constexpr (Tab::FSAL)
+                    acc = madd(S(Tab::E_NEW), knew[b], acc);
+                e = dt[b] * to_d(acc);
+                ratio[b] = fabs(e) / (a.atol + a.rtol * (1.0 * fabs(y[b]) + fabs(dt[b]) * fabs(to_d(K[0][b]))));
+            }
+            if (!active[b] || at_top[b])
+                ratio[b] = 0.0;
+        }
+        bundle_max<NT, NB>(ratio, red);
+        // controller, per instance (uniform across the CTA)
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            if (!active[b] || at_top[b])
+                continue;
+            const double err = ratio[b];
+            bool ok;
+            if (err != err) {
+                status[b] = ST_NONFINITE;
+                at_top[b] = true;
+                continue;
+            }
+            if (err > 1.0) {
+                dt[b] = decrease_step<Tab, S>(dt[b], err);
+                rej[b]++;
+                ok = false;
+            } else {
+                t[b] += dt[b];
+                dt[b] = increase_step<Tab, S>(dt[b], err);
+                y[b] = ynew[b];
+                ys[b] = ynew_s[b];
+                if constexpr (Tab::FSAL)
+                    K[0][b] = knew[b];
+                ok = true;
+            }
+            if (fails[b] >= a.max_fail) {
+                status[b] = ST_MAX_REJECTS;
+                at_top[b] = true;
+                continue;
+            }
+            fails[b]++;
+            if (ok) {
+                count[b]++;
+                at_top[b] = true;
+            } else if (!(dt[b] > 0.0) || !isfinite(dt[b])) {
+                status[b] = ST_NONFINITE;
+                at_top[b] = true;
+            }
+        }
+        if constexpr (!Tab::FSAL) {
+            // non-FSAL pairs: k_1 = f(y) at the new state of accepted instances
+#pragma unroll
+            for (int b = 0; b < NB; b++)
+                xs[i * NB + b] = ys[b];
+            __syncthreads();
+            S z[NB];
+            bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, z);
+#pragma unroll
+            for (int b = 0; b < NB; b++)
+                K[0][b] = ys[b] * (r[b] + z[b]);
+            __syncthreads();
+        }
+    }
+}
+
+// ----------------------------------------------------------- backward sweep
+
+template <int NT, int NB, class Tab, class S>
+__global__ void __launch_bounds__(NT) backward_bundle_kernel(BundleParams bp)
+{
+    constexpr int NS = Tab::S;
+    constexpr int RS = record_doubles(NT);
+    const AdjParams &a = bp.g;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    S *xall = reinterpret_cast<S *>(smem_raw);      // [NS][NT][NB] stage points
+    S *vall = xall + (size_t)NS * NT * NB;          // [NS][NT][NB] w . x per stage
+    S *zall = vall + (size_t)NS * NT * NB;          // [NS][NT][NB] A x per stage
+    const int i = threadIdx.x;
+    const int CH = a.pool.chunk_len;
+
+    int inst[NB], T[NB], j[NB], chunk[NB], slot[NB];
+    bool live[NB];
+    double lam[NB], mu[NB], t_next[NB];
+    S r[NB];
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+        inst[b] = blockIdx.x * bp.nb + b;
+        live[b] = b < bp.nb && inst[b] < a.B;
+        T[b] = 0;
+        j[b] = -1;
+        chunk[b] = -1;
+        slot[b] = 0;
+        lam[b] = 0.0;
+        mu[b] = 0.0;
+        t_next[b] = 0.0;
+        r[b] = S(0);
+        if (!live[b])
+            continue;
+        if (a.inst_status[inst[b]] != ST_OK) {
+            const double nan = __longlong_as_double(0x7ff8000000000000ll);
+            a.dy0[(size_t)inst[b] * NT + i] = nan;
+            a.dpar[(size_t)inst[b] * NT + i] = nan;
+            if (a.status_out && i == 0)
+                a.status_out[inst[b]] = a.inst_status[inst[b]];
+            live[b] = false;
+            continue;
+        }
+        r[b] = from_d<S>(a.par[(size_t)inst[b] * NT + i]);
+        T[b] = a.inst_T[inst[b]];
+        chunk[b] = a.inst_last[inst[b]];
+        slot[b] = T[b] % CH;
+        const double *rec = record_ptr<RS>(a.pool, chunk[b], slot[b]);
+        t_next[b] = rec[0];
+        const double yT = rec[2 + i];
+        lam[b] = a.cost == 0 ? 2.0 * yT : a.cost == 1 ? 1.0 : a.lambdaT[(size_t)inst[b] * NT + i];
+        j[b] = T[b] - 1;
+    }
+    // this CTA's partial of dA, transposed: part[jj][i] += dA_i,jj
+    double *part = bp.dA_part + (size_t)blockIdx.x * NT * NT;
+    for (int jj = 0; jj < NT; jj++)
+        part[(size_t)jj * NT + i] = 0.0;
+
+    for (;;) {
+        bool any = false;
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+            any = any || (live[b] && j[b] >= 0);
+        if (!any)
+            break;
+        bool step[NB];
+        double y[NB], h[NB], tn[NB];
+        S ys[NB], sh[NB];
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            step[b] = live[b] && j[b] >= 0;
+            y[b] = 0.0;
+            h[b] = 0.0;
+            tn[b] = 0.0;
+            if (step[b]) {
+                if (slot[b] == 0) {
+                    chunk[b] = a.pool.chunk_prev[chunk[b]];
+                    slot[b] = CH - 1;
+                } else {
+                    slot[b]--;
+                }
+                const double *rec = record_ptr<RS>(a.pool, chunk[b], slot[b]);
+                tn[b] = rec[0];
+                y[b] = rec[2 + i];
+                h[b] = t_next[b] - tn[b];
+            }
+            ys[b] = from_d<S>(y[b]);
+            sh[b] = from_d<S>(h[b]);
+        }
+        // recompute the stages (compute_intermediate_states)
+        S K[NS][NB];
+#pragma unroll
+        for (int m = 0; m < NS; m++) {
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+                S X;
+                if constexpr (std::is_same<S, double>::value) {
+                    double acc = y[b];
+#pragma unroll
+                    for (int jj = 0; jj < NS - 1; jj++)
+                        if (jj < m)
+                            acc = acc + (Tab::a(m, jj) * h[b]) * K[jj][b];
+                    X = acc;
+                } else {
+                    S acc = S(0);
+#pragma unroll
+                    for (int jj = 0; jj < NS - 1; jj++)
+                        if (jj < m)
+                            acc = madd(S(Tab::a(m, jj)), K[jj][b], acc);
+                    X = madd(acc, sh[b], ys[b]);
+                }
+                xall[((size_t)m * NT + i) * NB + b] = X;
+            }
+            __syncthreads();
+            S z[NB];
+            bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xall + (size_t)m * NT * NB, z);
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+                zall[((size_t)m * NT + i) * NB + b] = z[b];
+                K[m][b] = xall[((size_t)m * NT + i) * NB + b] * (r[b] + z[b]);
+            }
+        }
+        // seeds and the stage loop s..1 (back_prop_step)
+        S Kbar[NS][NB];
+        double ybar[NB];
+        S gsum[NB], vsum[NB];
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            ybar[b] = lam[b];
+#pragma unroll
+            for (int m = 0; m < NS; m++) {
+                if constexpr (std::is_same<S, double>::value)
+                    Kbar[m][b] = (Tab::b(m) * h[b]) * lam[b];
+                else
+                    Kbar[m][b] = (S(Tab::b(m)) * sh[b]) * from_d<S>(lam[b]);
+            }
+        }
+#pragma unroll
+        for (int m = NS - 1; m >= 0; m--) {
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+                const S x = xall[((size_t)m * NT + i) * NB + b];
+                vall[((size_t)m * NT + i) * NB + b] = step[b] ? Kbar[m][b] * x : S(0);
+            }
+            __syncthreads();
+            // g = w (r + z), then += A_ji v_j for j ascending (the oracle's
+            // order); A[j][i] is read row-major, coalesced across threads
+            S g_all[NB];
+#pragma unroll
+            for (int b = 0; b < NB; b++)
+                g_all[b] = Kbar[m][b] * (r[b] + zall[((size_t)m * NT + i) * NB + b]);
+            bundle_matvec_acc<NT, NB, S>(bp.A, bp.Aw, vall + (size_t)m * NT * NB, g_all);
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+                if (!step[b])
+                    continue;
+                const S v = vall[((size_t)m * NT + i) * NB + b];
+                const S g = g_all[b];
+                if constexpr (std::is_same<S, double>::value) {
+                    ybar[b] += g;
+                    mu[b] += v;
+                } else {
+                    gsum[b] = (m == NS - 1) ? g : gsum[b] + g;
+                    vsum[b] = (m == NS - 1) ? v : vsum[b] + v;
+                }
+#pragma unroll
+                for (int k = 0; k < NS - 1; k++)
+                    if (k < m) {
+                        if constexpr (std::is_same<S, double>::value)
+                            Kbar[k][b] += g * Tab::a(m, k) * h[b];
+                        else
+                            Kbar[k][b] = madd(g * S(Tab::a(m, k)), sh[b], Kbar[k][b]);
+                    }
+            }
+            __syncthreads();
+        }
+        // dA partial: part[jj][i] += sum_{m,b} v_{m,b,i} x_{m,b,jj}
+        {
+            S vi[NS][NB];
+#pragma unroll
+            for (int m = 0; m < NS; m++)
+#pragma unroll
+                for (int b = 0; b < NB; b++)
+                    vi[m][b] = vall[((size_t)m * NT + i) * NB + b];
+            for (int jj = 0; jj < NT; jj++) {
+                S acc = S(0);
+#pragma unroll
+                for (int m = NS - 1; m >= 0; m--)
+#pragma unroll
+                    for (int b = 0; b < NB; b++)
+                        acc = madd(vi[m][b], xall[((size_t)m * NT + jj) * NB + b], acc);
+                part[(size_t)jj * NT + i] += to_d(acc);
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            if (!step[b])
+                continue;
+            if constexpr (std::is_same<S, double>::value) {
+                lam[b] = ybar[b];
+            } else {
+                lam[b] += to_d(gsum[b]);
+                mu[b] += to_d(vsum[b]);
+            }
+            t_next[b] = tn[b];
+            j[b]--;
+            if (j[b] < 0) {
+                a.dy0[(size_t)inst[b] * NT + i] = lam[b];
+                const double d = a.mu_direct ? a.mu_direct[(size_t)inst[b] * NT + i] : 0.0;
+                a.dpar[(size_t)inst[b] * NT + i] = d + mu[b];
+                const bool finite = isfinite(lam[b]) && isfinite(mu[b]);
+                const int all_finite = __syncthreads_and(finite ? 1 : 0);
+                if (a.status_out && i == 0)
+                    a.status_out[inst[b]] = all_finite ? ST_OK : ST_NONFINITE;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// dA = sum over CTAs of the transposed partials, in CTA order.
+template <int NT>
+__global__ void reduce_dA_kernel(const double *part, int nparts, double *dA)
+{
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; // k = jj * NT + i
+    if (k >= (size_t)NT * NT)
+        return;
+    double s = 0.0;
+    for (int c = 0; c < nparts; c++)
+        s += part[(size_t)c * NT * NT + k];
+    const size_t jj = k / NT, i = k % NT;
+    dA[i * NT + jj] = s;
+}
+
+// A^T and the double-word copies of A and A^T.
+template <int NT>
+__global__ void prepare_A_kernel(const double *A, double *At, dword *Aw, dword *Atw)
+{
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (size_t)NT * NT)
+        return;
+    const size_t row = k / NT, col = k % NT;
+    const double v = A[k];
+    At[col * NT + row] = v;
+    Aw[k] = dword(v);
+    Atw[col * NT + row] = dword(v);
+}
+
+} // namespace va

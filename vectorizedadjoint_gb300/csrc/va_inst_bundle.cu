@@ -1,0 +1,52 @@
+// Shared-matrix GLV bundle kernels (N = 64, 256; 4 instances per CTA):
+// reduced-precision sweeps and the helper kernels.  FP64 sweeps come from
+// va_inst_bundle_fp64.cu, built without FMA contraction.
+#include "va_bundle.cuh"
+#include "va_registry.h"
+
+namespace va {
+
+void fill_fp64_bundle64(BundleKernelSet &k);
+void fill_fp64_bundle256(BundleKernelSet &k);
+
+template <int NT>
+static BundleKernelSet make_bundle(void (*fill_fp64)(BundleKernelSet &))
+{
+    constexpr int NB = kBundleNB;
+    BundleKernelSet k{};
+    k.N = NT;
+    k.nb = NB;
+    fill_fp64(k);
+    k.fwd[0][1] = (const void *)forward_bundle_kernel<NT, NB, TabDopri5, float>;
+    k.fwd[0][2] = (const void *)forward_bundle_kernel<NT, NB, TabDopri5, dword>;
+    k.fwd[1][1] = (const void *)forward_bundle_kernel<NT, NB, TabCK54, float>;
+    k.fwd[1][2] = (const void *)forward_bundle_kernel<NT, NB, TabCK54, dword>;
+    k.bwd[0][1] = (const void *)backward_bundle_kernel<NT, NB, TabDopri5, float>;
+    k.bwd[0][2] = (const void *)backward_bundle_kernel<NT, NB, TabDopri5, dword>;
+    k.bwd[1][1] = (const void *)backward_bundle_kernel<NT, NB, TabCK54, float>;
+    k.bwd[1][2] = (const void *)backward_bundle_kernel<NT, NB, TabCK54, dword>;
+    const size_t sz[3] = {sizeof(double), sizeof(float), sizeof(dword)};
+    for (int p = 0; p < 3; p++) {
+        k.smem_fwd[p] = sz[p] * NT * NB + sizeof(double) * (NT / 32) * NB + sizeof(int) * NB;
+        k.smem_bwd[p] = 3 * sz[p] * (size_t)TabDopri5::S * NT * NB;
+    }
+    k.prepare = (const void *)prepare_A_kernel<NT>;
+    k.reduce = (const void *)reduce_dA_kernel<NT>;
+    return k;
+}
+
+const BundleKernelSet *kernels_glv_shared(int n)
+{
+    static const BundleKernelSet k64 = make_bundle<64>(fill_fp64_bundle64);
+    static const BundleKernelSet k256 = make_bundle<256>(fill_fp64_bundle256);
+    switch (n) {
+    case 64:
+        return &k64;
+    case 256:
+        return &k256;
+    default:
+        return nullptr;
+    }
+}
+
+} // namespace va

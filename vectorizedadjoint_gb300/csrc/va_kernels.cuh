@@ -332,7 +332,8 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
         }
         if constexpr (Tab::FSAL)
             M::template rhs<S>(ynew_s, p, from_d<S>(t + dt), knew);
-        // error vector to FP64 from the leading word: an estimate needs no more
+        // error vector to FP64 at full stage precision: a coarser estimate
+        // (leading word only) flips accept/reject decisions near err = 1
 #pragma unroll
         for (int i = 0; i < N; i++) {
             S acc = S(0);
@@ -342,7 +343,7 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
                     acc = madd(S(Tab::e(j)), K[j][i], acc);
             if constexpr (Tab::FSAL)
                 acc = madd(S(Tab::E_NEW), knew[i], acc);
-            e[i] = dt * (double)hi_of(acc);
+            e[i] = dt * to_d(acc);
         }
     }
     const double adt = fabs(dt);
@@ -361,11 +362,11 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
     }
     // reduced paths: max-norm with one division, the largest ratio kept as a fraction
     double num = fabs(e[0]);
-    double den = atol + rtol * (1.0 * fabs(y[0]) + adt * fabs((double)hi_of(k0[0])));
+    double den = atol + rtol * (1.0 * fabs(y[0]) + adt * fabs(to_d(k0[0])));
 #pragma unroll
     for (int i = 1; i < N; i++) {
         double ni = fabs(e[i]);
-        double di = atol + rtol * (1.0 * fabs(y[i]) + adt * fabs((double)hi_of(k0[i])));
+        double di = atol + rtol * (1.0 * fabs(y[i]) + adt * fabs(to_d(k0[i])));
         if (ni * den > num * di || ni != ni) {
             num = ni;
             den = di;

@@ -18,4 +18,16 @@ const KernelSet *kernels_dho();
 const KernelSet *kernels_decay();
 const KernelSet *kernels_glv(int n); // nullptr when n has no compiled kernels
 
+// Shared-matrix GLV: bundles of kBundleNB instances per CTA of N threads.
+constexpr int kBundleNB = 4;
+struct BundleKernelSet {
+    int N, nb;
+    const void *fwd[2][3]; // __global__ void(BundleParams), blockDim = N
+    const void *bwd[2][3];
+    size_t smem_fwd[3], smem_bwd[3]; // dynamic shared memory per precision
+    const void *prepare;   // prepare_A_kernel: A -> A^T and double-word copies
+    const void *reduce;    // reduce_dA_kernel: CTA partials -> dA
+};
+const BundleKernelSet *kernels_glv_shared(int n); // n = 64 or 256
+
 } // namespace va

@@ -122,6 +122,12 @@ class Solver:
                                             hp(out["status"]), _stream()), "va_gradient_host")
         return out
 
+    def set_shared(self, A, dA=None):
+        """va_set_shared (shared-matrix GLV): A [n, n] CUDA tensor read by every
+        later sweep; dA [n, n] receives the gradient of the batch's summed cost."""
+        self._shared = (A, dA)
+        self._check(self.L.va_set_shared(self.h, _ptr(A), _ptr(dA)), "va_set_shared")
+
     def autotune(self, cost, y0, params, t0, t1):
         self._check(self.L.va_autotune(self.h, _lib.COSTS[cost], _ptr(y0), _ptr(params), _ptr(t0), _ptr(t1),
                                        _stream()), "va_autotune")
