@@ -107,16 +107,24 @@ def cpu_baseline(cfg_name, w, seconds=10.0, threads=None):
     from oracle import oracle_py as O
     c = w["cfg"]
     threads = threads or os.cpu_count() or 1
-    pb = O.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"])
     B = c["batch"]
-    pilot = min(B, 64 * threads)
+    params = w["params"]
+    if w["shared"] is not None:
+        # per instance the reference's GLV layout: r, then the (common) A
+        A = np.asarray(w["shared"]).ravel()
+        pb = O.problem("glv", c["tableau"], c["n"], c["n"] + c["n"] ** 2, c["tol"], c["tol"])
+        params = lambda k: np.concatenate([w["params"][:k], np.broadcast_to(A, (k, A.size))], axis=1)
+    else:
+        pb = O.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"])
+        params = (lambda k, P=params: P[:k])
+    pilot = min(B, (64 if c["n"] <= 16 else 1) * threads)
     t0 = time.perf_counter()
-    O.gradient_batch(pb, c["cost"], w["y0"][:pilot], w["params"][:pilot], w["t0"][:pilot], w["t1"][:pilot],
+    O.gradient_batch(pb, c["cost"], w["y0"][:pilot], params(pilot), w["t0"][:pilot], w["t1"][:pilot],
                      nthreads=threads)
     dt = time.perf_counter() - t0
     m = int(min(B, max(pilot, pilot * seconds / max(dt, 1e-6))))
     t0 = time.perf_counter()
-    O.gradient_batch(pb, c["cost"], w["y0"][:m], w["params"][:m], w["t0"][:m], w["t1"][:m], nthreads=threads)
+    O.gradient_batch(pb, c["cost"], w["y0"][:m], params(m), w["t0"][:m], w["t1"][:m], nthreads=threads)
     dt = time.perf_counter() - t0
     return {"value": m / dt, "unit": "gradients/s", "cores": threads, "kind": "port",
             "sample": f"first {m} of {B} instances of {cfg_name}, {dt:.1f} s on {threads} threads"}
@@ -214,8 +222,16 @@ def _bench(args, rank, world, local, torch, dist):
         c["budget"] = int(args.budget_gb * (1 << 30))
     dev = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")
     y0, par, t0, t1 = dev(w["y0"]), dev(w["params"]), dev(w["t0"]), dev(w["t1"])
-    s = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision=args.precision,
-               atol=c["tol"], rtol=c["tol"], ckpt_budget_bytes=c.get("budget", 0))
+    shared = dev(w["shared"]) if w["shared"] is not None else None
+
+    def make_solver(batch, precision, budget=c.get("budget", 0)):
+        sv = Solver(c["model"], c["n"], c["npar"], batch, tableau=c["tableau"], precision=precision,
+                    atol=c["tol"], rtol=c["tol"], ckpt_budget_bytes=budget)
+        if shared is not None:
+            sv.set_shared(shared, torch.empty_like(shared))
+        return sv
+
+    s = make_solver(B, args.precision)
     if not args.quick:
         s.autotune(c["cost"], y0, par, t0, t1)
     out = s.gradient(c["cost"], y0, par, t0, t1)
@@ -284,8 +300,7 @@ def _bench(args, rank, world, local, torch, dist):
 
     # the other precision modes on the same batch: throughput and gradient error vs FP64
     def run_mode(precision):
-        sm = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision=precision,
-                    atol=c["tol"], rtol=c["tol"], ckpt_budget_bytes=c.get("budget", 0))
+        sm = make_solver(B, precision)
         sm.autotune(c["cost"], y0, par, t0, t1)
         o = sm.gradient(c["cost"], y0, par, t0, t1)
         tt = []
@@ -324,9 +339,8 @@ def _bench(args, rank, world, local, torch, dist):
     err = modes[args.precision].get("grad_err_vs_fp64")
 
     # plain drop-in: the FP64 path called once per instance through the host entry point
-    M = 64
-    s1 = Solver(c["model"], c["n"], c["npar"], 1, tableau=c["tableau"], precision="fp64",
-                atol=c["tol"], rtol=c["tol"])
+    M = 64 if c["n"] <= 16 else 8
+    s1 = make_solver(1, "fp64", budget=0)
     s1.gradient_host(c["cost"], w["y0"][:1], w["params"][:1], w["t0"][:1], w["t1"][:1])
     tp = time.perf_counter()
     for b in range(M):
