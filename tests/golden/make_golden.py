@@ -1,0 +1,101 @@
+"""Generates tests/golden/reference_cases.npz from the REFERENCE ITSELF:
+its unchanged lib/include headers compiled against the project's Boost
+stand-in and linked with the AADC runtime it ships (oracle/ref/, built into
+oracle/_ref/libvaref.so by `make -C oracle/ref`).  Needs the reference
+sources at /root/reference and an x86-64 host (AADC is x86-only); the
+fixtures it writes are committed so the tests run anywhere.
+
+Cases: seeded instances of every benchmark configuration (same draws as
+vectorizedadjoint_gb300.workloads), and the reference's own GLV example
+(examples/GeneralizedLotkaVolterra/main.cpp: Cash-Karp, x0 = 0.1, t in
+[0, 10], dt = 1e-3, identity seeds Nout = N) on its data files
+data/N5/alphasfile_cpp.csv and data/N10/alphasfile_cpp.csv.
+
+Usage:  make -C oracle/ref && python tests/golden/make_golden.py
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+REF = "/root/reference"
+
+from vectorizedadjoint_gb300 import workloads as W  # noqa: E402
+
+MODEL_ID = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3}
+
+
+def load():
+    L = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libvaref.so"))
+    L.ref_solve.restype = ctypes.c_int
+    return L
+
+
+def solve(L, model, tableau, n, npar, tol, y0, p, t1, lam, mu, cap=200000):
+    nout = lam.shape[0]
+    times = np.zeros(cap + 1)
+    states = np.zeros((cap + 1, n))
+    T = ctypes.c_long()
+    yT = np.zeros(n)
+    lo = np.zeros((nout, n))
+    mo = np.zeros((nout, npar))
+    ptr = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(ctypes.c_void_p)
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (y0, p, lam, mu)]
+    rc = L.ref_solve(MODEL_ID[model], 0 if tableau == "dopri5" else 1, n, nout, npar, ctypes.c_double(tol),
+                     ctypes.c_double(tol), ctypes.c_double(1e-3), ptr(keep[0]), ptr(keep[1]),
+                     ctypes.c_double(0.0), ctypes.c_double(t1), ptr(keep[2]), ptr(keep[3]), ctypes.c_long(cap),
+                     times.ctypes.data_as(ctypes.c_void_p), states.ctypes.data_as(ctypes.c_void_p),
+                     ctypes.byref(T), yT.ctypes.data_as(ctypes.c_void_p), lo.ctypes.data_as(ctypes.c_void_p),
+                     mo.ctypes.data_as(ctypes.c_void_p))
+    assert rc == 0, rc
+    return T.value, times[:T.value + 1], states[:T.value + 1], yT, lo, mo
+
+
+def main():
+    L = load()
+    cases = []
+    # benchmark configurations: cost seeds from y(T) (sum of squares) or ones (sum)
+    for name, count in [("vdp1", 1), ("dho", 4), ("vdpb", 4), ("glv10", 3)]:
+        w = W.make(name, batch=count)
+        c = w["cfg"]
+        for b in range(count):
+            y0, p, t1 = w["y0"][b], w["params"][b], float(w["t1"][b])
+            mu = np.zeros((1, c["npar"]))
+            # forward first to get y(T) for the sum-of-squares seed
+            T, times, states, yT, _, _ = solve(L, c["model"], c["tableau"], c["n"], c["npar"], c["tol"], y0, p, t1,
+                                               np.zeros((1, c["n"])), mu)
+            lam = (2.0 * yT if c["cost"] == "sumsq" else np.ones(c["n"]))[None, :]
+            T, times, states, yT, lo, mo = solve(L, c["model"], c["tableau"], c["n"], c["npar"], c["tol"], y0, p,
+                                                 t1, lam, mu)
+            cases.append(dict(name=f"{name}[{b}]", model=c["model"], tableau=c["tableau"], n=c["n"],
+                              npar=c["npar"], tol=c["tol"], y0=y0, p=p, t1=t1, lam=lam, mu=mu, T=T, yT=yT,
+                              dy0=lo, dp=mo, times=times if name == "vdp1" else None,
+                              states=states if name == "vdp1" else None))
+    # the reference's GLV example on its own data, identity seeds (Nout = N)
+    for N in (5, 10):
+        vals = np.array([float(v) for v in open(f"{REF}/examples/GeneralizedLotkaVolterra/data/N{N}/alphasfile_cpp.csv")
+                         .read().replace("\n", ",").split(",") if v.strip()])
+        assert vals.size == N + N * N
+        y0 = np.full(N, 0.1)
+        lam, mu = np.eye(N), np.zeros((N, N + N * N))
+        for tol in (1e-6, 1e-9):
+            T, times, states, yT, lo, mo = solve(L, "glv", "ck54", N, N + N * N, tol, y0, vals, 10.0, lam, mu)
+            cases.append(dict(name=f"glv_example_N{N}_tol{tol:g}", model="glv", tableau="ck54", n=N,
+                              npar=N + N * N, tol=tol, y0=y0, p=vals, t1=10.0, lam=lam, mu=mu, T=T, yT=yT,
+                              dy0=lo, dp=mo, times=None, states=None))
+    out = {}
+    for k, cs in enumerate(cases):
+        for key, v in cs.items():
+            if v is not None:
+                out[f"c{k}_{key}"] = np.asarray(v)
+    out["count"] = np.array(len(cases))
+    path = os.path.join(ROOT, "tests", "golden", "reference_cases.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {len(cases)} cases to {path} ({os.path.getsize(path)} bytes)")
+
+
+if __name__ == "__main__":
+    main()
