@@ -316,9 +316,12 @@ def _bench(args, rank, world, local, torch, dist):
         return B / (float(np.median(tt)) * 1e-3), o
 
     def grad_err(o, o64):
+        """Per instance max|g - g64| / max(max|g64|, 1e-8 max|y0|): the floor keeps
+        damped instances whose gradient decays to ~1e-100 on a meaningful scale."""
         g = torch.cat([o["dy0"], o["dp"]], 1)
         g64 = torch.cat([o64["dy0"], o64["dp"]], 1)
-        rel = ((g - g64).abs().amax(1) / g64.abs().amax(1).clamp_min(1e-300)).cpu().numpy()
+        scale = torch.maximum(g64.abs().amax(1), 1e-8 * y0.abs().amax(1)).clamp_min(1e-300)
+        rel = ((g - g64).abs().amax(1) / scale).cpu().numpy()
         ok = (o["status"].cpu().numpy() == 0) & (o64["status"].cpu().numpy() == 0)
         same = float((o["n_acc"] == o64["n_acc"]).float().mean().item())
         return {"median": float(np.median(rel[ok])), "p99": float(np.quantile(rel[ok], 0.99)),
