@@ -98,8 +98,16 @@ typedef struct {
     int32_t max_steps;   /* accepted-step cap per instance                        */
     int32_t max_rejects; /* odeint failed_step_checker limit (500)                */
     int64_t ckpt_budget_bytes; /* HBM budget for checkpoints (0 = default 16 GiB) */
-    int32_t ckpt_stride; /* 0 = automatic; k > 1 stores every k-th accepted step
-                            and re-integrates segments during the backward sweep   */
+    int32_t ckpt_stride; /* 0 or 1: every accepted step is checkpointed (pool
+                            exhaustion -> VA_CKPT_BUDGET per instance).  k > 1:
+                            two-level checkpointing -- every k-th accepted step is
+                            stored and the backward sweep re-integrates each segment
+                            from its checkpoint into scratch (bit-identical steps,
+                            checked; one extra forward evaluation per step).  -1:
+                            automatic -- va_forward checks the pool after the sweep
+                            (synchronously) and reruns with a 4x larger stride
+                            until the checkpoints fit (up to 1024).  Strides > 1 and
+                            -1: one-thread-per-instance models only              */
     int32_t block_size;  /* 0 = autotuned / default                               */
     int32_t blocks_per_sm; /* 0 = occupancy limit                                 */
     int32_t chunk_len;   /* records per checkpoint chunk (0 = 64)                 */

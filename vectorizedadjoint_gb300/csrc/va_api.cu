@@ -19,6 +19,7 @@
 namespace {
 
 constexpr int64_t kDefaultBudget = 16LL << 30; // 16 GiB of checkpoints
+constexpr int kMaxAutoStride = 1024;            // automatic two-level stride cap
 
 struct GraphKey {
     int cost = -2;
@@ -66,6 +67,12 @@ struct va_handle {
 
     cudaGraphExec_t graph = nullptr;
     GraphKey graph_key;
+
+    // two-level checkpointing: stride, end times, re-integration scratch
+    int stride = 1;
+    double *inst_t1 = nullptr;
+    double *scratch = nullptr;
+    size_t scratch_doubles = 0;
 
     // shared-matrix bundle path (VA_MODEL_GLV_SHARED)
     const va::BundleKernelSet *bks = nullptr;
@@ -154,6 +161,7 @@ va_status ensure_buffers(va_handle *h)
     VA_CUDA(h, cudaMalloc(&h->inst_status, (size_t)B * sizeof(int)));
     VA_CUDA(h, cudaMalloc(&h->ctl, sizeof(va::Control)));
     VA_CUDA(h, cudaMemset(h->ctl, 0, sizeof(va::Control)));
+    VA_CUDA(h, cudaMalloc(&h->inst_t1, (size_t)B * sizeof(double)));
     if (h->bks) {
         const size_t NN = (size_t)h->N * h->N;
         const size_t grid = ((size_t)B + h->bks->nb - 1) / h->bks->nb;
@@ -185,6 +193,33 @@ va::BundleParams bundle_params(va_handle *h)
 }
 
 int bundle_grid(va_handle *h) { return (h->prob.batch + h->bks->nb - 1) / h->bks->nb; }
+
+// Two-level backward launch: 64-thread blocks, at most 4 per SM, so the
+// re-integration scratch stays (stride + 1) records x 256 threads per SM.
+constexpr int kTwoLevelBlock = 64, kTwoLevelBlocksPerSm = 4;
+
+int two_level_grid(va_handle *h)
+{
+    const long need = ((long)h->prob.batch + kTwoLevelBlock - 1) / kTwoLevelBlock;
+    return (int)std::max(1L, std::min(need, (long)h->sm_count * kTwoLevelBlocksPerSm));
+}
+
+// Scratch for the current stride; never called during stream capture.
+va_status ensure_scratch(va_handle *h)
+{
+    if (h->stride <= 1)
+        return VA_OK;
+    const size_t need = (size_t)two_level_grid(h) * kTwoLevelBlock * (h->stride + 1) * h->RS;
+    if (need <= h->scratch_doubles)
+        return VA_OK;
+    if (h->scratch)
+        cudaFree(h->scratch);
+    h->scratch = nullptr;
+    h->scratch_doubles = 0;
+    VA_CUDA(h, cudaMalloc(&h->scratch, need * sizeof(double)));
+    h->scratch_doubles = need;
+    return VA_OK;
+}
 
 va_status ensure_staging(va_handle *h)
 {
@@ -244,6 +279,8 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
     a.inst_T = h->inst_T;
     a.inst_last = h->inst_last;
     a.inst_status = h->inst_status;
+    a.inst_t1 = h->inst_t1;
+    a.stride = h->stride;
     a.pool = pool_of(h);
     a.ctl = h->ctl;
     if (h->bks) {
@@ -306,6 +343,19 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
         }
         h->bwd_grid = grid;
         h->bwd_block = h->N;
+        return VA_OK;
+    }
+    if (h->stride > 1) {
+        if (h->scratch_doubles < (size_t)two_level_grid(h) * kTwoLevelBlock * (h->stride + 1) * h->RS)
+            return fail(h, VA_BAD_ARGS, "two-level scratch not sized for the stride%s");
+        a.stride = h->stride;
+        a.inst_t1 = h->inst_t1;
+        a.scratch = h->scratch;
+        a.atol = h->opt.atol;
+        a.rtol = h->opt.rtol;
+        a.max_fail = h->opt.max_rejects;
+        VA_CUDA(h, cudaMemsetAsync(&h->ctl->adj_next, 0, sizeof(unsigned int), s));
+        VA_CUDA(h, launch(h->ks->bwd2[h->opt.tableau][h->opt.precision], two_level_grid(h), kTwoLevelBlock, &a, s));
         return VA_OK;
     }
     const void *fn = h->ks->bwd[h->opt.tableau][h->opt.precision];
@@ -416,9 +466,12 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
     }
     if (prob->n != N || prob->npar != P)
         return VA_BAD_ARGS;
-    if (o.ckpt_stride > 1)
-        return VA_BAD_ARGS; // two-level checkpointing is handled by the segment path
+    // checkpoint stride: -1 automatic, 0/1 every step, k > 1 every k-th step
+    // (two-level checkpointing: one-thread-per-instance models only)
+    if (o.ckpt_stride < -1 || ((o.ckpt_stride > 1 || o.ckpt_stride == -1) && !(ks && ks->tpi == 1)))
+        return VA_BAD_ARGS;
     va_handle *h = new va_handle();
+    h->stride = o.ckpt_stride > 1 ? o.ckpt_stride : 1;
     h->prob = *prob;
     h->opt = o;
     h->ks = ks;
@@ -450,7 +503,7 @@ va_status va_destroy(va_handle *h)
                     h->ctl,      h->s_y0,       h->s_par,   h->s_t0,      h->s_t1,
                     h->s_yT,     h->s_dy0,      h->s_dpar,  h->s_nacc,    h->s_status,
                     h->s_nrej,   h->s_lam,      h->s_mu,    h->At,        h->Aw,
-                    h->Atw,      h->dA_part};
+                    h->Atw,      h->dA_part,    h->inst_t1, h->scratch};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -469,7 +522,21 @@ va_status va_forward(va_handle *h, const double *y0, const double *params, const
     va_status st = ensure_buffers(h);
     if (st != VA_OK)
         return st;
-    st = enqueue_forward(h, y0, params, t0, t1, yT, n_acc, n_rej, status, (cudaStream_t)stream);
+    for (;;) {
+        st = enqueue_forward(h, y0, params, t0, t1, yT, n_acc, n_rej, status, (cudaStream_t)stream);
+        if (st != VA_OK || h->opt.ckpt_stride != -1)
+            break;
+        // automatic stride: if the pool ran out, store 4x fewer steps and rerun
+        va::Control c{};
+        VA_CUDA(h, cudaMemcpyAsync(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+        VA_CUDA(h, cudaStreamSynchronize((cudaStream_t)stream));
+        if (!c.pool_fail || h->stride >= kMaxAutoStride)
+            break;
+        h->stride *= 4;
+        drop_graph(h);
+    }
+    if (st == VA_OK)
+        st = ensure_scratch(h);
     if (st == VA_OK)
         h->forward_done = true;
     return st;
@@ -485,6 +552,9 @@ va_status va_backward(va_handle *h, const double *params, const double *lambdaT,
         return fail(h, VA_NOT_READY, "va_backward: no forward sweep has run on this handle%s");
     if (!params || !lambdaT || !dy0 || !dparams)
         return fail(h, VA_BAD_ARGS, "va_backward: null pointer%s");
+    va_status st = ensure_scratch(h);
+    if (st != VA_OK)
+        return st;
     return enqueue_backward(h, params, lambdaT, mu_direct, VA_COST_SEEDS, dy0, dparams, status,
                             (cudaStream_t)stream);
 }
@@ -502,6 +572,8 @@ va_status va_gradient(va_handle *h, int32_t cost, const double *y0, const double
     if (!y0 || !params || !t0 || !t1 || !dy0 || !dparams)
         return fail(h, VA_BAD_ARGS, "va_gradient: null pointer%s");
     va_status st = ensure_buffers(h);
+    if (st == VA_OK)
+        st = ensure_scratch(h);
     if (st != VA_OK)
         return st;
     cudaStream_t s = (cudaStream_t)stream;
@@ -683,7 +755,7 @@ va_status va_checkpoint_info(const va_handle *h, int64_t *capacity_bytes, int64_
         }
     }
     if (stride)
-        *stride = 1;
+        *stride = h->stride;
     return VA_OK;
 }
 
@@ -692,6 +764,8 @@ va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double
 {
     if (!h || instance < 0 || instance >= h->prob.batch || capacity < 0)
         return VA_BAD_ARGS;
+    if (h->stride > 1)
+        return fail(h, VA_BAD_ARGS, "va_trajectory: checkpoint stride > 1 keeps only every k-th step%s");
     if (!h->forward_done || !h->inst_T)
         return fail(h, VA_NOT_READY, "va_trajectory: no forward sweep has run%s");
     VA_CUDA(h, cudaDeviceSynchronize());
@@ -753,6 +827,8 @@ va_status va_autotune(va_handle *h, int32_t cost, const double *y0, const double
     if (st != VA_OK)
         return st;
     st = ensure_staging(h);
+    if (st == VA_OK)
+        st = ensure_scratch(h);
     if (st != VA_OK)
         return st;
     if (h->bks)

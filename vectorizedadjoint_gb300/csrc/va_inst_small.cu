@@ -28,6 +28,10 @@ static KernelSet make_set(void (*fill_fp64)(KernelSet &))
     k.bwd[1][1] = (const void *)backward_kernel<M, TabCK54, float>;
     k.bwd[0][2] = (const void *)backward_kernel<M, TabDopri5, dword>;
     k.bwd[1][2] = (const void *)backward_kernel<M, TabCK54, dword>;
+    k.bwd2[0][1] = (const void *)backward_kernel_2level<M, TabDopri5, float>;
+    k.bwd2[1][1] = (const void *)backward_kernel_2level<M, TabCK54, float>;
+    k.bwd2[0][2] = (const void *)backward_kernel_2level<M, TabDopri5, dword>;
+    k.bwd2[1][2] = (const void *)backward_kernel_2level<M, TabCK54, dword>;
     return k;
 }
 

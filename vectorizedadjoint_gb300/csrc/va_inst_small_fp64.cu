@@ -15,6 +15,8 @@ static void fill(KernelSet &k)
     k.fwd[1][0] = (const void *)forward_kernel<M, TabCK54, double>;
     k.bwd[0][0] = (const void *)backward_kernel<M, TabDopri5, double>;
     k.bwd[1][0] = (const void *)backward_kernel<M, TabCK54, double>;
+    k.bwd2[0][0] = (const void *)backward_kernel_2level<M, TabDopri5, double>;
+    k.bwd2[1][0] = (const void *)backward_kernel_2level<M, TabCK54, double>;
 }
 
 void fill_fp64_vdp(KernelSet &k) { fill<ModelVdP>(k); }

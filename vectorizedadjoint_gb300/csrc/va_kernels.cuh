@@ -72,6 +72,8 @@ struct FwdParams {
     int *inst_T;     // [B] accepted steps
     int *inst_last;  // [B] last checkpoint chunk
     int *inst_status;// [B]
+    double *inst_t1; // [B] end times (kept for segment re-integration; may be null)
+    int stride;      // store every stride-th accepted step (and the last); 1 = all
     Pool pool;
     Control *ctl;
 };
@@ -92,6 +94,12 @@ struct AdjParams {
     const int *inst_status;
     Pool pool;
     Control *ctl;
+    // two-level checkpointing (stride > 1): segment re-integration
+    int stride;
+    const double *inst_t1;   // [B]
+    double *scratch;         // per thread: (stride + 1) records
+    double atol, rtol;
+    int max_fail;
 };
 
 __host__ __device__ constexpr int record_doubles(int n) { return (2 + n + 1) & ~1; }
@@ -375,6 +383,38 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
     return num / den;
 }
 
+// State after an accepted attempt: y (FP64, what a checkpoint stores), its
+// stage-precision copy ys and k0 = f(y).  For double-word stages ys restarts
+// from the rounded FP64 value, exactly what a re-integration from a
+// checkpoint starts from, and f(y_new) is reused only when that copy equals
+// the attempt's own (it does unless a double-word split rounds at a tie).
+template <class M, class Tab, class S>
+__host__ __device__ __forceinline__ void accept_state(double (&y)[M::N], S (&ys)[M::N], S (&k0)[M::N],
+                                                      const double (&ynew)[M::N], const S (&ynew_s)[M::N],
+                                                      const S (&knew)[M::N], const S (&p)[M::P], double t)
+{
+    constexpr int N = M::N;
+    bool same = true;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        if constexpr (std::is_same<S, dword>::value) {
+            y[i] = to_d(ynew_s[i]); // the one rounding to FP64 per accepted step
+            ys[i] = from_d<S>(y[i]);
+            same = same && ys[i].hi == ynew_s[i].hi && ys[i].lo == ynew_s[i].lo;
+        } else {
+            y[i] = ynew[i];
+            ys[i] = ynew_s[i];
+        }
+    }
+    if (Tab::FSAL && same) {
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            k0[i] = knew[i];
+    } else {
+        M::template rhs<S>(ys, p, from_d<S>(t), k0);
+    }
+}
+
 // k = f(y) at an FP64 state, in stage precision.
 template <class M, class S>
 __host__ __device__ __forceinline__ void eval_rhs(const double (&y)[M::N], const S (&p)[M::P], double t,
@@ -480,11 +520,11 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
         return true;
     };
 
-    // Reserve the slot of record `count`; false if the pool ran out.
+    // Reserve the slot of the next stored record; false if the pool ran out.
     auto reserve = [&]() -> bool {
         if (chunk < 0)
             return false;
-        if (count > 0 && slot == CH) {
+        if (slot == CH) {
             int c = (int)atomicAdd(&a.ctl->pool_next, 1u);
             if (c >= a.pool.n_chunks) {
                 atomicOr(&a.ctl->pool_fail, 1u);
@@ -518,6 +558,8 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
         a.inst_T[b] = count;
         a.inst_last[b] = chunk;
         a.inst_status[b] = status;
+        if (a.inst_t1)
+            a.inst_t1[b] = t1;
         if (a.n_acc_out)
             a.n_acc_out[b] = count;
         if (a.n_rej_out)
@@ -544,12 +586,15 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
                 status = ST_MAX_STEPS;
                 continue;
             }
-            if (!reserve()) {
-                status = ST_CKPT_BUDGET;
-                continue;
+            // every stride-th accepted step is checkpointed (stride 1: all)
+            if (count % a.stride == 0) {
+                if (!reserve()) {
+                    status = ST_CKPT_BUDGET;
+                    continue;
+                }
+                write_record<N>(record_ptr<RS>(a.pool, chunk, slot), t, dt, y);
+                slot++;
             }
-            write_record<N>(record_ptr<RS>(a.pool, chunk, slot), t, dt, y);
-            slot++;
             // end clamp (runge_kutta.hpp:160-163)
             if ((t + dt) - t1 > kDblEps)
                 dt = t1 - t;
@@ -571,21 +616,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
         } else {
             t += dt;
             dt = increase_step<Tab, S>(dt, err);
-#pragma unroll
-            for (int i = 0; i < N; i++) {
-                ys[i] = ynew_s[i];
-                if constexpr (std::is_same<S, dword>::value)
-                    y[i] = to_d(ynew_s[i]); // the one rounding to FP64 per accepted step
-                else
-                    y[i] = ynew[i];
-            }
-            if constexpr (Tab::FSAL) {
-#pragma unroll
-                for (int i = 0; i < N; i++)
-                    k0[i] = knew[i];
-            } else {
-                M::template rhs<S>(ys, p, from_d<S>(t), k0);
-            }
+            accept_state<M, Tab, S>(y, ys, k0, ynew, ynew_s, knew, p, t);
             ok = true;
         }
         // failed_step_checker: at most max_fail attempts per accepted step
@@ -808,6 +839,223 @@ __global__ void __launch_bounds__(256) backward_kernel(AdjParams a)
         back_step<M, Tab, S>(y, tn, h, p, lam, mu);
         t_next = tn;
         j--;
+    }
+}
+
+// --------------------------------------------- backward sweep, two levels
+
+// Backward sweep over checkpoints stored every `stride` accepted steps (plus
+// the last).  For each segment, last first: re-run the forward controller
+// from the segment's checkpoint (t, dt, y) -- the same device code, so the
+// same bits -- for the segment's accepted steps into this thread's scratch,
+// check that it lands exactly on the next checkpoint's t and y, then run
+// back_step through the segment in reverse.  Memory: one record per stride
+// steps plus (stride + 1) scratch records per thread, for one extra forward
+// evaluation of every step.
+template <class M, class Tab, class S>
+__global__ void __launch_bounds__(256) backward_kernel_2level(AdjParams a)
+{
+    constexpr int N = M::N, P = M::P;
+    constexpr int RS = record_doubles(N);
+    const int CH = a.pool.chunk_len, SK = a.stride;
+    double *scr = a.scratch + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * (SK + 1) * RS;
+
+    int b = -1, q = 0, T = 0, R = 0, k = 0, last = -1, chunk = -1, slot = 0, L = 0, done = 0, jb = 0, fails = 0;
+    int phase = 0; // 0: re-integrate segment k, 1: back-step through it
+    double lam[N], mu[P], t = 0.0, dt = 0.0, t1 = 0.0, y[N], t_end = 0.0, y_end[N];
+    S p[P], ys[N], k0[N];
+    bool at_top = true;
+
+    // Record r of the instance: chunk r / CH of its chain.  The walk only
+    // moves backwards, one record at a time.
+    auto step_back = [&]() {
+        if (slot == 0) {
+            chunk = a.pool.chunk_prev[chunk];
+            slot = CH - 1;
+        } else {
+            slot--;
+        }
+    };
+
+    auto fail_instance = [&](int st) {
+        for (int qq = 0; qq < a.nout; qq++) {
+            const size_t o = ((size_t)b * a.nout + qq);
+            for (int i = 0; i < N; i++)
+                a.dy0[o * N + i] = __longlong_as_double(0x7ff8000000000000ll);
+            for (int kk = 0; kk < P; kk++)
+                a.dpar[o * P + kk] = __longlong_as_double(0x7ff8000000000000ll);
+        }
+        if (a.status_out)
+            a.status_out[b] = st;
+    };
+
+    // Load the start of segment k (the walk is on record k + 1) and set up
+    // its re-integration.
+    auto begin_segment = [&]() {
+        step_back();
+        double rec_t, rec_y[N];
+        const double *r = record_ptr<RS>(a.pool, chunk, slot);
+        read_record<N>(r, rec_t, rec_y);
+        t = rec_t;
+        dt = r[1];
+        const int first = k * SK;
+        L = (k == R - 2) ? T - first : SK;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            y[i] = rec_y[i];
+            ys[i] = from_d<S>(y[i]);
+            scr[2 + i] = y[i];
+        }
+        scr[0] = t;
+        M::template rhs<S>(ys, p, from_d<S>(t), k0);
+        done = 0;
+        fails = 0;
+        at_top = true;
+        phase = 0;
+    };
+
+    auto start_seed = [&]() {
+        chunk = last;
+        slot = (R - 1) % CH;
+        double yTl[N];
+        read_record<N>(record_ptr<RS>(a.pool, chunk, slot), t_end, yTl);
+        const size_t o = ((size_t)b * a.nout + q);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            y_end[i] = yTl[i];
+            lam[i] = a.cost == 0 ? 2.0 * yTl[i] : a.cost == 1 ? 1.0 : a.lambdaT[o * N + i];
+        }
+#pragma unroll
+        for (int kk = 0; kk < P; kk++)
+            mu[kk] = 0.0;
+        k = R - 2;
+        if (k >= 0)
+            begin_segment();
+    };
+
+    auto finish_seed = [&](int st) {
+        const size_t o = ((size_t)b * a.nout + q);
+        bool finite = st == ST_OK;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            a.dy0[o * N + i] = st == ST_OK ? lam[i] : __longlong_as_double(0x7ff8000000000000ll);
+            finite = finite && isfinite(lam[i]);
+        }
+#pragma unroll
+        for (int kk = 0; kk < P; kk++) {
+            const double d = a.mu_direct ? a.mu_direct[o * P + kk] : 0.0;
+            a.dpar[o * P + kk] = st == ST_OK ? d + mu[kk] : __longlong_as_double(0x7ff8000000000000ll);
+            finite = finite && isfinite(mu[kk]);
+        }
+        if (a.status_out && (q == a.nout - 1 || !finite))
+            a.status_out[b] = st != ST_OK ? st : (finite ? ST_OK : ST_NONFINITE);
+    };
+
+    auto fetch = [&]() -> bool {
+        for (;;) {
+            unsigned w = atomicAdd(&a.ctl->adj_next, 1u);
+            if ((int)w >= a.B)
+                return false;
+            b = a.order ? a.order[w] : (int)w;
+            const int st = a.inst_status[b];
+            if (st != ST_OK) {
+                fail_instance(st);
+                continue;
+            }
+#pragma unroll
+            for (int kk = 0; kk < P; kk++)
+                p[kk] = from_d<S>(a.par[(size_t)b * P + kk]);
+            T = a.inst_T[b];
+            R = (T + SK - 1) / SK + 1;
+            last = a.inst_last[b];
+            t1 = a.inst_t1[b];
+            q = 0;
+            start_seed();
+            return true;
+        }
+    };
+
+    bool alive = fetch();
+    while (alive) {
+        if (k < 0) {
+            finish_seed(ST_OK);
+            if (q + 1 < a.nout) {
+                q++;
+                start_seed();
+            } else {
+                alive = fetch();
+            }
+            continue;
+        }
+        if (phase == 0) {
+            // one attempt of the forward controller, as forward_kernel does
+            if (at_top) {
+                if ((t + dt) - t1 > kDblEps)
+                    dt = t1 - t;
+                fails = 0;
+                at_top = false;
+            }
+            double ynew[N];
+            S ynew_s[N], knew[N];
+            const double err = attempt<M, Tab, S>(y, ys, k0, p, t, dt, a.atol, a.rtol, ynew, ynew_s, knew);
+            if (err != err || fails >= a.max_fail) {
+                fail_instance(ST_RECOMPUTE_MISMATCH);
+                alive = fetch();
+                continue;
+            }
+            fails++;
+            if (err > 1.0) {
+                dt = decrease_step<Tab, S>(dt, err);
+                continue;
+            }
+            t += dt;
+            dt = increase_step<Tab, S>(dt, err);
+            accept_state<M, Tab, S>(y, ys, k0, ynew, ynew_s, knew, p, t);
+            at_top = true;
+            done++;
+            double *r = scr + (size_t)done * RS;
+            r[0] = t;
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                r[2 + i] = y[i];
+            if (done == L) {
+                // the re-integration must land exactly on the next checkpoint
+                bool same = t == t_end;
+#pragma unroll
+                for (int i = 0; i < N; i++)
+                    same = same && y[i] == y_end[i];
+                if (!same) {
+                    fail_instance(ST_RECOMPUTE_MISMATCH);
+                    alive = fetch();
+                    continue;
+                }
+                phase = 1;
+                jb = L - 1;
+            }
+            continue;
+        }
+        // phase 1: back_step through the segment, last step first
+        {
+            const double *r = scr + (size_t)jb * RS;
+            double yj[N];
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                yj[i] = r[2 + i];
+            const double tn = r[0];
+            const double h = scr[(size_t)(jb + 1) * RS] - tn;
+            back_step<M, Tab, S>(yj, tn, h, p, lam, mu);
+            jb--;
+            if (jb < 0) {
+                // the segment's start becomes the next segment's end
+                t_end = scr[0];
+#pragma unroll
+                for (int i = 0; i < N; i++)
+                    y_end[i] = scr[2 + i];
+                k--;
+                if (k >= 0)
+                    begin_segment();
+            }
+        }
     }
 }
 

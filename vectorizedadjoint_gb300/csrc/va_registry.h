@@ -10,6 +10,7 @@ struct KernelSet {
     int tpi;           // threads that carry one instance
     const void *fwd[2][3]; // [tableau][precision] -> __global__ void(FwdParams)
     const void *bwd[2][3]; // [tableau][precision] -> __global__ void(AdjParams)
+    const void *bwd2[2][3]; // two-level backward (checkpoint stride > 1); null if unsupported
 };
 
 const KernelSet *kernels_vdp();
