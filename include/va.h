@@ -111,7 +111,9 @@ typedef struct {
     int32_t block_size;  /* 0 = autotuned / default                               */
     int32_t blocks_per_sm; /* 0 = occupancy limit                                 */
     int32_t chunk_len;   /* records per checkpoint chunk (0 = 64)                 */
-    int32_t reserved[6];
+    int32_t schedule;    /* 0: longest instances first (forward: by t1 - t0;
+                            backward: by accepted steps), 1: index order          */
+    int32_t reserved[5];
 } va_options;
 
 /* Fills the reference's defaults: DOPRI5, FP64, atol=rtol=1e-6, dt0=1e-3,

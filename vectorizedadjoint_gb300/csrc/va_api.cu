@@ -14,6 +14,7 @@
 #include "../../include/va.h"
 #include "va_bundle.cuh"
 #include "va_kernels.cuh"
+#include "va_order.h"
 #include "va_registry.h"
 
 namespace {
@@ -67,6 +68,9 @@ struct va_handle {
 
     cudaGraphExec_t graph = nullptr;
     GraphKey graph_key;
+
+    // longest-first work order of the two sweeps
+    int *order_fwd = nullptr, *order_bwd = nullptr, *order_work = nullptr;
 
     // two-level checkpointing: stride, end times, re-integration scratch
     int stride = 1;
@@ -162,6 +166,11 @@ va_status ensure_buffers(va_handle *h)
     VA_CUDA(h, cudaMalloc(&h->ctl, sizeof(va::Control)));
     VA_CUDA(h, cudaMemset(h->ctl, 0, sizeof(va::Control)));
     VA_CUDA(h, cudaMalloc(&h->inst_t1, (size_t)B * sizeof(double)));
+    if (!h->bks && h->opt.schedule == 0) {
+        VA_CUDA(h, cudaMalloc(&h->order_fwd, (size_t)B * sizeof(int)));
+        VA_CUDA(h, cudaMalloc(&h->order_bwd, (size_t)B * sizeof(int)));
+        VA_CUDA(h, cudaMalloc(&h->order_work, va::order_work_ints() * sizeof(int)));
+    }
     if (h->bks) {
         const size_t NN = (size_t)h->N * h->N;
         const size_t grid = ((size_t)B + h->bks->nb - 1) / h->bks->nb;
@@ -303,6 +312,11 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
     const void *fn = h->ks->fwd[h->opt.tableau][h->opt.precision];
     if (h->fwd_grid <= 0)
         h->fwd_grid = grid_for(h, fn, h->fwd_block, a.B);
+    if (h->order_fwd) {
+        va::OrderArgs o{a.B, nullptr, t0, t1, h->order_work, h->order_fwd};
+        VA_CUDA(h, va::enqueue_order(o, s));
+        a.order = h->order_fwd;
+    }
     VA_CUDA(h, cudaMemsetAsync(h->ctl, 0, sizeof(va::Control), s));
     VA_CUDA(h, launch(fn, h->fwd_grid, h->fwd_block, &a, s));
     return VA_OK;
@@ -328,6 +342,11 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
     a.inst_status = h->inst_status;
     a.pool = pool_of(h);
     a.ctl = h->ctl;
+    if (h->order_bwd) {
+        va::OrderArgs o{a.B, h->inst_T, nullptr, nullptr, h->order_work, h->order_bwd};
+        VA_CUDA(h, va::enqueue_order(o, s));
+        a.order = h->order_bwd;
+    }
     if (h->bks) {
         va::BundleParams bp = bundle_params(h);
         bp.g = a;
@@ -503,7 +522,8 @@ va_status va_destroy(va_handle *h)
                     h->ctl,      h->s_y0,       h->s_par,   h->s_t0,      h->s_t1,
                     h->s_yT,     h->s_dy0,      h->s_dpar,  h->s_nacc,    h->s_status,
                     h->s_nrej,   h->s_lam,      h->s_mu,    h->At,        h->Aw,
-                    h->Atw,      h->dA_part,    h->inst_t1, h->scratch};
+                    h->Atw,      h->dA_part,    h->inst_t1, h->scratch, h->order_fwd,
+                    h->order_bwd, h->order_work};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);

@@ -157,6 +157,8 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
         b = shfl(nb, src, mask);
         if (b >= a.B)
             return false;
+        if (a.order)
+            b = a.order[b];
         y[0] = a.y0[(size_t)b * NT + li];
         M::template load_params<S>(a.par + (size_t)b * PT, li, p);
         t = a.t0[b];

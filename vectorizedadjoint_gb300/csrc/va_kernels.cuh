@@ -74,6 +74,7 @@ struct FwdParams {
     int *inst_status;// [B]
     double *inst_t1; // [B] end times (kept for segment re-integration; may be null)
     int stride;      // store every stride-th accepted step (and the last); 1 = all
+    const int *order;// [B] work order (may be null = index order)
     Pool pool;
     Control *ctl;
 };
@@ -490,6 +491,8 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
         b = (int)atomicAdd(&a.ctl->fwd_next, 1u);
         if (b >= a.B)
             return false;
+        if (a.order)
+            b = a.order[b];
 #pragma unroll
         for (int i = 0; i < N; i++)
             y[i] = a.y0[(size_t)b * N + i];

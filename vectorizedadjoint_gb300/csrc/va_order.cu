@@ -1,0 +1,102 @@
+// Longest-first work order for the persistent sweeps.  A lane that takes a
+// long instance late holds the whole kernel open (the tail); handing out the
+// longest instances first removes most of it.  The forward sweep orders by
+// the horizon t1 - t0 (known before it runs), the backward sweep by the
+// accepted-step count the forward produced.  A counting sort over 4096
+// buckets (descending) builds the permutation on the device, so it can sit
+// inside the captured graph.  The atomics here only decide the order; each
+// instance's result does not depend on it.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "va_order.h"
+
+namespace va {
+
+namespace {
+
+constexpr int kBuckets = 4096;
+
+__device__ __forceinline__ int horizon_bucket(double h)
+{
+    // 64 buckets per octave of t1 - t0, from 2^-32 to 2^32
+    if (!(h > 0.0))
+        return 0;
+    const double l = log2(h);
+    const int k = (int)((l + 32.0) * 64.0);
+    return k < 0 ? 0 : k >= kBuckets ? kBuckets - 1 : k;
+}
+
+__device__ __forceinline__ int key_of(const OrderArgs &a, int b)
+{
+    if (a.steps)
+        return a.steps[b] < kBuckets ? (a.steps[b] < 0 ? 0 : a.steps[b]) : kBuckets - 1;
+    return horizon_bucket(a.t1[b] - a.t0[b]);
+}
+
+__global__ void order_hist(OrderArgs a)
+{
+    __shared__ int h[kBuckets];
+    for (int i = threadIdx.x; i < kBuckets; i += blockDim.x)
+        h[i] = 0;
+    __syncthreads();
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < a.B; b += gridDim.x * blockDim.x)
+        atomicAdd(&h[key_of(a, b)], 1);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kBuckets; i += blockDim.x)
+        if (h[i])
+            atomicAdd(&a.work[i], h[i]);
+}
+
+// Exclusive scan from the top bucket down: offset of bucket k = number of
+// instances in buckets > k.  One block of 1024 threads, 4 buckets each.
+__global__ void order_scan(OrderArgs a)
+{
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    int v[4], s = 0;
+    for (int j = 0; j < 4; j++) {
+        v[j] = a.work[kBuckets - 1 - (t * 4 + j)];
+        s += v[j];
+    }
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int x = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += x;
+        __syncthreads();
+    }
+    int run = t ? part[t - 1] : 0;
+    for (int j = 0; j < 4; j++) {
+        a.work[kBuckets + (kBuckets - 1 - (t * 4 + j))] = run;
+        run += v[j];
+    }
+}
+
+__global__ void order_scatter(OrderArgs a)
+{
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < a.B; b += gridDim.x * blockDim.x) {
+        const int pos = atomicAdd(&a.work[kBuckets + key_of(a, b)], 1);
+        a.order[pos] = b;
+    }
+}
+
+} // namespace
+
+size_t order_work_ints() { return 2 * kBuckets; }
+
+cudaError_t enqueue_order(const OrderArgs &a, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(int) * kBuckets, s);
+    if (e != cudaSuccess)
+        return e;
+    const int grid = (a.B + 255) / 256 < 1024 ? (a.B + 255) / 256 : 1024;
+    order_hist<<<grid, 256, 0, s>>>(a);
+    order_scan<<<1, 1024, 0, s>>>(a);
+    order_scatter<<<grid, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+} // namespace va

@@ -1,0 +1,22 @@
+// Longest-first work order for the persistent sweeps (va_order.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace va {
+
+struct OrderArgs {
+    int B;
+    const int *steps;  // backward: accepted steps per instance (or null)
+    const double *t0;  // forward: horizons t1 - t0 (used when steps is null)
+    const double *t1;
+    int *work;         // order_work_ints() scratch ints
+    int *order;        // [B] output permutation, longest first
+};
+
+size_t order_work_ints();
+cudaError_t enqueue_order(const OrderArgs &a, cudaStream_t s);
+
+} // namespace va
