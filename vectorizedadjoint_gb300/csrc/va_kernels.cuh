@@ -589,8 +589,8 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
                 status = ST_MAX_STEPS;
                 continue;
             }
-            // every stride-th accepted step is checkpointed (stride 1: all)
-            if (count % a.stride == 0) {
+            // every stride-th accepted step is checkpointed (stride <= 1: all)
+            if (a.stride <= 1 || count % a.stride == 0) {
                 if (!reserve()) {
                     status = ST_CKPT_BUDGET;
                     continue;

@@ -167,6 +167,7 @@ extern "C" va_status va_gradient_noalloc(int32_t model, int32_t tableau, int32_t
     fa.inst_T = inst_T;
     fa.inst_last = inst_last;
     fa.inst_status = inst_status;
+    fa.stride = 1; // every accepted step is checkpointed
     fa.pool = pool;
     fa.ctl = ctl;
     const void *ffn = ks->fwd[tableau][precision];
