@@ -156,6 +156,20 @@ def run_reference(args, rank, world):
                                     "d2h_bytes_per_step": 0}}), flush=True)
 
 
+def max_over_ranks(ms, world, dist, torch, device="cpu"):
+    """The job's step time: the slowest rank's (ranks run independent replicas)."""
+    if world <= 1:
+        return ms
+    tt = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_throughput(batch_per_rank, ms, world):
+    """Whole-job gradients/s: every rank differentiates its own batch (weak scaling)."""
+    return world * batch_per_rank / (ms * 1e-3)
+
+
 def fp64_peak_tflops(torch):
     """FP64 peak of this GPU measured as cuBLAS DGEMM throughput (best of 5)."""
     n = 4096
@@ -253,14 +267,10 @@ def _bench(args, rank, world, local, torch, dist):
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
     torch.cuda.synchronize()
-    ms = float(np.mean(times))
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(float(np.mean(times)), world, dist, torch, device="cuda")
     status = out["status"].cpu().numpy()
     n_acc = out["n_acc"].cpu().numpy().astype(np.int64)
-    value = world * B / (ms * 1e-3)
+    value = replica_throughput(B, ms, world)
     if args.quick:
         if rank == 0:
             print(json.dumps({"metric": "adjoint gradients/s", "value": value, "unit": "gradients/s",

@@ -400,8 +400,15 @@ __host__ __device__ __forceinline__ void accept_state(double (&y)[M::N], S (&ys)
     for (int i = 0; i < N; i++) {
         if constexpr (std::is_same<S, dword>::value) {
             y[i] = to_d(ynew_s[i]); // the one rounding to FP64 per accepted step
-            ys[i] = from_d<S>(y[i]);
-            same = same && ys[i].hi == ynew_s[i].hi && ys[i].lo == ynew_s[i].lo;
+            // from_d(y) splits hi + lo (exact in FP64) as hi' = RN_float(hi + lo)
+            // and lo' = the rest: it returns the same pair exactly when the
+            // float sum hi + lo rounds back to hi, which one FP32 add decides
+            if (ynew_s[i].hi + ynew_s[i].lo == ynew_s[i].hi) {
+                ys[i] = ynew_s[i];
+            } else {
+                ys[i] = from_d<S>(y[i]);
+                same = false;
+            }
         } else {
             y[i] = ynew[i];
             ys[i] = ynew_s[i];
