@@ -84,4 +84,26 @@ __host__ __device__ __forceinline__ dword &operator+=(dword &x, dword y) { retur
 
 __host__ __device__ __forceinline__ dword dabs(dword x) { return x.hi < 0.0f ? -x : x; }
 
+// x / y: one long-division step on the leading words (DWDivDW2 of the same
+// paper: t = xh / yh, remainder x - t y by DWTimesFP, correction / yh,
+// Fast2Sum), relative error O(u^2).
+__host__ __device__ __forceinline__ dword operator/(dword x, dword y)
+{
+    const float th = x.hi / y.hi;
+    const dword r = y * th;
+    const float ph = x.hi - r.hi;
+    const float dl = x.lo - r.lo;
+    const float d = ph + dl;
+    const float tl = d / y.hi;
+    dword z;
+    fast_two_sum(th, tl, z.hi, z.lo);
+    return z;
+}
+
+// x > y for normalized double-words (leading words first)
+__host__ __device__ __forceinline__ bool dw_greater(dword x, dword y)
+{
+    return x.hi > y.hi || (x.hi == y.hi && x.lo > y.lo);
+}
+
 } // namespace va

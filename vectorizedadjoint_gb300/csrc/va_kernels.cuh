@@ -20,6 +20,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <type_traits>
 
 #include "va_dword.cuh"
@@ -341,8 +342,9 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
         }
         if constexpr (Tab::FSAL)
             M::template rhs<S>(ynew_s, p, from_d<S>(t + dt), knew);
-        // error vector to FP64 at full stage precision: a coarser estimate
-        // (leading word only) flips accept/reject decisions near err = 1
+        // error vector at full stage precision: a coarser estimate (leading
+        // word only) flips accept/reject decisions near err = 1
+        S eacc[N];
 #pragma unroll
         for (int i = 0; i < N; i++) {
             S acc = S(0);
@@ -352,7 +354,29 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
                     acc = madd(S(Tab::e(j)), K[j][i], acc);
             if constexpr (Tab::FSAL)
                 acc = madd(S(Tab::E_NEW), knew[i], acc);
-            e[i] = dt * to_d(acc);
+            eacc[i] = acc;
+            if constexpr (!std::is_same<S, dword>::value)
+                e[i] = dt * to_d(acc);
+        }
+        if constexpr (std::is_same<S, dword>::value) {
+            // The norm in double-word arithmetic on the FP32 pipe (relative
+            // error ~2^-44, the decision quality of FP64), rounded once to FP64
+            // for the FP64 controller: the FP64 pipe of this part is scarce and
+            // the conversions an FP64 norm needs cost more than its arithmetic.
+            const dword sat = dword(atol), srt = dword(rtol);
+            dword m = dword(0);
+            bool nan = false;
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+                const dword num = dabs(eacc[i] * sdt);
+                const dword den = sat + srt * (dabs(ys[i]) + sdt * dabs(k0[i]));
+                const dword r = num / den;
+                nan = nan || r.hi != r.hi;
+                if (dw_greater(r, m))
+                    m = r;
+            }
+            (void)e;
+            return nan ? std::numeric_limits<double>::quiet_NaN() : to_d(m);
         }
     }
     const double adt = fabs(dt);
