@@ -424,10 +424,12 @@ __host__ __device__ __forceinline__ void accept_state(double (&y)[M::N], S (&ys)
     for (int i = 0; i < N; i++) {
         if constexpr (std::is_same<S, dword>::value) {
             y[i] = to_d(ynew_s[i]); // the one rounding to FP64 per accepted step
-            // from_d(y) splits hi + lo (exact in FP64) as hi' = RN_float(hi + lo)
-            // and lo' = the rest: it returns the same pair exactly when the
-            // float sum hi + lo rounds back to hi, which one FP32 add decides
-            if (ynew_s[i].hi + ynew_s[i].lo == ynew_s[i].hi) {
+            // from_d(y) returns the same pair exactly when y = hi + lo holds
+            // without rounding (false for about 1 in 32 components: lo more
+            // than 29 binades below hi carries bits under the FP64 grid) and
+            // the float sum hi + lo rounds back to hi (false only at ties)
+            if ((y[i] - (double)ynew_s[i].hi) == (double)ynew_s[i].lo &&
+                ynew_s[i].hi + ynew_s[i].lo == ynew_s[i].hi) {
                 ys[i] = ynew_s[i];
             } else {
                 ys[i] = from_d<S>(y[i]);
