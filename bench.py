@@ -201,6 +201,8 @@ def main():
     ap.add_argument("--quick", action="store_true",
                     help="only the timed steps of one mode (no autotune sweep, other modes, plain, e2e or CPU "
                          "legs): the small case used for ncu captures")
+    ap.add_argument("--tune", action="store_true",
+                    help="with --quick: pick the launch shape by the autotune sweep first, as the full run does")
     ap.add_argument("--batch", type=int, default=0, help="override the workload's batch size")
     ap.add_argument("--budget-gb", type=float, default=0.0, help="checkpoint pool budget (GiB)")
     args = ap.parse_args()
@@ -246,7 +248,7 @@ def _bench(args, rank, world, local, torch, dist):
         return sv
 
     s = make_solver(B, args.precision)
-    if not args.quick:
+    if not args.quick or args.tune:
         s.autotune(c["cost"], y0, par, t0, t1)
     out = s.gradient(c["cost"], y0, par, t0, t1)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
@@ -261,9 +263,13 @@ def _bench(args, rank, world, local, torch, dist):
         for _ in range(args.steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            # the NVTX range lets a profiler select the timed launches
+            # (ncu --nvtx --nvtx-include "timed_step/")
+            torch.cuda.nvtx.range_push("timed_step")
             e0.record(stream)
             s.gradient(c["cost"], y0, par, t0, t1, out=out)
             e1.record(stream)
+            torch.cuda.nvtx.range_pop()
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
     torch.cuda.synchronize()

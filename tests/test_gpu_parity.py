@@ -98,6 +98,39 @@ def test_fp64_accepted_step_sequence(oracle, cuda, name, B):
     s.close()
 
 
+@pytest.mark.parametrize("name,B", [("vdpb", 64), ("dho", 32), ("glv10", 16)])
+def test_mixed_dw_trajectory(oracle, cuda, name, B):
+    """mixed_dw checkpoints (double-word states for the one-thread models)
+    read back through trajectory(): the last record is y(T) exactly, and
+    times and states follow the oracle's on instances with its step count.
+    (The error estimate cancels to ~1e-3 of the stage slopes, so its
+    double-word value carries ~1e-7 relative error and the step sizes drift
+    from the FP64 ones by ~1e-8: hence the loose bounds.)"""
+    w = W.make(name, batch=B)
+    c = w["cfg"]
+    s = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision="mixed_dw",
+               atol=c["tol"], rtol=c["tol"])
+    f = s.forward(dev(w["y0"]), dev(w["params"]), dev(w["t0"]), dev(w["t1"]))
+    torch.cuda.synchronize()
+    pb = oracle.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"])
+    yT = f["yT"].cpu().numpy()
+    checked = 0
+    for b in range(0, B, max(1, B // 8)):
+        fw = oracle.forward(pb, w["y0"][b], w["params"][b], 0.0, w["t1"][b])
+        t, dt, y = s.trajectory(b)
+        if len(t) != fw["n_acc"] + 1:
+            continue
+        checked += 1
+        scale = max(1.0, float(np.abs(fw["states"]).max()))
+        assert t[0] == 0.0 and t[-1] == w["t1"][b]
+        np.testing.assert_allclose(t, fw["times"], rtol=1e-6, atol=0)
+        np.testing.assert_allclose(y, fw["states"], rtol=0, atol=1e-6 * scale)
+        np.testing.assert_array_equal(y[-1], yT[b])
+        assert (dt > 0).all()
+    assert checked >= 4
+    s.close()
+
+
 @pytest.mark.parametrize("name,B", [("vdp1", 1), ("dho", 64), ("vdpb", 64), ("glv10", 16)])
 def test_fp64_vs_libm_pow_controller(oracle, cuda, name, B):
     """Against the oracle with the C library's pow (odeint's std::pow): same

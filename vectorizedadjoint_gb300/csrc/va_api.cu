@@ -798,6 +798,15 @@ va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double
     if (st != VA_OK || last < 0)
         return fail(h, (va_status)st, "va_trajectory: instance has no complete record%s");
     const int CH = h->chunk_len, RS = h->RS, N = h->N;
+    // mixed_dw records of the one-thread kernels hold double-words
+    // (float pairs {hi, lo} in 8 bytes) after the FP64 time
+    const bool dw = h->ks && h->ks->dw_records && h->opt.precision == VA_PREC_MIXED_DW;
+    auto field = [dw](double v) {
+        if (!dw)
+            return v;
+        const va::dword d = va::dw_unpack(v);
+        return (double)d.hi + (double)d.lo;
+    };
     std::vector<double> buf((size_t)CH * RS);
     int chunk = last;
     int first_in_chunk = (T / CH) * CH; // record index at slot 0 of the last chunk
@@ -812,10 +821,10 @@ va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double
             if (t)
                 t[j] = buf[(size_t)k * RS];
             if (dt)
-                dt[j] = buf[(size_t)k * RS + 1];
+                dt[j] = field(buf[(size_t)k * RS + 1]);
             if (y)
                 for (int i = 0; i < N; i++)
-                    y[(size_t)j * N + i] = buf[(size_t)k * RS + 2 + i];
+                    y[(size_t)j * N + i] = field(buf[(size_t)k * RS + 2 + i]);
         }
         int prev = -1;
         VA_CUDA(h, cudaMemcpy(&prev, h->chunk_prev + chunk, sizeof(int), cudaMemcpyDeviceToHost));

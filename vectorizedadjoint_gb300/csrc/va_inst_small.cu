@@ -1,7 +1,9 @@
 // Kernel tables of the one-thread-per-instance models.  This unit holds the
-// reduced-precision sweeps (float and double-word stages); the FP64 sweeps
-// come from va_inst_small_fp64.cu, which is built without FMA contraction.
+// reduced-precision sweeps (float stages; double-word state and stages); the
+// FP64 sweeps come from va_inst_small_fp64.cu, which is built without FMA
+// contraction.
 #include "va_kernels.cuh"
+#include "va_kernels_dw.cuh"
 #include "va_models.cuh"
 #include "va_registry.h"
 
@@ -22,16 +24,17 @@ static KernelSet make_set(void (*fill_fp64)(KernelSet &))
     fill_fp64(k);
     k.fwd[0][1] = (const void *)forward_kernel<M, TabDopri5, float>;
     k.fwd[1][1] = (const void *)forward_kernel<M, TabCK54, float>;
-    k.fwd[0][2] = (const void *)forward_kernel<M, TabDopri5, dword>;
-    k.fwd[1][2] = (const void *)forward_kernel<M, TabCK54, dword>;
+    k.fwd[0][2] = (const void *)forward_kernel_dw<M, TabDopri5>;
+    k.fwd[1][2] = (const void *)forward_kernel_dw<M, TabCK54>;
     k.bwd[0][1] = (const void *)backward_kernel<M, TabDopri5, float>;
     k.bwd[1][1] = (const void *)backward_kernel<M, TabCK54, float>;
-    k.bwd[0][2] = (const void *)backward_kernel<M, TabDopri5, dword>;
-    k.bwd[1][2] = (const void *)backward_kernel<M, TabCK54, dword>;
+    k.bwd[0][2] = (const void *)backward_kernel_dw<M, TabDopri5>;
+    k.bwd[1][2] = (const void *)backward_kernel_dw<M, TabCK54>;
     k.bwd2[0][1] = (const void *)backward_kernel_2level<M, TabDopri5, float>;
     k.bwd2[1][1] = (const void *)backward_kernel_2level<M, TabCK54, float>;
-    k.bwd2[0][2] = (const void *)backward_kernel_2level<M, TabDopri5, dword>;
-    k.bwd2[1][2] = (const void *)backward_kernel_2level<M, TabCK54, dword>;
+    k.bwd2[0][2] = (const void *)backward_kernel_2level_dw<M, TabDopri5>;
+    k.bwd2[1][2] = (const void *)backward_kernel_2level_dw<M, TabCK54>;
+    k.dw_records = true;
     return k;
 }
 

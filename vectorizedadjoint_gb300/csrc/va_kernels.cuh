@@ -164,12 +164,9 @@ __host__ __device__ __forceinline__ float f32_from_bits(int32_t i)
 // result has the same bits on any IEEE machine, which the oracle relies on
 // for a bit-exact comparison of step sequences.  a >= 1e30 (decrease only)
 // returns 0, which the 0.2 limiter turns into the same factor pow would.
-template <int K, int FP64_STEPS = 2>
-__host__ __device__ __forceinline__ double inv_root(double a)
+template <int K>
+__host__ __device__ __forceinline__ float inv_root_f32(float af)
 {
-    if (!(a < 1e30))
-        return 0.0;
-    const float af = (float)a;
     constexpr int32_t c = (int32_t)(((int64_t)(K + 1) * 0x3F800000LL) / K);
     float x = f32_from_bits(c - f32_bits(af) / K);
     const float rk = 1.0f / (float)K;
@@ -182,6 +179,15 @@ __host__ __device__ __forceinline__ double inv_root(double a)
         const float r = fmaf(-af, xk, 1.0f);
         x = fmaf(x * r, rk, x);
     }
+    return x;
+}
+
+template <int K, int FP64_STEPS = 2>
+__host__ __device__ __forceinline__ double inv_root(double a)
+{
+    if (!(a < 1e30))
+        return 0.0;
+    const float x = inv_root_f32<K>((float)a);
     double xd = (double)x;
 #pragma unroll
     for (int it = 0; it < FP64_STEPS; it++) {

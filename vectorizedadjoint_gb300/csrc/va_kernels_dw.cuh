@@ -1,0 +1,787 @@
+// Double-word sweeps of the one-thread-per-instance models.
+//
+// The mixed_dw variant of the forward and backward sweeps keeps FP64 for the
+// time coordinate alone: the state y, the stages, the step size and its
+// controller, the error norm, the adjoint (lambda, mu) and the checkpoint
+// records are double-words (pairs of floats, ~48 significant bits).  On this
+// part FP64 issues at 1/64 of the FP32 rate and the FP64 <-> FP32
+// conversions share that narrow pipe, so a sweep that rounds its state to
+// FP64 every step (to store it) and runs its controller in FP64 spends more
+// of the FP64 pipe on conversions than the stages spend on the FP32 pipe.
+//
+// Sums of products -- the stage combinations y + dt sum_j a_mj K_j, the
+// solution and error combinations, the adjoint accumulations -- go through
+// the compensated accumulator dacc (va_dword.cuh): ~12 FP32 operations per
+// term against ~29 for a double-word multiply followed by a double-word add,
+// at the same O(u^2) accuracy.
+//
+// The algorithms are those of va_kernels.cuh: odeint 1.74's controlled
+// stepper with its default error checker and step adjuster (forward), the
+// reference's back_prop_step (lib/include/backpropagation.hpp:160-229,
+// backward); only the arithmetic type differs.  Records keep the FP64
+// layout's size: [t_n (FP64), dt_n (double-word), y_n (double-words)], each
+// double-word packed into one 8-byte slot (dw_pack).
+#pragma once
+
+#include "va_kernels.cuh"
+
+namespace va {
+
+struct DwTol {
+    dword atol, rtol;
+};
+
+__host__ __device__ __forceinline__ dword dw_nan() { return dword(f32_from_bits(0x7fc00000), 0.0f); }
+
+// ------------------------------------------------------------- controller
+
+// a^(-1/K) for a double-word a > 0: inv_root's FP32 iteration on the leading
+// word (~1e-7), then one Newton step x + x (1 - a x^K) / K with the residual
+// formed in double-word: relative error ~4e-14, the accuracy of the single
+// FP64 Newton step the float-stage path takes.  a >= 1e30 returns 0, which
+// the 0.2 limiter of decrease_dw turns into the factor pow would give.
+template <int K>
+__host__ __device__ __forceinline__ dword inv_root_dw(dword a)
+{
+    if (!(a.hi < 1e30f))
+        return dword(0.0f, 0.0f);
+    const float x = inv_root_f32<K>(a.hi);
+    dword xk(x, 0.0f);
+#pragma unroll
+    for (int k = 1; k < K; k++)
+        xk = xk * x;
+    dacc r{1.0f, 0.0f};
+    dacc_fma(r, -a, xk);
+    const dword res = dacc_get(r);
+    const float corr = fmul_rn(fmul_rn(x, res.hi), 1.0f / (float)K);
+    dword z;
+    fast_two_sum(x, corr, z.hi, z.lo);
+    return z;
+}
+
+// odeint default_step_adjuster::decrease_step: dt * max(0.9 err^(-1/(q-1)), 0.2)
+template <class Tab>
+__host__ __device__ __forceinline__ dword decrease_dw(dword dt, dword err)
+{
+    const dword f = dword(9.0 / 10.0) * inv_root_dw<Tab::ERROR_ORDER - 1>(err);
+    const dword lim = dword(1.0 / 5.0);
+    return dt * (dw_greater(f, lim) ? f : lim);
+}
+
+// odeint default_step_adjuster::increase_step:
+//   if err < 0.5: dt * 0.9 max(err, 5^-p)^(-1/p)
+template <class Tab>
+__host__ __device__ __forceinline__ dword increase_dw(dword dt, dword err)
+{
+    static_assert(Tab::STEPPER_ORDER == 5, "floor constant assumes a fifth-order stepper");
+    if (dw_less(err, dword(0.5))) {
+        const dword fl = dword(1.0 / 3125.0);
+        const dword e = dw_greater(fl, err) ? fl : err;
+        return dt * (dword(9.0 / 10.0) * inv_root_dw<Tab::STEPPER_ORDER>(e));
+    }
+    return dt;
+}
+
+// ---------------------------------------------------------- stage algebra
+
+// sum_j w_j K_j[i] over the nonzero compile-time weights w_j = W(j), j < J
+template <int J, class W, int NS, int N>
+__host__ __device__ __forceinline__ dacc wsum_dw(W w, const dword (&K)[NS][N], int i)
+{
+    dacc s{0.0f, 0.0f};
+    bool first = true;
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+        const double c = w(j);
+        if (c != 0.0) {
+            if (first)
+                s = dacc_mul_k(c, K[j][i]);
+            else
+                dacc_fma_k(s, c, K[j][i]);
+            first = false;
+        }
+    }
+    return s;
+}
+
+// y + dt s, rounded to a double-word
+__host__ __device__ __forceinline__ dword axpy_dw(dword y, dword dt, dacc s)
+{
+    dacc r = dacc_of(y);
+    dacc_fma(r, dt, dacc_get(s));
+    return dacc_get(r);
+}
+
+// X_m = y + dt sum_{j<m} a_mj K_j (the order odeint's scale_sum and the
+// reference's compute_intermediate_states use, backpropagation.hpp:36-45)
+template <class Tab, int N>
+__host__ __device__ __forceinline__ void stage_dw(int m, const dword (&y)[N], const dword (&K)[Tab::S][N],
+                                                  dword dt, dword (&X)[N])
+{
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        dacc s{0.0f, 0.0f};
+        bool first = true;
+#pragma unroll
+        for (int j = 0; j < Tab::S - 1; j++) {
+            if (j < m && Tab::a(m, j) != 0.0) {
+                if (first)
+                    s = dacc_mul_k(Tab::a(m, j), K[j][i]);
+                else
+                    dacc_fma_k(s, Tab::a(m, j), K[j][i]);
+                first = false;
+            }
+        }
+        X[i] = axpy_dw(y[i], dt, s);
+    }
+}
+
+struct BWeights {
+    template <class Tab>
+    struct of {
+        __host__ __device__ constexpr double operator()(int j) const { return Tab::b(j); }
+    };
+};
+struct EWeights {
+    template <class Tab>
+    struct of {
+        __host__ __device__ constexpr double operator()(int j) const { return Tab::e(j); }
+    };
+};
+
+// One attempted step from (y, k0 = f(y), t) with step dt: y_new, k_new =
+// f(y_new) (FSAL pairs) and the error norm
+//   max_i |dt e_i| / (atol + rtol (|y_i| + |dt| |k0_i|))
+// (odeint's default_error_checker with a_x = a_dxdt = 1), NaN if any ratio is.
+template <class M, class Tab>
+__host__ __device__ __forceinline__ dword attempt_dw(const dword (&y)[M::N], const dword (&k0)[M::N],
+                                                     const dword (&p)[M::P], dword t, dword dt,
+                                                     const DwTol &tol, dword (&ynew)[M::N],
+                                                     dword (&knew)[M::N])
+{
+    constexpr int N = M::N, NS = Tab::S;
+    dword K[NS][N];
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        K[0][i] = k0[i];
+#pragma unroll
+    for (int m = 1; m < NS; m++) {
+        dword X[N];
+        stage_dw<Tab, N>(m, y, K, dt, X);
+        M::template rhs<dword>(X, p, t + dt * dword(Tab::c(m)), K[m]);
+    }
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        ynew[i] = axpy_dw(y[i], dt, wsum_dw<NS>(typename BWeights::template of<Tab>(), K, i));
+    if constexpr (Tab::FSAL)
+        M::template rhs<dword>(ynew, p, t + dt, knew);
+    const dword adt = dabs(dt);
+    const dword rdt = tol.rtol * adt;
+    dword worst(0.0f, 0.0f);
+    bool nan = false;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        dacc e = wsum_dw<NS>(typename EWeights::template of<Tab>(), K, i);
+        if constexpr (Tab::FSAL)
+            dacc_fma_k(e, Tab::E_NEW, knew[i]);
+        const dword num = dabs(dacc_get(e) * adt);
+        dacc d = dacc_of(tol.atol);
+        dacc_fma(d, tol.rtol, dabs(y[i]));
+        dacc_fma(d, rdt, dabs(k0[i]));
+        const dword r = num / dacc_get(d);
+        nan = nan || r.hi != r.hi;
+        if (dw_greater(r, worst))
+            worst = r;
+    }
+    return nan ? dw_nan() : worst;
+}
+
+// ----------------------------------------------------------------- records
+
+template <int N>
+__device__ __forceinline__ void write_record_dw(double *r, double t, dword dt, const dword (&y)[N])
+{
+    constexpr int RS = record_doubles(N);
+    double v[RS];
+    v[0] = t;
+    v[1] = dw_pack(dt);
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        v[2 + i] = dw_pack(y[i]);
+#pragma unroll
+    for (int i = 2 + N; i < RS; i++)
+        v[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < RS; i += 2)
+        *reinterpret_cast<double2 *>(r + i) = make_double2(v[i], v[i + 1]);
+}
+
+template <int N>
+__device__ __forceinline__ void read_record_dw(const double *r, double &t, dword &dt, dword (&y)[N])
+{
+    constexpr int RS = record_doubles(N);
+    double v[RS];
+#pragma unroll
+    for (int i = 0; i < RS; i += 2) {
+        double2 q = __ldcs(reinterpret_cast<const double2 *>(r + i));
+        v[i] = q.x;
+        v[i + 1] = q.y;
+    }
+    t = v[0];
+    dt = dw_unpack(v[1]);
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        y[i] = dw_unpack(v[2 + i]);
+}
+
+__host__ __device__ __forceinline__ bool dw_same(dword x, dword y) { return x.hi == y.hi && x.lo == y.lo; }
+
+// ------------------------------------------------------------ forward sweep
+
+// forward_kernel with double-word state.  The end clamp and the loop test
+// stay in FP64 (less_with_sign, runge_kutta.hpp:155-163); an accepted step
+// that was clamped to the end lands on t1 itself.
+template <class M, class Tab>
+__global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
+{
+    constexpr int N = M::N, P = M::P;
+    constexpr int RS = record_doubles(N);
+    const int CH = a.pool.chunk_len;
+    const DwTol tol{dword(a.atol), dword(a.rtol)};
+
+    int b = -1;
+    double t = 0.0, t1 = 0.0;
+    dword y[N], k0[N], p[P], dt;
+    int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
+    bool at_top = true, to_end = false;
+
+    auto fetch = [&]() -> bool {
+        b = (int)atomicAdd(&a.ctl->fwd_next, 1u);
+        if (b >= a.B)
+            return false;
+        if (a.order)
+            b = a.order[b];
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            y[i] = dword(a.y0[(size_t)b * N + i]);
+#pragma unroll
+        for (int k = 0; k < P; k++)
+            p[k] = dword(a.par[(size_t)b * P + k]);
+        t = a.t0[b];
+        t1 = a.t1[b];
+        dt = dword(a.dt0);
+        count = rej = fails = 0;
+        status = ST_OK;
+        at_top = true;
+        slot = 0;
+        chunk = (int)atomicAdd(&a.ctl->pool_next, 1u);
+        if (chunk >= a.pool.n_chunks) {
+            status = ST_CKPT_BUDGET;
+            chunk = -1;
+            atomicOr(&a.ctl->pool_fail, 1u);
+        } else {
+            a.pool.chunk_prev[chunk] = -1;
+        }
+        M::template rhs<dword>(y, p, dword(t), k0);
+        return true;
+    };
+
+    auto reserve = [&]() -> bool {
+        if (chunk < 0)
+            return false;
+        if (slot == CH) {
+            int c = (int)atomicAdd(&a.ctl->pool_next, 1u);
+            if (c >= a.pool.n_chunks) {
+                atomicOr(&a.ctl->pool_fail, 1u);
+                return false;
+            }
+            a.pool.chunk_prev[c] = chunk;
+            chunk = c;
+            slot = 0;
+        }
+        return true;
+    };
+
+    auto finish = [&]() {
+        if (status == ST_OK) {
+            if (reserve()) {
+                write_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), t, dt, y);
+                slot++;
+            } else {
+                status = ST_CKPT_BUDGET;
+            }
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                if (!isfinite(y[i].hi))
+                    status = ST_NONFINITE;
+        }
+        if (a.yT) {
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                a.yT[(size_t)b * N + i] = to_d(y[i]);
+        }
+        a.inst_T[b] = count;
+        a.inst_last[b] = chunk;
+        a.inst_status[b] = status;
+        if (a.inst_t1)
+            a.inst_t1[b] = t1;
+        if (a.n_acc_out)
+            a.n_acc_out[b] = count;
+        if (a.n_rej_out)
+            a.n_rej_out[b] = rej;
+        if (a.status_out)
+            a.status_out[b] = status;
+    };
+
+    bool alive = fetch();
+    while (alive) {
+        if (status != ST_OK) {
+            finish();
+            alive = fetch();
+            continue;
+        }
+        if (at_top) {
+            if (!(t1 - t > kDblEps)) {
+                finish();
+                alive = fetch();
+                continue;
+            }
+            if (count >= a.max_steps) {
+                status = ST_MAX_STEPS;
+                continue;
+            }
+            if (a.stride <= 1 || count % a.stride == 0) {
+                if (!reserve()) {
+                    status = ST_CKPT_BUDGET;
+                    continue;
+                }
+                write_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), t, dt, y);
+                slot++;
+            }
+            to_end = (t + to_d(dt)) - t1 > kDblEps;
+            if (to_end)
+                dt = dword(t1 - t);
+            fails = 0;
+            at_top = false;
+        }
+        dword ynew[N], knew[N];
+        const dword err = attempt_dw<M, Tab>(y, k0, p, dword(t), dt, tol, ynew, knew);
+        bool ok;
+        if (err.hi != err.hi) {
+            status = ST_NONFINITE;
+            continue;
+        }
+        if (dw_greater(err, dword(1.0f, 0.0f))) {
+            dt = decrease_dw<Tab>(dt, err);
+            rej++;
+            to_end = false;
+            ok = false;
+        } else {
+            t = to_end ? t1 : t + to_d(dt);
+            dt = increase_dw<Tab>(dt, err);
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                y[i] = ynew[i];
+            if constexpr (Tab::FSAL) {
+#pragma unroll
+                for (int i = 0; i < N; i++)
+                    k0[i] = knew[i];
+            } else {
+                M::template rhs<dword>(y, p, dword(t), k0);
+            }
+            ok = true;
+        }
+        if (fails >= a.max_fail) {
+            status = ST_MAX_REJECTS;
+            continue;
+        }
+        fails++;
+        if (ok) {
+            count++;
+            at_top = true;
+        } else if (!(dt.hi > 0.0f) || !isfinite(dt.hi)) {
+            status = ST_NONFINITE;
+        }
+    }
+}
+
+// ----------------------------------------------------------- backward sweep
+
+// back_step in double-word: lambda_{n+1} -> lambda_n, mu += the step's
+// parameter adjoint.  Kbar_m and the lambda / mu increments are compensated
+// accumulators, finished when stage m's VJP needs Kbar_m.
+template <class M, class Tab>
+__host__ __device__ __forceinline__ void back_step_dw(const dword (&y)[M::N], dword tn, dword h,
+                                                      const dword (&p)[M::P], dword (&lam)[M::N],
+                                                      dword (&mu)[M::PG])
+{
+    constexpr int N = M::N, PG = M::PG, NS = Tab::S;
+    // K[NS - 1] stays unset: the stages read K_j for j < m only, and the
+    // VJPs need the stage values, not the last slope
+    dword K[NS][N];
+    dword X[NS][N];
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        X[0][i] = y[i];
+    // stages from y_n (compute_intermediate_states, :24-64)
+#pragma unroll
+    for (int m = 0; m < NS; m++) {
+        if (m > 0)
+            stage_dw<Tab, N>(m, y, K, h, X[m]);
+        if (m < NS - 1)
+            M::template rhs<dword>(X[m], p, tn + h * dword(Tab::c(m)), K[m]);
+    }
+    // seeds Kbar_m = (b_m h) lambda (:178-184)
+    dacc Kb[NS][N];
+#pragma unroll
+    for (int m = 0; m < NS; m++) {
+        if (Tab::b(m) != 0.0) {
+            const dword bh = dacc_get(dacc_mul_k(Tab::b(m), h));
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                Kb[m][i] = dacc_mul(bh, lam[i]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                Kb[m][i] = dacc{0.0f, 0.0f};
+        }
+    }
+    dacc dl[N], dm[PG];
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        dl[i] = dacc_of(lam[i]);
+#pragma unroll
+    for (int k = 0; k < PG; k++)
+        dm[k] = dacc_of(mu[k]);
+    // stages s..1 (:196-224): ybar += J^T Kbar_m, Kbar_k += a_mk h J^T Kbar_m,
+    // mu += J_p^T Kbar_m
+#pragma unroll
+    for (int m = NS - 1; m >= 0; m--) {
+        dword w[N], gx[N], gp[PG];
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            w[i] = dacc_get(Kb[m][i]);
+        M::template vjp<dword>(w, X[m], p, tn + h * dword(Tab::c(m)), gx, gp);
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            dacc_add(dl[i], gx[i]);
+            if (m > 0) {
+                const dword g = gx[i] * h;
+#pragma unroll
+                for (int k = 0; k < NS - 1; k++)
+                    if (k < m && Tab::a(m, k) != 0.0)
+                        dacc_fma_k(Kb[k][i], Tab::a(m, k), g);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < PG; k++)
+            dacc_add(dm[k], gp[k]);
+    }
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        lam[i] = dacc_get(dl[i]);
+#pragma unroll
+    for (int k = 0; k < PG; k++)
+        mu[k] = dacc_get(dm[k]);
+}
+
+// cost seeds lambda_T from the last record's y_T
+template <int N>
+__device__ __forceinline__ void seed_lambda_dw(const AdjParams &a, size_t o, const dword (&yT)[N], dword (&lam)[N])
+{
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        if (a.cost == 0)
+            lam[i] = dword(2.0f * yT[i].hi, 2.0f * yT[i].lo); // 2 y(T), exact
+        else if (a.cost == 1)
+            lam[i] = dword(1.0f, 0.0f);
+        else
+            lam[i] = dword(a.lambdaT[o * N + i]);
+    }
+}
+
+template <int N, int P>
+__device__ __forceinline__ void fail_outputs(const AdjParams &a, int b)
+{
+    for (int qq = 0; qq < a.nout; qq++) {
+        const size_t o = ((size_t)b * a.nout + qq);
+        for (int i = 0; i < N; i++)
+            a.dy0[o * N + i] = __longlong_as_double(0x7ff8000000000000ll);
+        for (int k = 0; k < P; k++)
+            a.dpar[o * P + k] = __longlong_as_double(0x7ff8000000000000ll);
+    }
+}
+
+// dy0 = lambda_0, dparams = mu_direct + mu (backpropagation.hpp:317-321)
+template <int N, int P>
+__device__ __forceinline__ void write_seed_dw(const AdjParams &a, int b, int q, const dword (&lam)[N],
+                                              const dword (&mu)[P])
+{
+    const size_t o = ((size_t)b * a.nout + q);
+    bool finite = true;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const double v = to_d(lam[i]);
+        a.dy0[o * N + i] = v;
+        finite = finite && isfinite(v);
+    }
+#pragma unroll
+    for (int k = 0; k < P; k++) {
+        const double d = a.mu_direct ? a.mu_direct[o * P + k] : 0.0;
+        const double v = d + to_d(mu[k]);
+        a.dpar[o * P + k] = v;
+        finite = finite && isfinite(v);
+    }
+    if (a.status_out && (q == a.nout - 1 || !finite))
+        a.status_out[b] = finite ? ST_OK : ST_NONFINITE;
+}
+
+template <class M, class Tab>
+__global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
+{
+    constexpr int N = M::N, P = M::P;
+    static_assert(M::PG == M::P, "parameter adjoint covers every parameter");
+    constexpr int RS = record_doubles(N);
+    const int CH = a.pool.chunk_len;
+
+    int b = -1, q = 0, j = -1, chunk = -1, slot = 0, T = 0, last = -1;
+    double t_next = 0.0;
+    dword lam[N], mu[P], p[P];
+
+    auto start_seed = [&]() {
+        chunk = last;
+        slot = T % a.pool.chunk_len;
+        dword yTl[N], dtr;
+        read_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), t_next, dtr, yTl);
+        seed_lambda_dw<N>(a, (size_t)b * a.nout + q, yTl, lam);
+#pragma unroll
+        for (int k = 0; k < P; k++)
+            mu[k] = dword(0.0f, 0.0f);
+        j = T - 1;
+    };
+
+    auto fetch = [&]() -> bool {
+        for (;;) {
+            unsigned w = atomicAdd(&a.ctl->adj_next, 1u);
+            if ((int)w >= a.B)
+                return false;
+            b = a.order ? a.order[w] : (int)w;
+            const int st = a.inst_status[b];
+            if (st != ST_OK) {
+                fail_outputs<N, P>(a, b);
+                if (a.status_out)
+                    a.status_out[b] = st;
+                continue;
+            }
+#pragma unroll
+            for (int k = 0; k < P; k++)
+                p[k] = dword(a.par[(size_t)b * P + k]);
+            T = a.inst_T[b];
+            last = a.inst_last[b];
+            q = 0;
+            start_seed();
+            return true;
+        }
+    };
+
+    bool alive = fetch();
+    while (alive) {
+        if (j < 0) {
+            write_seed_dw<N, P>(a, b, q, lam, mu);
+            if (q + 1 < a.nout) {
+                q++;
+                start_seed();
+            } else {
+                alive = fetch();
+            }
+            continue;
+        }
+        if (slot == 0) {
+            chunk = a.pool.chunk_prev[chunk];
+            slot = CH - 1;
+        } else {
+            slot--;
+        }
+        dword y[N], dtr;
+        double tn;
+        read_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), tn, dtr, y);
+        back_step_dw<M, Tab>(y, dword(tn), dword(t_next - tn), p, lam, mu);
+        t_next = tn;
+        j--;
+    }
+}
+
+// --------------------------------------------- backward sweep, two levels
+
+// backward_kernel_2level with double-word state: segments re-run from their
+// checkpoint's exact double-words (t, dt, y), so the re-integration
+// reproduces the forward's bits and lands on the next checkpoint.  (The
+// restart evaluates k_1 = f(y) afresh; the built-in models do not read t,
+// so it equals the forward's FSAL value.)
+template <class M, class Tab>
+__global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
+{
+    constexpr int N = M::N, P = M::P;
+    static_assert(M::PG == M::P, "parameter adjoint covers every parameter");
+    constexpr int RS = record_doubles(N);
+    const int CH = a.pool.chunk_len, SK = a.stride;
+    double *scr = a.scratch + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * (SK + 1) * RS;
+    const DwTol tol{dword(a.atol), dword(a.rtol)};
+
+    int b = -1, q = 0, T = 0, R = 0, k = 0, last = -1, chunk = -1, slot = 0, L = 0, done = 0, jb = 0, fails = 0;
+    int phase = 0; // 0: re-integrate segment k, 1: back-step through it
+    double t = 0.0, t1 = 0.0, t_end = 0.0;
+    dword lam[N], mu[P], p[P], y[N], k0[N], y_end[N], dt;
+    bool at_top = true, to_end = false;
+
+    auto step_back = [&]() {
+        if (slot == 0) {
+            chunk = a.pool.chunk_prev[chunk];
+            slot = CH - 1;
+        } else {
+            slot--;
+        }
+    };
+
+    auto fail_instance = [&](int st) {
+        fail_outputs<N, P>(a, b);
+        if (a.status_out)
+            a.status_out[b] = st;
+    };
+
+    auto begin_segment = [&]() {
+        step_back();
+        read_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), t, dt, y);
+        const int first = k * SK;
+        L = (k == R - 2) ? T - first : SK;
+        write_record_dw<N>(scr, t, dt, y);
+        M::template rhs<dword>(y, p, dword(t), k0);
+        done = 0;
+        fails = 0;
+        at_top = true;
+        phase = 0;
+    };
+
+    auto start_seed = [&]() {
+        chunk = last;
+        slot = (R - 1) % CH;
+        dword dtr;
+        read_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), t_end, dtr, y_end);
+        seed_lambda_dw<N>(a, (size_t)b * a.nout + q, y_end, lam);
+#pragma unroll
+        for (int kk = 0; kk < P; kk++)
+            mu[kk] = dword(0.0f, 0.0f);
+        k = R - 2;
+        if (k >= 0)
+            begin_segment();
+    };
+
+    auto fetch = [&]() -> bool {
+        for (;;) {
+            unsigned w = atomicAdd(&a.ctl->adj_next, 1u);
+            if ((int)w >= a.B)
+                return false;
+            b = a.order ? a.order[w] : (int)w;
+            const int st = a.inst_status[b];
+            if (st != ST_OK) {
+                fail_instance(st);
+                continue;
+            }
+#pragma unroll
+            for (int kk = 0; kk < P; kk++)
+                p[kk] = dword(a.par[(size_t)b * P + kk]);
+            T = a.inst_T[b];
+            R = (T + SK - 1) / SK + 1;
+            last = a.inst_last[b];
+            t1 = a.inst_t1[b];
+            q = 0;
+            start_seed();
+            return true;
+        }
+    };
+
+    bool alive = fetch();
+    while (alive) {
+        if (k < 0) {
+            write_seed_dw<N, P>(a, b, q, lam, mu);
+            if (q + 1 < a.nout) {
+                q++;
+                start_seed();
+            } else {
+                alive = fetch();
+            }
+            continue;
+        }
+        if (phase == 0) {
+            // one attempt of the forward controller, as forward_kernel_dw does
+            if (at_top) {
+                to_end = (t + to_d(dt)) - t1 > kDblEps;
+                if (to_end)
+                    dt = dword(t1 - t);
+                fails = 0;
+                at_top = false;
+            }
+            dword ynew[N], knew[N];
+            const dword err = attempt_dw<M, Tab>(y, k0, p, dword(t), dt, tol, ynew, knew);
+            if (err.hi != err.hi || fails >= a.max_fail) {
+                fail_instance(ST_RECOMPUTE_MISMATCH);
+                alive = fetch();
+                continue;
+            }
+            fails++;
+            if (dw_greater(err, dword(1.0f, 0.0f))) {
+                dt = decrease_dw<Tab>(dt, err);
+                to_end = false;
+                continue;
+            }
+            t = to_end ? t1 : t + to_d(dt);
+            dt = increase_dw<Tab>(dt, err);
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                y[i] = ynew[i];
+            if constexpr (Tab::FSAL) {
+#pragma unroll
+                for (int i = 0; i < N; i++)
+                    k0[i] = knew[i];
+            } else {
+                M::template rhs<dword>(y, p, dword(t), k0);
+            }
+            at_top = true;
+            done++;
+            write_record_dw<N>(scr + (size_t)done * RS, t, dt, y);
+            if (done == L) {
+                // the re-integration must land exactly on the next checkpoint
+                bool same = t == t_end;
+#pragma unroll
+                for (int i = 0; i < N; i++)
+                    same = same && dw_same(y[i], y_end[i]);
+                if (!same) {
+                    fail_instance(ST_RECOMPUTE_MISMATCH);
+                    alive = fetch();
+                    continue;
+                }
+                phase = 1;
+                jb = L - 1;
+            }
+            continue;
+        }
+        // phase 1: back_step through the segment, last step first
+        {
+            dword yj[N], dtr;
+            double tn, tn1;
+            read_record_dw<N>(scr + (size_t)jb * RS, tn, dtr, yj);
+            tn1 = scr[(size_t)(jb + 1) * RS];
+            back_step_dw<M, Tab>(yj, dword(tn), dword(tn1 - tn), p, lam, mu);
+            jb--;
+            if (jb < 0) {
+                // the segment's start becomes the next segment's end
+                read_record_dw<N>(scr, t_end, dtr, y_end);
+                k--;
+                if (k >= 0)
+                    begin_segment();
+            }
+        }
+    }
+}
+
+} // namespace va

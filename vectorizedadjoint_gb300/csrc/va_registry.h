@@ -11,6 +11,7 @@ struct KernelSet {
     const void *fwd[2][3]; // [tableau][precision] -> __global__ void(FwdParams)
     const void *bwd[2][3]; // [tableau][precision] -> __global__ void(AdjParams)
     const void *bwd2[2][3]; // two-level backward (checkpoint stride > 1); null if unsupported
+    bool dw_records;        // mixed_dw records hold double-words (t stays FP64)
 };
 
 const KernelSet *kernels_vdp();
