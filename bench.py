@@ -5,14 +5,14 @@ Default workload: the Van der Pol batch (262,144 instances, mu = 10^U[-1,1],
 x0 ~ U[-2,2]^2, t in [0,20], DOPRI5, atol = rtol = 1e-6), the configuration
 the batched-vs-plain target is quoted on; seeded synthetic inputs.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--config vdpb|dho|glv10|vdp1]
-                  [--precision mixed|fp64] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config vdpb|dho|glv10|glv256|vdp1]
+                  [--precision mixed_dw|mixed|fp64] [--impl ours|reference]
 
 One JSON line on rank 0.  `value` = gradients/s of va_gradient with inputs
 resident in HBM (CUDA events around each step, L2 flushed between steps);
 `e2e` = the same through va_gradient_host (host buffers, copies inside the
-timed region); `roofline` = the dominant sweep kernel's algorithmic FLOP rate
-against the FP64 FMA peak measured in the same run (cuBLAS DGEMM);
+timed region); `roofline` = the dominant sweep kernel's FLOP rate against
+the peak of the pipe it runs on, measured in the same run (roofline_of);
 `cpu_baseline` = the CPU port of the reference algorithm (oracle/) on the
 host cores, on a bounded sample.
 """
@@ -51,6 +51,18 @@ def flops(model, tableau, n, attempts, accepted):
     fwd = t["s"] * cf + 2 * n * (t["a"] + t["b"] + t["e"]) + 6 * n + 30
     adj = t["s"] * cf + 2 * n * t["a"] + t["s"] * cv + 2 * n * (t["a"] + t["b"]) + n * t["s"]
     return fwd * attempts, adj * accepted
+
+
+# FP32 FLOPs the double-word sweeps execute per forward attempt and per
+# backward step (FADD + FMUL + 2 FFMA, thread level), counted by ncu on the
+# one-thread-per-instance kernels at the named workload's acceptance ratio
+# (profiles/forward_kernel_dw_vdpb.md, profiles/backward_kernel_dw_vdpb.md).
+# Double-word arithmetic is FADD-heavy (2Sum chains), so its FLOP ceiling
+# sits near half the FFMA peak.
+DW_FP32_FLOPS = {
+    ("vdp", "dopri5"): (1709.0, 2670.5),
+    ("dho", "ck54"): (1445.8, None),
+}
 
 
 class Clocks:
@@ -170,11 +182,25 @@ def replica_throughput(batch_per_rank, ms, world):
     return world * batch_per_rank / (ms * 1e-3)
 
 
+def fp32_peak_tflops(torch):
+    """FP32 (non-tensor) peak of this GPU measured as cuBLAS SGEMM throughput
+    with TF32 off (best of 5)."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        return gemm_tflops(torch, torch.float32, 8192)
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
 def fp64_peak_tflops(torch):
     """FP64 peak of this GPU measured as cuBLAS DGEMM throughput (best of 5)."""
-    n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    return gemm_tflops(torch, torch.float64, 4096)
+
+
+def gemm_tflops(torch, dtype, n):
+    a = torch.randn(n, n, dtype=dtype, device="cuda")
+    b = torch.randn(n, n, dtype=dtype, device="cuda")
     for _ in range(2):
         torch.matmul(a, b)
     torch.cuda.synchronize()
@@ -187,6 +213,50 @@ def fp64_peak_tflops(torch):
         e1.synchronize()
         best = min(best, e0.elapsed_time(e1))
     return 2 * n ** 3 / (best * 1e-3) / 1e12
+
+
+# DRAM bytes per launch of the one-thread double-word kernels on the Van der
+# Pol batch (262,144 instances), one ncu capture each: the forward writes the
+# checkpoints (32 B per accepted step), the backward reads them back.
+DW_TRAFFIC = {("vdpb", "forward"): 20.04e6 + 1367.69e6, ("vdpb", "backward"): 1421.82e6 + 9.21e6}
+
+
+def roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted):
+    """Roofline of the dominant sweep kernel.  fp64: algorithmic FP64 FLOPs
+    against cuBLAS DGEMM.  mixed_dw: the FP32 FLOPs the double-word
+    arithmetic executes (ncu-counted per attempt / per step, scaled by this
+    run's attempts and steps) against cuBLAS SGEMM; mixed: the algorithmic
+    count, executed in FP32, against SGEMM.  Every mode also reports the
+    FP64-equivalent rate (algorithmic FP64 FLOPs / time) against DGEMM."""
+    fwd_dom = fms >= bms
+    kernel, ms = ("forward", fms) if fwd_dom else ("backward", bms)
+    alg = fl_f if fwd_dom else fl_b
+    peak64 = fp64_peak_tflops(torch)
+    equiv = alg / (ms * 1e-3) / 1e12
+    out = {"kernel": kernel, "unit": "TFLOP/s", "launch_ms": ms, "forward_ms": fms, "backward_ms": bms,
+           "traffic": DW_TRAFFIC.get((args.config, kernel)) if args.precision == "mixed_dw" else None,
+           "fp64_equivalent": {"achieved": equiv, "dgemm_peak": peak64, "ratio": equiv / peak64}}
+    dgemm = "cuBLAS DGEMM 4096^3 measured in this run (FP64 is absent from the measured-peaks file)"
+    sgemm = "cuBLAS SGEMM 8192^3, TF32 off, measured in this run (FP32 is absent from the measured-peaks file)"
+    per = DW_FP32_FLOPS.get((c["model"], c["tableau"]), (None, None))[0 if fwd_dom else 1]
+    if args.precision == "fp64":
+        out.update(bound="fp64", achieved=equiv, peak=peak64, peak_source=dgemm, flops_per_launch=alg,
+                   flop_count="algorithmic FP64 FLOPs (FMA = 2) of stages, VJPs and error norm")
+    elif args.precision == "mixed" or per is not None:
+        fl = alg if args.precision == "mixed" else per * (attempts if fwd_dom else accepted)
+        peak32 = fp32_peak_tflops(torch)
+        out.update(bound="fp32", achieved=fl / (ms * 1e-3) / 1e12, peak=peak32, peak_source=sgemm,
+                   flops_per_launch=fl,
+                   flop_count=("algorithmic FLOPs executed in FP32" if args.precision == "mixed" else
+                               f"{per} FP32 FLOPs per {'attempt' if fwd_dom else 'step'} of the double-word "
+                               "arithmetic (ncu instruction counts, FFMA = 2)"))
+    else:
+        out.update(bound="fp64-equivalent", achieved=equiv, peak=peak64, peak_source=dgemm,
+                   flops_per_launch=alg,
+                   flop_count="algorithmic FP64 FLOPs done in double-word arithmetic (its FP32 count is "
+                              "not measured for this kernel)")
+    out["frac"] = out["achieved"] / out["peak"]
+    return out
 
 
 def main():
@@ -308,11 +378,10 @@ def _bench(args, rank, world, local, torch, dist):
         fw_ms.append(e0.elapsed_time(e1))
         bw_ms.append(e1.elapsed_time(e2))
     n_rej = f["n_rej"].cpu().numpy().astype(np.int64)
-    fl_f, fl_b = flops(c["model"], c["tableau"], c["n"], int((n_acc + n_rej).sum()), int(n_acc.sum()))
+    attempts, accepted = int((n_acc + n_rej).sum()), int(n_acc.sum())
+    fl_f, fl_b = flops(c["model"], c["tableau"], c["n"], attempts, accepted)
     fms, bms = float(np.median(fw_ms)), float(np.median(bw_ms))
-    peak = fp64_peak_tflops(torch)
-    dom = ("forward", fl_f, fms) if fms >= bms else ("backward", fl_b, bms)
-    achieved = dom[1] / (dom[2] * 1e-3) / 1e12
+    roofline = roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted)
 
     # the other precision modes on the same batch: throughput and gradient error vs FP64
     def run_mode(precision):
@@ -404,13 +473,10 @@ def _bench(args, rank, world, local, torch, dist):
                        "l2": "flushed between timed steps (256 MB write)",
                        "launch": s.launch(), "status_ok": int((status == 0).sum())},
             "e2e": {"value": e2e, "unit": "gradients/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": 2 * args.steps,
-            "roofline": {"bound": "fp64", "kernel": dom[0], "achieved": achieved, "peak": peak,
-                         "unit": "TFLOP/s", "frac": achieved / peak,
-                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 is absent from "
-                                        "the measured-peaks file)",
-                         "flops_per_launch": dom[1], "launch_ms": dom[2], "traffic": None,
-                         "forward_ms": fms, "backward_ms": bms},
+            # per gradient: forward order (3) + forward + backward order (3) +
+            # backward; shared-matrix bundles: prepare + forward + backward + dA reduce
+            "gpu_launches": (4 if c["model"] == "glv_shared" else 8) * args.steps,
+            "roofline": roofline,
             "fp64_batched": fp64_value,
             "modes": modes,
             "plain_fp64_per_instance": plain,

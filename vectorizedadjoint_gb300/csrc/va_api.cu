@@ -69,8 +69,9 @@ struct va_handle {
     cudaGraphExec_t graph = nullptr;
     GraphKey graph_key;
 
-    // longest-first work order of the two sweeps
-    int *order_fwd = nullptr, *order_bwd = nullptr, *order_work = nullptr;
+    // longest-first work order of the two sweeps; inst_work[B] (+ flag) holds
+    // the last forward sweep's attempt counts, the next forward's order key
+    int *order_fwd = nullptr, *order_bwd = nullptr, *order_work = nullptr, *inst_work = nullptr;
 
     // two-level checkpointing: stride, end times, re-integration scratch
     int stride = 1;
@@ -170,6 +171,9 @@ va_status ensure_buffers(va_handle *h)
         VA_CUDA(h, cudaMalloc(&h->order_fwd, (size_t)B * sizeof(int)));
         VA_CUDA(h, cudaMalloc(&h->order_bwd, (size_t)B * sizeof(int)));
         VA_CUDA(h, cudaMalloc(&h->order_work, va::order_work_ints() * sizeof(int)));
+        // attempts per instance of the last forward sweep, then its valid flag
+        VA_CUDA(h, cudaMalloc(&h->inst_work, ((size_t)B + 1) * sizeof(int)));
+        VA_CUDA(h, cudaMemset(h->inst_work + B, 0, sizeof(int)));
     }
     if (h->bks) {
         const size_t NN = (size_t)h->N * h->N;
@@ -313,9 +317,12 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
     if (h->fwd_grid <= 0)
         h->fwd_grid = grid_for(h, fn, h->fwd_block, a.B);
     if (h->order_fwd) {
-        va::OrderArgs o{a.B, nullptr, t0, t1, h->order_work, h->order_fwd};
+        const int *valid = h->inst_work + a.B;
+        va::OrderArgs o{a.B, nullptr, t0, t1, h->inst_work, valid, h->order_work, h->order_fwd};
         VA_CUDA(h, va::enqueue_order(o, s));
         a.order = h->order_fwd;
+        a.inst_work = h->inst_work;
+        a.work_valid = h->inst_work + a.B;
     }
     VA_CUDA(h, cudaMemsetAsync(h->ctl, 0, sizeof(va::Control), s));
     VA_CUDA(h, launch(fn, h->fwd_grid, h->fwd_block, &a, s));
@@ -343,7 +350,7 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
     a.pool = pool_of(h);
     a.ctl = h->ctl;
     if (h->order_bwd) {
-        va::OrderArgs o{a.B, h->inst_T, nullptr, nullptr, h->order_work, h->order_bwd};
+        va::OrderArgs o{a.B, h->inst_T, nullptr, nullptr, nullptr, nullptr, h->order_work, h->order_bwd};
         VA_CUDA(h, va::enqueue_order(o, s));
         a.order = h->order_bwd;
     }
@@ -523,7 +530,7 @@ va_status va_destroy(va_handle *h)
                     h->s_yT,     h->s_dy0,      h->s_dpar,  h->s_nacc,    h->s_status,
                     h->s_nrej,   h->s_lam,      h->s_mu,    h->At,        h->Aw,
                     h->Atw,      h->dA_part,    h->inst_t1, h->scratch, h->order_fwd,
-                    h->order_bwd, h->order_work};
+                    h->order_bwd, h->order_work, h->inst_work};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);

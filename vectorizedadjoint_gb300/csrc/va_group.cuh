@@ -223,6 +223,7 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
             a.inst_T[b] = count;
             a.inst_last[b] = chunk;
             a.inst_status[b] = status;
+            note_work(a, b, count + rej);
             if (a.n_acc_out)
                 a.n_acc_out[b] = count;
             if (a.n_rej_out)

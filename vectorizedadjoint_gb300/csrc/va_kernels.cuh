@@ -76,9 +76,21 @@ struct FwdParams {
     double *inst_t1; // [B] end times (kept for segment re-integration; may be null)
     int stride;      // store every stride-th accepted step (and the last); 1 = all
     const int *order;// [B] work order (may be null = index order)
+    int *inst_work;  // [B] attempts (accepted + rejected) of this sweep, the next
+                     // sweep's length estimate (may be null)
+    int *work_valid; // set to 1 once inst_work holds a sweep's counts (may be null)
     Pool pool;
     Control *ctl;
 };
+
+// Record an instance's attempt count for the next forward sweep's order.
+__device__ __forceinline__ void note_work(const FwdParams &a, int b, int attempts)
+{
+    if (a.inst_work) {
+        a.inst_work[b] = attempts;
+        *a.work_valid = 1;
+    }
+}
 
 struct AdjParams {
     int B;
@@ -600,6 +612,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
         a.inst_T[b] = count;
         a.inst_last[b] = chunk;
         a.inst_status[b] = status;
+        note_work(a, b, count + rej);
         if (a.inst_t1)
             a.inst_t1[b] = t1;
         if (a.n_acc_out)

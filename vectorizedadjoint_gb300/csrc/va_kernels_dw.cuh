@@ -33,6 +33,25 @@ struct DwTol {
 
 __host__ __device__ __forceinline__ dword dw_nan() { return dword(f32_from_bits(0x7fc00000), 0.0f); }
 
+// (double)f by integer operations for zero and normal f: rebias the exponent
+// (127 -> 1023) and shift the 23 fraction bits to the top of the 52.  The
+// FP64 pipe's own conversion is as scarce as its arithmetic.  Subnormal,
+// infinite and NaN f take the hardware conversion.  Exact, like the cast.
+__device__ __forceinline__ double f2d_int(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if ((u & 0x7fffffffu) == 0u)
+        return __hiloint2double((int)(u & 0x80000000u), 0);
+    if (e == 0u || e == 0xffu)
+        return (double)f;
+    const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+// hi + lo rounded to FP64, as to_d, without FP64-pipe conversions
+__device__ __forceinline__ double to_d_int(dword v) { return f2d_int(v.hi) + f2d_int(v.lo); }
+
 // ------------------------------------------------------------- controller
 
 // a^(-1/K) for a double-word a > 0: inv_root's FP32 iteration on the leading
@@ -323,6 +342,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
         a.inst_T[b] = count;
         a.inst_last[b] = chunk;
         a.inst_status[b] = status;
+        note_work(a, b, count + rej);
         if (a.inst_t1)
             a.inst_t1[b] = t1;
         if (a.n_acc_out)
@@ -358,7 +378,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
                 write_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), t, dt, y);
                 slot++;
             }
-            to_end = (t + to_d(dt)) - t1 > kDblEps;
+            to_end = (t + to_d_int(dt)) - t1 > kDblEps;
             if (to_end)
                 dt = dword(t1 - t);
             fails = 0;
@@ -377,7 +397,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
             to_end = false;
             ok = false;
         } else {
-            t = to_end ? t1 : t + to_d(dt);
+            t = to_end ? t1 : t + to_d_int(dt);
             dt = increase_dw<Tab>(dt, err);
 #pragma unroll
             for (int i = 0; i < N; i++)
@@ -715,7 +735,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
         if (phase == 0) {
             // one attempt of the forward controller, as forward_kernel_dw does
             if (at_top) {
-                to_end = (t + to_d(dt)) - t1 > kDblEps;
+                to_end = (t + to_d_int(dt)) - t1 > kDblEps;
                 if (to_end)
                     dt = dword(t1 - t);
                 fails = 0;
@@ -734,7 +754,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
                 to_end = false;
                 continue;
             }
-            t = to_end ? t1 : t + to_d(dt);
+            t = to_end ? t1 : t + to_d_int(dt);
             dt = increase_dw<Tab>(dt, err);
 #pragma unroll
             for (int i = 0; i < N; i++)

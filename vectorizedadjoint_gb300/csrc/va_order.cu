@@ -1,8 +1,15 @@
 // Longest-first work order for the persistent sweeps.  A lane that takes a
 // long instance late holds the whole kernel open (the tail); handing out the
-// longest instances first removes most of it.  The forward sweep orders by
-// the horizon t1 - t0 (known before it runs), the backward sweep by the
-// accepted-step count the forward produced.  A counting sort over 4096
+// longest instances first removes most of it.  The backward sweep orders by
+// the accepted-step count the forward produced.  The forward sweep orders by
+// the attempt count of the handle's previous forward sweep when there is one
+// (repeated solves of a batch -- optimisation loops, sensitivity sweeps --
+// change step counts little between calls), else by the horizon t1 - t0.
+// Only the order comes from the previous sweep: every step is computed
+// again, and each instance's result does not depend on the order.  On a
+// batch with one horizon (every instance to the same T) the horizon order
+// is the index order, and lanes whose last instances run long idle the rest
+// of their warp.  A counting sort over 4096
 // buckets (descending) builds the permutation on the device, so it can sit
 // inside the captured graph.  The atomics here only decide the order; each
 // instance's result does not depend on it.
@@ -28,10 +35,14 @@ __device__ __forceinline__ int horizon_bucket(double h)
     return k < 0 ? 0 : k >= kBuckets ? kBuckets - 1 : k;
 }
 
+__device__ __forceinline__ int count_bucket(int n) { return n < kBuckets ? (n < 0 ? 0 : n) : kBuckets - 1; }
+
 __device__ __forceinline__ int key_of(const OrderArgs &a, int b)
 {
     if (a.steps)
-        return a.steps[b] < kBuckets ? (a.steps[b] < 0 ? 0 : a.steps[b]) : kBuckets - 1;
+        return count_bucket(a.steps[b]);
+    if (a.prev_work && *a.prev_valid)
+        return count_bucket(a.prev_work[b]);
     return horizon_bucket(a.t1[b] - a.t0[b]);
 }
 

@@ -10,8 +10,10 @@ namespace va {
 struct OrderArgs {
     int B;
     const int *steps;  // backward: accepted steps per instance (or null)
-    const double *t0;  // forward: horizons t1 - t0 (used when steps is null)
-    const double *t1;
+    const double *t0;  // forward: horizons t1 - t0 (used when steps is null and
+    const double *t1;  //   no previous sweep's counts are valid)
+    const int *prev_work;  // forward: attempts per instance of the previous forward sweep
+    const int *prev_valid; //   and its flag (device int, 1 once written); may be null
     int *work;         // order_work_ints() scratch ints
     int *order;        // [B] output permutation, longest first
 };
