@@ -111,9 +111,18 @@ typedef struct {
     int32_t block_size;  /* 0 = autotuned / default                               */
     int32_t blocks_per_sm; /* 0 = occupancy limit                                 */
     int32_t chunk_len;   /* records per checkpoint chunk (0 = 64)                 */
-    int32_t schedule;    /* 0: longest instances first (forward: by t1 - t0;
-                            backward: by accepted steps), 1: index order          */
-    int32_t reserved[5];
+    int32_t schedule;    /* 0: longest instances first (forward: by the previous
+                            forward's attempt counts, else by t1 - t0; backward:
+                            by accepted steps), 1: index order                    */
+    int32_t stage_records; /* mixed_dw, one-thread models, every step checkpointed:
+                            1 (default) -- each record also holds the step's RK
+                            stage values and the backward sweep reads them instead
+                            of recomputing them (records of 2 + 6N doubles instead
+                            of 2 + N); 0 -- [t, dt, y] records and stage recompute,
+                            the reference's scheme.  With ckpt_stride = -1 a pool
+                            overflow first drops the stage values, then thins the
+                            checkpoints                                           */
+    int32_t reserved[4];
 } va_options;
 
 /* Fills the reference's defaults: DOPRI5, FP64, atol=rtol=1e-6, dt0=1e-3,

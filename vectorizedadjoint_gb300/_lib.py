@@ -38,7 +38,8 @@ class VaOptions(ctypes.Structure):
                 ("max_steps", ctypes.c_int32), ("max_rejects", ctypes.c_int32),
                 ("ckpt_budget_bytes", ctypes.c_int64), ("ckpt_stride", ctypes.c_int32),
                 ("block_size", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
-                ("chunk_len", ctypes.c_int32), ("schedule", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+                ("chunk_len", ctypes.c_int32), ("schedule", ctypes.c_int32),
+                ("stage_records", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
 
 
 class VaError(RuntimeError):

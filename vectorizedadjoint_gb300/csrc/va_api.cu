@@ -46,7 +46,11 @@ struct va_handle {
     int device = 0;
     int sm_count = 0;
     const va::KernelSet *ks = nullptr;
-    int N = 0, P = 0, RS = 0;
+    int N = 0, P = 0;
+    int RS = 0; // doubles per checkpoint record at the current stride (record_layout)
+    bool stages_on = true; // opt.stage_records, cleared by the automatic checkpoint ladder
+    size_t pool_bytes = 0;
+    int64_t worst_chunks = 0;
 
     // checkpoint pool and per-instance metadata
     double *pool_rec = nullptr;
@@ -143,24 +147,56 @@ int grid_for(va_handle *h, const void *fn, int block, int instances)
     return (int)std::max(1L, std::min(g, need));
 }
 
+// Record size and chunk count of the checkpoint pool at the current stride:
+// the double-word sweeps store stage records when every step is kept and
+// [t, dt, y] records otherwise, so the same bytes hold more chunks at a
+// stride > 1.
+bool stages_now(const va_handle *h)
+{
+    return !h->bks && va::stage_records_on(h->ks, h->opt.precision, h->stride, h->stages_on);
+}
+
+void record_layout(va_handle *h)
+{
+    h->RS = h->bks ? va::record_doubles(h->N)
+                   : va::record_doubles_for(h->ks, h->opt.precision, h->stride, h->N, h->stages_on);
+    if (!h->pool_bytes)
+        return;
+    const int64_t chunk_bytes = (int64_t)h->RS * sizeof(double) * h->chunk_len;
+    int64_t nch = std::min<int64_t>(h->worst_chunks, (int64_t)h->pool_bytes / chunk_bytes);
+    nch = std::max<int64_t>(nch, 1);
+    h->n_chunks = (int)std::min<int64_t>(nch, 0x7fffffff);
+}
+
+// doubles per record of the two-level re-integration scratch (the
+// double-word kernels keep stage records there)
+int scratch_record_doubles(const va_handle *h)
+{
+    return va::record_doubles_for(h->ks, h->opt.precision, 1, h->N, true);
+}
+
 va_status ensure_buffers(va_handle *h)
 {
     if (h->pool_rec)
         return VA_OK;
     const int B = h->prob.batch;
-    const size_t rec_bytes = (size_t)h->RS * sizeof(double);
-    const size_t chunk_bytes = rec_bytes * h->chunk_len;
+    // the pool is sized for the largest record layout of the handle; the
+    // chunk links for the smallest (most chunks)
+    const int rs_small = va::record_doubles(h->N);
+    const int rs_big = h->bks ? rs_small : va::record_doubles_for(h->ks, h->opt.precision, 1, h->N, h->stages_on);
     int64_t budget = h->opt.ckpt_budget_bytes > 0 ? h->opt.ckpt_budget_bytes : kDefaultBudget;
     const int64_t per_inst_chunks = ((int64_t)h->opt.max_steps + 1 + h->chunk_len - 1) / h->chunk_len;
-    int64_t worst = per_inst_chunks * B;
-    int64_t by_budget = budget / (int64_t)chunk_bytes;
-    int64_t nch = std::min(worst, by_budget);
-    nch = std::max<int64_t>(nch, 1);
-    if (nch > 0x7fffffff)
-        nch = 0x7fffffff;
-    h->n_chunks = (int)nch;
-    VA_CUDA(h, cudaMalloc(&h->pool_rec, (size_t)nch * chunk_bytes));
-    VA_CUDA(h, cudaMalloc(&h->chunk_prev, (size_t)nch * sizeof(int)));
+    h->worst_chunks = per_inst_chunks * B;
+    const int64_t big_chunk = (int64_t)rs_big * sizeof(double) * h->chunk_len;
+    const int64_t small_chunk = (int64_t)rs_small * sizeof(double) * h->chunk_len;
+    int64_t bytes = std::min<int64_t>(budget, h->worst_chunks * big_chunk);
+    bytes = std::max<int64_t>(bytes, big_chunk);
+    h->pool_bytes = (size_t)bytes;
+    int64_t links = std::min<int64_t>(h->worst_chunks, bytes / small_chunk);
+    links = std::max<int64_t>(std::min<int64_t>(links, 0x7fffffff), 1);
+    record_layout(h);
+    VA_CUDA(h, cudaMalloc(&h->pool_rec, h->pool_bytes));
+    VA_CUDA(h, cudaMalloc(&h->chunk_prev, (size_t)links * sizeof(int)));
     VA_CUDA(h, cudaMalloc(&h->inst_T, (size_t)B * sizeof(int)));
     VA_CUDA(h, cudaMalloc(&h->inst_last, (size_t)B * sizeof(int)));
     VA_CUDA(h, cudaMalloc(&h->inst_status, (size_t)B * sizeof(int)));
@@ -222,7 +258,8 @@ va_status ensure_scratch(va_handle *h)
 {
     if (h->stride <= 1)
         return VA_OK;
-    const size_t need = (size_t)two_level_grid(h) * kTwoLevelBlock * (h->stride + 1) * h->RS;
+    const size_t need =
+        (size_t)two_level_grid(h) * kTwoLevelBlock * (h->stride + 1) * scratch_record_doubles(h);
     if (need <= h->scratch_doubles)
         return VA_OK;
     if (h->scratch)
@@ -314,6 +351,8 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
         return VA_OK;
     }
     const void *fn = h->ks->fwd[h->opt.tableau][h->opt.precision];
+    if (!stages_now(h) && h->ks->fwd2[h->opt.tableau][h->opt.precision])
+        fn = h->ks->fwd2[h->opt.tableau][h->opt.precision];
     if (h->fwd_grid <= 0)
         h->fwd_grid = grid_for(h, fn, h->fwd_block, a.B);
     if (h->order_fwd) {
@@ -372,7 +411,8 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
         return VA_OK;
     }
     if (h->stride > 1) {
-        if (h->scratch_doubles < (size_t)two_level_grid(h) * kTwoLevelBlock * (h->stride + 1) * h->RS)
+        if (h->scratch_doubles <
+            (size_t)two_level_grid(h) * kTwoLevelBlock * (h->stride + 1) * scratch_record_doubles(h))
             return fail(h, VA_BAD_ARGS, "two-level scratch not sized for the stride%s");
         a.stride = h->stride;
         a.inst_t1 = h->inst_t1;
@@ -385,6 +425,8 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
         return VA_OK;
     }
     const void *fn = h->ks->bwd[h->opt.tableau][h->opt.precision];
+    if (!stages_now(h) && h->ks->bwd1[h->opt.tableau][h->opt.precision])
+        fn = h->ks->bwd1[h->opt.tableau][h->opt.precision];
     if (h->bwd_grid <= 0)
         h->bwd_grid = grid_for(h, fn, h->bwd_block, a.B);
     VA_CUDA(h, cudaMemsetAsync(&h->ctl->adj_next, 0, sizeof(unsigned int), s));
@@ -452,6 +494,7 @@ va_status va_default_options(va_options *o)
     o->block_size = 0;
     o->blocks_per_sm = 0;
     o->chunk_len = 0;
+    o->stage_records = 1;
     return VA_OK;
 }
 
@@ -498,14 +541,15 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
         return VA_BAD_ARGS;
     va_handle *h = new va_handle();
     h->stride = o.ckpt_stride > 1 ? o.ckpt_stride : 1;
+    h->stages_on = o.stage_records != 0;
     h->prob = *prob;
     h->opt = o;
     h->ks = ks;
     h->bks = bks;
     h->N = N;
     h->P = P;
-    h->RS = va::record_doubles(N);
     h->chunk_len = o.chunk_len > 0 ? o.chunk_len : 64;
+    record_layout(h);
     if (o.block_size > 0) {
         h->fwd_block = h->bwd_block = o.block_size;
     }
@@ -559,7 +603,12 @@ va_status va_forward(va_handle *h, const double *y0, const double *params, const
         VA_CUDA(h, cudaStreamSynchronize((cudaStream_t)stream));
         if (!c.pool_fail || h->stride >= kMaxAutoStride)
             break;
-        h->stride *= 4;
+        // the ladder: drop the stage values first, then thin the checkpoints
+        if (stages_now(h))
+            h->stages_on = false;
+        else
+            h->stride *= 4;
+        record_layout(h);
         drop_graph(h);
     }
     if (st == VA_OK)

@@ -24,12 +24,18 @@ static KernelSet make_set(void (*fill_fp64)(KernelSet &))
     fill_fp64(k);
     k.fwd[0][1] = (const void *)forward_kernel<M, TabDopri5, float>;
     k.fwd[1][1] = (const void *)forward_kernel<M, TabCK54, float>;
-    k.fwd[0][2] = (const void *)forward_kernel_dw<M, TabDopri5>;
-    k.fwd[1][2] = (const void *)forward_kernel_dw<M, TabCK54>;
+    k.fwd[0][2] = (const void *)forward_kernel_dw<M, TabDopri5, true>;
+    k.fwd[1][2] = (const void *)forward_kernel_dw<M, TabCK54, true>;
+    k.fwd2[0][2] = (const void *)forward_kernel_dw<M, TabDopri5, false>;
+    k.fwd2[1][2] = (const void *)forward_kernel_dw<M, TabCK54, false>;
+    static_assert(TabDopri5::S == TabCK54::S, "one stage-record size per model");
+    k.rs_stage = stage_record_doubles(M::N, TabDopri5::S);
     k.bwd[0][1] = (const void *)backward_kernel<M, TabDopri5, float>;
     k.bwd[1][1] = (const void *)backward_kernel<M, TabCK54, float>;
-    k.bwd[0][2] = (const void *)backward_kernel_dw<M, TabDopri5>;
-    k.bwd[1][2] = (const void *)backward_kernel_dw<M, TabCK54>;
+    k.bwd[0][2] = (const void *)backward_kernel_dw<M, TabDopri5, true>;
+    k.bwd[1][2] = (const void *)backward_kernel_dw<M, TabCK54, true>;
+    k.bwd1[0][2] = (const void *)backward_kernel_dw<M, TabDopri5, false>;
+    k.bwd1[1][2] = (const void *)backward_kernel_dw<M, TabCK54, false>;
     k.bwd2[0][1] = (const void *)backward_kernel_2level<M, TabDopri5, float>;
     k.bwd2[1][1] = (const void *)backward_kernel_2level<M, TabCK54, float>;
     k.bwd2[0][2] = (const void *)backward_kernel_2level_dw<M, TabDopri5>;

@@ -18,14 +18,31 @@
 // The algorithms are those of va_kernels.cuh: odeint 1.74's controlled
 // stepper with its default error checker and step adjuster (forward), the
 // reference's back_prop_step (lib/include/backpropagation.hpp:160-229,
-// backward); only the arithmetic type differs.  Records keep the FP64
-// layout's size: [t_n (FP64), dt_n (double-word), y_n (double-words)], each
-// double-word packed into one 8-byte slot (dw_pack).
+// backward); only the arithmetic type differs.
+//
+// Stage records.  The reference's backward step recomputes the stage values
+// X_m = y_n + h sum_j a_mj K_j from y_n (compute_intermediate_states,
+// backpropagation.hpp:24-64) before its VJPs; that recompute is ~40% of a
+// backward step here.  With 288 GB of HBM at ~7 TB/s the sweeps store them
+// instead: when every step is checkpointed, the record of step n is
+//   [t_n (FP64), dt_n, y_n, X_1 .. X_{s-1} (double-words)]
+// (stage_record_doubles), each double-word packed into one 8-byte slot
+// (dw_pack).  Every attempt of step n writes its stage values into the
+// record; the accepted one is the last to write.  The backward step reads
+// X_0 = y_n .. X_{s-1} and runs only the VJPs: the adjoint differentiates
+// the stages the forward computed, bit for bit.  The two-level backward
+// (checkpoints every k-th step, records [t, dt, y]) keeps the stage values
+// of its re-integration in the same layout in its scratch, so both modes
+// give the same bits.
 #pragma once
 
 #include "va_kernels.cuh"
 
 namespace va {
+
+// doubles per stage record: t, dt, X_0 = y, X_1 .. X_{s-1}; even, so every
+// record (and every 2-state group in it) starts on a 16-byte boundary
+__host__ __device__ constexpr int stage_record_doubles(int n, int s) { return (2 + n * s + 1) & ~1; }
 
 struct DwTol {
     dword atol, rtol;
@@ -33,20 +50,29 @@ struct DwTol {
 
 __host__ __device__ __forceinline__ dword dw_nan() { return dword(f32_from_bits(0x7fc00000), 0.0f); }
 
-// (double)f by integer operations for zero and normal f: rebias the exponent
-// (127 -> 1023) and shift the 23 fraction bits to the top of the 52.  The
-// FP64 pipe's own conversion is as scarce as its arithmetic.  Subnormal,
-// infinite and NaN f take the hardware conversion.  Exact, like the cast.
+// (double)f by integer operations: rebias the exponent (127 -> 1023) and
+// shift the 23 fraction bits to the top of the 52; subnormals are normalised
+// first, infinities and NaNs keep their fraction (payload).  The FP64 pipe's
+// own conversion is as scarce as its arithmetic.  Exact, like the cast.
 __device__ __forceinline__ double f2d_int(float f)
 {
     const unsigned u = __float_as_uint(f);
     const unsigned e = (u >> 23) & 0xffu;
-    if ((u & 0x7fffffffu) == 0u)
-        return __hiloint2double((int)(u & 0x80000000u), 0);
-    if (e == 0u || e == 0xffu)
-        return (double)f;
-    const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
-    return __hiloint2double((int)hi, (int)(u << 29));
+    unsigned m = u & 0x7fffffu, ed;
+    if (e == 0xffu) {
+        ed = 0x7ffu;
+    } else if (e != 0u) {
+        ed = e + 896u;
+    } else if (m != 0u) {
+        // m 2^-149 with the leading one at bit p: shift it to bit 23
+        const unsigned sh = (unsigned)__clz((int)m) - 8u;
+        m = (m << sh) & 0x7fffffu;
+        ed = 897u - sh;
+    } else {
+        ed = 0u;
+    }
+    const unsigned hi = (u & 0x80000000u) | (ed << 20) | (m >> 3);
+    return __hiloint2double((int)hi, (int)(m << 29));
 }
 
 // hi + lo rounded to FP64, as to_d, without FP64-pipe conversions
@@ -168,15 +194,31 @@ struct EWeights {
     };
 };
 
+// N packed double-words at r (16-byte aligned when N is even)
+template <int N>
+__host__ __device__ __forceinline__ void store_dw(double *r, const dword (&X)[N])
+{
+    if constexpr (N % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < N; i += 2)
+            *reinterpret_cast<double2 *>(r + i) = make_double2(dw_pack(X[i]), dw_pack(X[i + 1]));
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            r[i] = dw_pack(X[i]);
+    }
+}
+
 // One attempted step from (y, k0 = f(y), t) with step dt: y_new, k_new =
 // f(y_new) (FSAL pairs) and the error norm
 //   max_i |dt e_i| / (atol + rtol (|y_i| + |dt| |k0_i|))
 // (odeint's default_error_checker with a_x = a_dxdt = 1), NaN if any ratio is.
+// xrec (may be null): where the stage values X_1 .. X_{s-1} go, N each.
 template <class M, class Tab>
 __host__ __device__ __forceinline__ dword attempt_dw(const dword (&y)[M::N], const dword (&k0)[M::N],
                                                      const dword (&p)[M::P], dword t, dword dt,
                                                      const DwTol &tol, dword (&ynew)[M::N],
-                                                     dword (&knew)[M::N])
+                                                     dword (&knew)[M::N], double *xrec = nullptr)
 {
     constexpr int N = M::N, NS = Tab::S;
     dword K[NS][N];
@@ -187,6 +229,8 @@ __host__ __device__ __forceinline__ dword attempt_dw(const dword (&y)[M::N], con
     for (int m = 1; m < NS; m++) {
         dword X[N];
         stage_dw<Tab, N>(m, y, K, dt, X);
+        if (xrec)
+            store_dw<N>(xrec + (m - 1) * N, X);
         M::template rhs<dword>(X, p, t + dt * dword(Tab::c(m)), K[m]);
     }
 #pragma unroll
@@ -253,18 +297,40 @@ __device__ __forceinline__ void read_record_dw(const double *r, double &t, dword
         y[i] = dw_unpack(v[2 + i]);
 }
 
+// t_n and the stage values X_0 = y_n .. X_{S-1} of a stage record
+template <int N, int S>
+__device__ __forceinline__ void read_stage_record_dw(const double *r, double &t, dword (&X)[S][N])
+{
+    constexpr int RS = stage_record_doubles(N, S);
+    double v[RS];
+#pragma unroll
+    for (int i = 0; i < RS; i += 2) {
+        double2 q = __ldcs(reinterpret_cast<const double2 *>(r + i));
+        v[i] = q.x;
+        v[i + 1] = q.y;
+    }
+    t = v[0];
+#pragma unroll
+    for (int m = 0; m < S; m++)
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            X[m][i] = dw_unpack(v[2 + m * N + i]);
+}
+
 __host__ __device__ __forceinline__ bool dw_same(dword x, dword y) { return x.hi == y.hi && x.lo == y.lo; }
 
 // ------------------------------------------------------------ forward sweep
 
 // forward_kernel with double-word state.  The end clamp and the loop test
 // stay in FP64 (less_with_sign, runge_kutta.hpp:155-163); an accepted step
-// that was clamped to the end lands on t1 itself.
-template <class M, class Tab>
+// that was clamped to the end lands on t1 itself.  STAGES: every step is
+// checkpointed as a stage record (the stride is ignored); otherwise records
+// are [t, dt, y] every stride-th step.
+template <class M, class Tab, bool STAGES>
 __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
 {
     constexpr int N = M::N, P = M::P;
-    constexpr int RS = record_doubles(N);
+    constexpr int RS = STAGES ? stage_record_doubles(N, Tab::S) : record_doubles(N);
     const int CH = a.pool.chunk_len;
     const DwTol tol{dword(a.atol), dword(a.rtol)};
 
@@ -273,6 +339,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
     dword y[N], k0[N], p[P], dt;
     int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
     bool at_top = true, to_end = false;
+    double *xrec = nullptr; // stage values of the current step (STAGES)
 
     auto fetch = [&]() -> bool {
         b = (int)atomicAdd(&a.ctl->fwd_next, 1u);
@@ -370,12 +437,15 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
                 status = ST_MAX_STEPS;
                 continue;
             }
-            if (a.stride <= 1 || count % a.stride == 0) {
+            if (STAGES || a.stride <= 1 || count % a.stride == 0) {
                 if (!reserve()) {
                     status = ST_CKPT_BUDGET;
                     continue;
                 }
-                write_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), t, dt, y);
+                double *r = record_ptr<RS>(a.pool, chunk, slot);
+                write_record_dw<N>(r, t, dt, y);
+                if (STAGES)
+                    xrec = r + 2 + N;
                 slot++;
             }
             to_end = (t + to_d_int(dt)) - t1 > kDblEps;
@@ -385,7 +455,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
             at_top = false;
         }
         dword ynew[N], knew[N];
-        const dword err = attempt_dw<M, Tab>(y, k0, p, dword(t), dt, tol, ynew, knew);
+        const dword err = attempt_dw<M, Tab>(y, k0, p, dword(t), dt, tol, ynew, knew, xrec);
         bool ok;
         if (err.hi != err.hi) {
             status = ST_NONFINITE;
@@ -427,30 +497,16 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
 
 // ----------------------------------------------------------- backward sweep
 
-// back_step in double-word: lambda_{n+1} -> lambda_n, mu += the step's
-// parameter adjoint.  Kbar_m and the lambda / mu increments are compensated
-// accumulators, finished when stage m's VJP needs Kbar_m.
+// back_step in double-word from the stage values X_0 = y_n .. X_{s-1} of
+// step n: lambda_{n+1} -> lambda_n, mu += the step's parameter adjoint.
+// Kbar_m and the lambda / mu increments are compensated accumulators,
+// finished when stage m's VJP needs Kbar_m.
 template <class M, class Tab>
-__host__ __device__ __forceinline__ void back_step_dw(const dword (&y)[M::N], dword tn, dword h,
-                                                      const dword (&p)[M::P], dword (&lam)[M::N],
-                                                      dword (&mu)[M::PG])
+__host__ __device__ __forceinline__ void back_step_dw_x(const dword (&X)[Tab::S][M::N], dword tn, dword h,
+                                                        const dword (&p)[M::P], dword (&lam)[M::N],
+                                                        dword (&mu)[M::PG])
 {
     constexpr int N = M::N, PG = M::PG, NS = Tab::S;
-    // K[NS - 1] stays unset: the stages read K_j for j < m only, and the
-    // VJPs need the stage values, not the last slope
-    dword K[NS][N];
-    dword X[NS][N];
-#pragma unroll
-    for (int i = 0; i < N; i++)
-        X[0][i] = y[i];
-    // stages from y_n (compute_intermediate_states, :24-64)
-#pragma unroll
-    for (int m = 0; m < NS; m++) {
-        if (m > 0)
-            stage_dw<Tab, N>(m, y, K, h, X[m]);
-        if (m < NS - 1)
-            M::template rhs<dword>(X[m], p, tn + h * dword(Tab::c(m)), K[m]);
-    }
     // seeds Kbar_m = (b_m h) lambda (:178-184)
     dacc Kb[NS][N];
 #pragma unroll
@@ -505,6 +561,32 @@ __host__ __device__ __forceinline__ void back_step_dw(const dword (&y)[M::N], dw
         mu[k] = dacc_get(dm[k]);
 }
 
+// back_step_dw_x after recomputing the stage values from y_n with step h
+// (compute_intermediate_states, :24-64), as the reference's backward step
+// does.
+template <class M, class Tab>
+__host__ __device__ __forceinline__ void back_step_dw(const dword (&y)[M::N], dword tn, dword h,
+                                                      const dword (&p)[M::P], dword (&lam)[M::N],
+                                                      dword (&mu)[M::PG])
+{
+    constexpr int N = M::N, NS = Tab::S;
+    // K[NS - 1] stays unset: the stages read K_j for j < m only, and the
+    // VJPs need the stage values, not the last slope
+    dword K[NS][N];
+    dword X[NS][N];
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        X[0][i] = y[i];
+#pragma unroll
+    for (int m = 0; m < NS; m++) {
+        if (m > 0)
+            stage_dw<Tab, N>(m, y, K, h, X[m]);
+        if (m < NS - 1)
+            M::template rhs<dword>(X[m], p, tn + h * dword(Tab::c(m)), K[m]);
+    }
+    back_step_dw_x<M, Tab>(X, tn, h, p, lam, mu);
+}
+
 // cost seeds lambda_T from the last record's y_T
 template <int N>
 __device__ __forceinline__ void seed_lambda_dw(const AdjParams &a, size_t o, const dword (&yT)[N], dword (&lam)[N])
@@ -556,12 +638,15 @@ __device__ __forceinline__ void write_seed_dw(const AdjParams &a, int b, int q, 
         a.status_out[b] = finite ? ST_OK : ST_NONFINITE;
 }
 
-template <class M, class Tab>
+// Backward sweep over every-step checkpoints: the stage records of
+// forward_kernel_dw<M, Tab, true> (STAGES), or [t, dt, y] records with the
+// stages recomputed from y_n as the reference does.
+template <class M, class Tab, bool STAGES>
 __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
 {
-    constexpr int N = M::N, P = M::P;
+    constexpr int N = M::N, P = M::P, NS = Tab::S;
     static_assert(M::PG == M::P, "parameter adjoint covers every parameter");
-    constexpr int RS = record_doubles(N);
+    constexpr int RS = STAGES ? stage_record_doubles(N, NS) : record_doubles(N);
     const int CH = a.pool.chunk_len;
 
     int b = -1, q = 0, j = -1, chunk = -1, slot = 0, T = 0, last = -1;
@@ -622,10 +707,16 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
         } else {
             slot--;
         }
-        dword y[N], dtr;
         double tn;
-        read_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), tn, dtr, y);
-        back_step_dw<M, Tab>(y, dword(tn), dword(t_next - tn), p, lam, mu);
+        if constexpr (STAGES) {
+            dword X[NS][N];
+            read_stage_record_dw<N, NS>(record_ptr<RS>(a.pool, chunk, slot), tn, X);
+            back_step_dw_x<M, Tab>(X, dword(tn), dword(t_next - tn), p, lam, mu);
+        } else {
+            dword y[N], dtr;
+            read_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), tn, dtr, y);
+            back_step_dw<M, Tab>(y, dword(tn), dword(t_next - tn), p, lam, mu);
+        }
         t_next = tn;
         j--;
     }
@@ -637,15 +728,17 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
 // checkpoint's exact double-words (t, dt, y), so the re-integration
 // reproduces the forward's bits and lands on the next checkpoint.  (The
 // restart evaluates k_1 = f(y) afresh; the built-in models do not read t,
-// so it equals the forward's FSAL value.)
+// so it equals the forward's FSAL value.)  The re-integration keeps stage
+// records in the thread's scratch, and the back-steps read them, as the
+// every-step sweep does.
 template <class M, class Tab>
 __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
 {
-    constexpr int N = M::N, P = M::P;
+    constexpr int N = M::N, P = M::P, NS = Tab::S;
     static_assert(M::PG == M::P, "parameter adjoint covers every parameter");
-    constexpr int RS = record_doubles(N);
+    constexpr int RS = record_doubles(N), RX = stage_record_doubles(N, NS);
     const int CH = a.pool.chunk_len, SK = a.stride;
-    double *scr = a.scratch + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * (SK + 1) * RS;
+    double *scr = a.scratch + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * (SK + 1) * RX;
     const DwTol tol{dword(a.atol), dword(a.rtol)};
 
     int b = -1, q = 0, T = 0, R = 0, k = 0, last = -1, chunk = -1, slot = 0, L = 0, done = 0, jb = 0, fails = 0;
@@ -742,7 +835,8 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
                 at_top = false;
             }
             dword ynew[N], knew[N];
-            const dword err = attempt_dw<M, Tab>(y, k0, p, dword(t), dt, tol, ynew, knew);
+            const dword err = attempt_dw<M, Tab>(y, k0, p, dword(t), dt, tol, ynew, knew,
+                                                 scr + (size_t)done * RX + 2 + N);
             if (err.hi != err.hi || fails >= a.max_fail) {
                 fail_instance(ST_RECOMPUTE_MISMATCH);
                 alive = fetch();
@@ -768,7 +862,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
             }
             at_top = true;
             done++;
-            write_record_dw<N>(scr + (size_t)done * RS, t, dt, y);
+            write_record_dw<N>(scr + (size_t)done * RX, t, dt, y);
             if (done == L) {
                 // the re-integration must land exactly on the next checkpoint
                 bool same = t == t_end;
@@ -787,11 +881,11 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
         }
         // phase 1: back_step through the segment, last step first
         {
-            dword yj[N], dtr;
+            dword X[NS][N], dtr;
             double tn, tn1;
-            read_record_dw<N>(scr + (size_t)jb * RS, tn, dtr, yj);
-            tn1 = scr[(size_t)(jb + 1) * RS];
-            back_step_dw<M, Tab>(yj, dword(tn), dword(tn1 - tn), p, lam, mu);
+            read_stage_record_dw<N, NS>(scr + (size_t)jb * RX, tn, X);
+            tn1 = scr[(size_t)(jb + 1) * RX];
+            back_step_dw_x<M, Tab>(X, dword(tn), dword(tn1 - tn), p, lam, mu);
             jb--;
             if (jb < 0) {
                 // the segment's start becomes the next segment's end

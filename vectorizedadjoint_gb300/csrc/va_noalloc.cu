@@ -101,7 +101,8 @@ extern "C" va_status va_gradient_noalloc(int32_t model, int32_t tableau, int32_t
     // chunk_prev | checkpoint chunks.  Every instance needs at least one
     // chunk; a batch whose metadata and first chunks do not fit is rejected.
     const size_t B = (size_t)batch;
-    const size_t rec_bytes = (size_t)va::record_doubles(ks->N) * sizeof(double);
+    // every step is checkpointed: the double-word sweeps use stage records
+    const size_t rec_bytes = (size_t)va::record_doubles_for(ks, precision, 1, ks->N, true) * sizeof(double);
     const size_t chunk_bytes = rec_bytes * kChunkLen;
     const size_t off_T = 256, off_last = off_T + align256(B * 4), off_st = off_last + align256(B * 4);
     const size_t off_prev = off_st + align256(B * 4);

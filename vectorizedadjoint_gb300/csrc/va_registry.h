@@ -10,9 +10,27 @@ struct KernelSet {
     int tpi;           // threads that carry one instance
     const void *fwd[2][3]; // [tableau][precision] -> __global__ void(FwdParams)
     const void *bwd[2][3]; // [tableau][precision] -> __global__ void(AdjParams)
+    const void *fwd2[2][3]; // forward writing [t, dt, y] records when fwd writes stage
+                            // records; null: fwd handles every layout
+    const void *bwd1[2][3]; // every-step backward over [t, dt, y] records when bwd reads
+                            // stage records; null: bwd
     const void *bwd2[2][3]; // two-level backward (checkpoint stride > 1); null if unsupported
     bool dw_records;        // mixed_dw records hold double-words (t stays FP64)
+    int rs_stage;           // mixed_dw: doubles per stage record (0: no stage records)
 };
+
+// whether the sweeps keep stage records: mixed_dw kernels that have them,
+// every step checkpointed, and stage storage enabled
+inline bool stage_records_on(const KernelSet *ks, int precision, int stride, bool enabled)
+{
+    return enabled && ks && ks->rs_stage > 0 && precision == 2 && stride <= 1;
+}
+
+// doubles per checkpoint record: the stage record, or [t, dt, y] padded to even
+inline int record_doubles_for(const KernelSet *ks, int precision, int stride, int n, bool enabled)
+{
+    return stage_records_on(ks, precision, stride, enabled) ? ks->rs_stage : (2 + n + 1) & ~1;
+}
 
 const KernelSet *kernels_vdp();
 const KernelSet *kernels_vdp_petsc();

@@ -30,11 +30,14 @@ class Solver:
     nout      : cost functions (seed rows) per instance
     tableau   : 'dopri5' | 'ck54'
     precision : 'fp64' | 'mixed' (FP32 stages) | 'mixed_dw' (double-word FP32-pair stages)
+    stage_records : mixed_dw, every step checkpointed: 1 stores each step's stage
+                values for the backward sweep, 0 recomputes them (va_options)
     """
 
     def __init__(self, model, n, npar, batch, nout=1, tableau="dopri5", precision="fp64",
                  atol=1e-6, rtol=1e-6, dt0=1e-3, max_steps=1000000, max_rejects=500,
-                 ckpt_budget_bytes=0, ckpt_stride=0, block_size=0, blocks_per_sm=0, chunk_len=0):
+                 ckpt_budget_bytes=0, ckpt_stride=0, block_size=0, blocks_per_sm=0, chunk_len=0,
+                 stage_records=1):
         self.L = _lib.load()
         if not torch.cuda.is_available():
             raise RuntimeError("vectorizedadjoint_gb300 needs a CUDA device (no CPU fallback)")
@@ -49,6 +52,7 @@ class Solver:
         opt.max_steps, opt.max_rejects = max_steps, max_rejects
         opt.ckpt_budget_bytes, opt.ckpt_stride = ckpt_budget_bytes, ckpt_stride
         opt.block_size, opt.blocks_per_sm, opt.chunk_len = block_size, blocks_per_sm, chunk_len
+        opt.stage_records = stage_records
         torch.cuda.init()
         self.h = ctypes.c_void_p()
         st = self.L.va_create(ctypes.byref(prob), ctypes.byref(opt), ctypes.byref(self.h))
