@@ -56,12 +56,13 @@ def flops(model, tableau, n, attempts, accepted):
 # FP32 FLOPs the double-word sweeps execute per forward attempt and per
 # backward step (FADD + FMUL + 2 FFMA, thread level), counted by ncu on the
 # one-thread-per-instance kernels at the named workload's acceptance ratio
-# (profiles/forward_kernel_dw_vdpb.md, profiles/backward_kernel_dw_vdpb.md).
+# (profiles/forward_kernel_dw_vdpb.md, profiles/backward_kernel_dw_vdpb.md,
+# profiles/dw_kernels_dho.md), stage records on.
 # Double-word arithmetic is FADD-heavy (2Sum chains), so its FLOP ceiling
 # sits near half the FFMA peak.
 DW_FP32_FLOPS = {
-    ("vdp", "dopri5"): (1709.0, 2670.5),
-    ("dho", "ck54"): (1445.8, None),
+    ("vdp", "dopri5"): (1562.9, 1644.8),
+    ("dho", "ck54"): (1357.5, 1566.8),
 }
 
 
@@ -217,8 +218,8 @@ def gemm_tflops(torch, dtype, n):
 
 # DRAM bytes per launch of the one-thread double-word kernels on the Van der
 # Pol batch (262,144 instances), one ncu capture each: the forward writes the
-# checkpoints (32 B per accepted step), the backward reads them back.
-DW_TRAFFIC = {("vdpb", "forward"): 20.04e6 + 1367.69e6, ("vdpb", "backward"): 1421.82e6 + 9.21e6}
+# stage records (112 B per accepted step), the backward reads them back.
+DW_TRAFFIC = {("vdpb", "forward"): 453.99e6 + 5110.17e6, ("vdpb", "backward"): 4894.20e6 + 11.09e6}
 
 
 def roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted):

@@ -652,6 +652,25 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
     int b = -1, q = 0, j = -1, chunk = -1, slot = 0, T = 0, last = -1;
     double t_next = 0.0;
     dword lam[N], mu[P], p[P];
+    // record j, loaded one step ahead: its loads are in flight while the
+    // previous step's VJPs run
+    double nv[RS];
+
+    auto step_back_load = [&]() {
+        if (slot == 0) {
+            chunk = a.pool.chunk_prev[chunk];
+            slot = CH - 1;
+        } else {
+            slot--;
+        }
+        const double *r = record_ptr<RS>(a.pool, chunk, slot);
+#pragma unroll
+        for (int i = 0; i < RS; i += 2) {
+            const double2 v = __ldcs(reinterpret_cast<const double2 *>(r + i));
+            nv[i] = v.x;
+            nv[i + 1] = v.y;
+        }
+    };
 
     auto start_seed = [&]() {
         chunk = last;
@@ -663,6 +682,8 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
         for (int k = 0; k < P; k++)
             mu[k] = dword(0.0f, 0.0f);
         j = T - 1;
+        if (j >= 0)
+            step_back_load();
     };
 
     auto fetch = [&]() -> bool {
@@ -701,20 +722,26 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
             }
             continue;
         }
-        if (slot == 0) {
-            chunk = a.pool.chunk_prev[chunk];
-            slot = CH - 1;
-        } else {
-            slot--;
-        }
-        double tn;
+        double cv[RS];
+#pragma unroll
+        for (int i = 0; i < RS; i++)
+            cv[i] = nv[i];
+        if (j > 0)
+            step_back_load();
+        const double tn = cv[0];
         if constexpr (STAGES) {
             dword X[NS][N];
-            read_stage_record_dw<N, NS>(record_ptr<RS>(a.pool, chunk, slot), tn, X);
+#pragma unroll
+            for (int m = 0; m < NS; m++)
+#pragma unroll
+                for (int i = 0; i < N; i++)
+                    X[m][i] = dw_unpack(cv[2 + m * N + i]);
             back_step_dw_x<M, Tab>(X, dword(tn), dword(t_next - tn), p, lam, mu);
         } else {
-            dword y[N], dtr;
-            read_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), tn, dtr, y);
+            dword y[N];
+#pragma unroll
+            for (int i = 0; i < N; i++)
+                y[i] = dw_unpack(cv[2 + i]);
             back_step_dw<M, Tab>(y, dword(tn), dword(t_next - tn), p, lam, mu);
         }
         t_next = tn;
