@@ -6,4 +6,5 @@ ABI of include/va.h).  This package is the Python host layer over that ABI:
 `driver` (Driver, runge_kutta, setCostGradients, adjointSolve, ...).
 """
 from ._lib import LIB_PATH, STATUS_NAMES, VaError, load  # noqa: F401
+from .autograd import odeint_adjoint  # noqa: F401
 from .solver import Solver  # noqa: F401
