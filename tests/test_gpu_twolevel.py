@@ -100,6 +100,22 @@ def test_stage_records_vs_recompute(cuda, name, B):
         assert (np.abs(st[k] - rc[k]) / scale).max() < 1e-8
 
 
+@pytest.mark.parametrize("stage_records", [1, 0])
+def test_glv_lane_group_modes(cuda, stage_records):
+    """GLV N=10 lane groups, mixed_dw: the double-word stage-record sweeps
+    (stage_records = 1) and the double-word-stage sweeps over FP64 records
+    (0) both stay within 1e-6 of the FP64 path on every instance."""
+    B = 256
+    ref, _ = grads("glv10", B, precision="fp64")
+    r, info = grads("glv10", B, precision="mixed_dw", stage_records=stage_records)
+    assert info["stride"] == 1
+    assert (r["status"] == 0).all()
+    g = np.concatenate([r["dy0"], r["dp"]], 1)
+    g64 = np.concatenate([ref["dy0"], ref["dp"]], 1)
+    scale = np.maximum(np.abs(g64).max(1, keepdims=True), 1e-8)
+    assert (np.abs(g - g64) / scale).max() < 1e-6
+
+
 def test_ladder_drops_stage_values_first(cuda):
     """Automatic checkpointing with a pool that holds [t, dt, y] records of
     every step but not stage records: the stride stays 1, the stage values

@@ -854,9 +854,9 @@ va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double
     if (st != VA_OK || last < 0)
         return fail(h, (va_status)st, "va_trajectory: instance has no complete record%s");
     const int CH = h->chunk_len, RS = h->RS, N = h->N;
-    // mixed_dw records of the one-thread kernels hold double-words
-    // (float pairs {hi, lo} in 8 bytes) after the FP64 time
-    const bool dw = h->ks && h->ks->dw_records && h->opt.precision == VA_PREC_MIXED_DW;
+    // mixed_dw stage records, and the one-thread kernels' [t, dt, y] records,
+    // hold double-words (float pairs {hi, lo} in 8 bytes) after the FP64 time
+    const bool dw = h->ks && h->opt.precision == VA_PREC_MIXED_DW && (h->ks->dw_records || stages_now(h));
     auto field = [dw](double v) {
         if (!dw)
             return v;

@@ -1,7 +1,10 @@
 // Generalized Lotka-Volterra kernels with a per-instance interaction matrix:
 // lane groups of N threads per instance, for the compiled sizes N = 5, 10.
-// Reduced-precision sweeps here; FP64 sweeps in va_inst_glv_fp64.cu.
+// Reduced-precision sweeps here; FP64 sweeps in va_inst_glv_fp64.cu.  The
+// mixed_dw entries are the double-word stage-record sweeps; with stage
+// records off, the double-word-stage sweeps over [t, dt, y] FP64 records.
 #include "va_group.cuh"
+#include "va_group_dw.cuh"
 #include "va_registry.h"
 
 namespace va {
@@ -19,13 +22,20 @@ static KernelSet make_glv(void (*fill_fp64)(KernelSet &))
     k.tpi = NN;
     fill_fp64(k);
     k.fwd[0][1] = (const void *)forward_group_kernel<M, TabDopri5, float>;
-    k.fwd[0][2] = (const void *)forward_group_kernel<M, TabDopri5, dword>;
     k.fwd[1][1] = (const void *)forward_group_kernel<M, TabCK54, float>;
-    k.fwd[1][2] = (const void *)forward_group_kernel<M, TabCK54, dword>;
     k.bwd[0][1] = (const void *)backward_group_kernel<M, TabDopri5, float>;
-    k.bwd[0][2] = (const void *)backward_group_kernel<M, TabDopri5, dword>;
     k.bwd[1][1] = (const void *)backward_group_kernel<M, TabCK54, float>;
-    k.bwd[1][2] = (const void *)backward_group_kernel<M, TabCK54, dword>;
+    k.fwd[0][2] = (const void *)forward_group_dw_kernel<NN, TabDopri5>;
+    k.fwd[1][2] = (const void *)forward_group_dw_kernel<NN, TabCK54>;
+    k.bwd[0][2] = (const void *)backward_group_dw_kernel<NN, TabDopri5>;
+    k.bwd[1][2] = (const void *)backward_group_dw_kernel<NN, TabCK54>;
+    k.fwd2[0][2] = (const void *)forward_group_kernel<M, TabDopri5, dword>;
+    k.fwd2[1][2] = (const void *)forward_group_kernel<M, TabCK54, dword>;
+    k.bwd1[0][2] = (const void *)backward_group_kernel<M, TabDopri5, dword>;
+    k.bwd1[1][2] = (const void *)backward_group_kernel<M, TabCK54, dword>;
+    static_assert(TabDopri5::S == TabCK54::S, "one stage-record size per model");
+    k.rs_stage = stage_record_doubles(NN, TabDopri5::S);
+    k.dw_records = false; // the [t, dt, y] records of the fallback sweeps are FP64
     return k;
 }
 

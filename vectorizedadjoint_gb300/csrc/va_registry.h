@@ -15,7 +15,8 @@ struct KernelSet {
     const void *bwd1[2][3]; // every-step backward over [t, dt, y] records when bwd reads
                             // stage records; null: bwd
     const void *bwd2[2][3]; // two-level backward (checkpoint stride > 1); null if unsupported
-    bool dw_records;        // mixed_dw records hold double-words (t stays FP64)
+    bool dw_records;        // mixed_dw [t, dt, y] records hold double-words (t stays
+                            // FP64); stage records always do
     int rs_stage;           // mixed_dw: doubles per stage record (0: no stage records)
 };
 
