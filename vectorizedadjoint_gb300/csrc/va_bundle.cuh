@@ -81,17 +81,36 @@ __device__ __forceinline__ void bundle_max(double (&v)[NB], double *red /* [NT/3
 // z_b += sum_j M_ij xs[b][j], j ascending, for the NB vectors in shared
 // memory (thread i).  Mt is the matrix read as Mt[j][i] (consecutive i are
 // consecutive addresses).  One pass over the matrix serves all NB vectors.
+// (Double-word path: the dot products run through the compensated
+// accumulator dacc, ~12 FP32 operations per term.)
 template <int NT, int NB, class S>
 __device__ __forceinline__ void bundle_matvec_acc(const double *Mt, const dword *Mtw,
                                                   const S *xs /* [NT][NB] */, S (&z)[NB])
 {
     const int i = threadIdx.x;
-#pragma unroll 4
-    for (int j = 0; j < NT; j++) {
-        const S a = load_A<S>(Mt, Mtw, (size_t)j * NT + i);
+    if constexpr (std::is_same<S, dword>::value) {
+        dacc zc[NB];
 #pragma unroll
         for (int b = 0; b < NB; b++)
-            z[b] = madd(a, xs[j * NB + b], z[b]);
+            zc[b] = dacc_of(z[b]);
+#pragma unroll 4
+        for (int j = 0; j < NT; j++) {
+            const dword a = Mtw[(size_t)j * NT + i];
+#pragma unroll
+            for (int b = 0; b < NB; b++)
+                dacc_fma(zc[b], a, xs[j * NB + b]);
+        }
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+            z[b] = dacc_get(zc[b]);
+    } else {
+#pragma unroll 4
+        for (int j = 0; j < NT; j++) {
+            const S a = load_A<S>(Mt, Mtw, (size_t)j * NT + i);
+#pragma unroll
+            for (int b = 0; b < NB; b++)
+                z[b] = madd(a, xs[j * NB + b], z[b]);
+        }
     }
 }
 
@@ -99,17 +118,10 @@ template <int NT, int NB, class S>
 __device__ __forceinline__ void bundle_matvec(const double *Mt, const dword *Mtw, const S *xs /* [NT][NB] */,
                                               S (&z)[NB])
 {
-    const int i = threadIdx.x;
 #pragma unroll
     for (int b = 0; b < NB; b++)
         z[b] = S(0);
-#pragma unroll 4
-    for (int j = 0; j < NT; j++) {
-        const S a = load_A<S>(Mt, Mtw, (size_t)j * NT + i);
-#pragma unroll
-        for (int b = 0; b < NB; b++)
-            z[b] = madd(a, xs[j * NB + b], z[b]);
-    }
+    bundle_matvec_acc<NT, NB, S>(Mt, Mtw, xs, z);
 }
 
 // ------------------------------------------------------------ forward sweep
@@ -625,13 +637,23 @@ __global__ void __launch_bounds__(NT) backward_bundle_kernel(BundleParams bp)
                 for (int b = 0; b < NB; b++)
                     vi[m][b] = vall[((size_t)m * NT + i) * NB + b];
             for (int jj = 0; jj < NT; jj++) {
-                S acc = S(0);
+                if constexpr (std::is_same<S, dword>::value) {
+                    dacc acc{0.0f, 0.0f};
 #pragma unroll
-                for (int m = NS - 1; m >= 0; m--)
+                    for (int m = NS - 1; m >= 0; m--)
 #pragma unroll
-                    for (int b = 0; b < NB; b++)
-                        acc = madd(vi[m][b], xall[((size_t)m * NT + jj) * NB + b], acc);
-                part[(size_t)jj * NT + i] += to_d(acc);
+                        for (int b = 0; b < NB; b++)
+                            dacc_fma(acc, vi[m][b], xall[((size_t)m * NT + jj) * NB + b]);
+                    part[(size_t)jj * NT + i] += to_d(dacc_get(acc));
+                } else {
+                    S acc = S(0);
+#pragma unroll
+                    for (int m = NS - 1; m >= 0; m--)
+#pragma unroll
+                        for (int b = 0; b < NB; b++)
+                            acc = madd(vi[m][b], xall[((size_t)m * NT + jj) * NB + b], acc);
+                    part[(size_t)jj * NT + i] += to_d(acc);
+                }
             }
         }
 #pragma unroll
