@@ -55,9 +55,11 @@ typedef enum {
                                params = r[n]; shared params = A[n][n]                   */
 } va_model;
 
-/* Embedded pairs (ButcherTable.hpp:259-308 for Cash-Karp; Dormand-Prince is
- * added from the published tableau). */
-typedef enum { VA_TAB_DOPRI5 = 0, VA_TAB_CK54 = 1 } va_tableau;
+/* Embedded pairs (ButcherTable.hpp:259-308 for Cash-Karp, :191-246 for
+ * Fehlberg 7(8); Dormand-Prince is added from the published tableau).
+ * Fehlberg 7(8) is compiled for the one-thread models (VdP, damped
+ * oscillator, decay); va_create rejects it for GLV. */
+typedef enum { VA_TAB_DOPRI5 = 0, VA_TAB_CK54 = 1, VA_TAB_RKF78 = 2 } va_tableau;
 
 typedef enum {
     VA_PREC_FP64 = 0, /* all arithmetic FP64: the drop-in path                          */

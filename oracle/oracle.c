@@ -13,7 +13,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-#define SMAX 8
+#define SMAX 16  /* largest stage count (Fehlberg 7(8): 13) */
 #define NMAX 256 /* largest state dimension */
 
 typedef struct {
@@ -119,6 +119,98 @@ static void tab_dopri5(tableau *T)
     T->stepper_order = 5;
 }
 
+/* Fehlberg 7(8): E. Fehlberg, "Classical fifth-, sixth-, seventh-, and
+ * eighth-order Runge-Kutta formulas with stepsize control", NASA TR R-287
+ * (1968).  Thirteen stages; the eighth-order weights propagate (odeint's
+ * runge_kutta_fehlberg78, read by the reference's ButcherTable.hpp:191-246),
+ * the error weights are b8 - b7, nonzero on k_1, k_11, k_12, k_13. */
+static void tab_rkf78(tableau *T)
+{
+    memset(T, 0, sizeof(*T));
+    T->s = 13;
+    T->fsal = 0;
+    T->a[1][0] = 2.0 / 27.0;
+    T->a[2][0] = 1.0 / 36.0;
+    T->a[2][1] = 1.0 / 12.0;
+    T->a[3][0] = 1.0 / 24.0;
+    T->a[3][2] = 1.0 / 8.0;
+    T->a[4][0] = 5.0 / 12.0;
+    T->a[4][2] = -25.0 / 16.0;
+    T->a[4][3] = 25.0 / 16.0;
+    T->a[5][0] = 1.0 / 20.0;
+    T->a[5][3] = 1.0 / 4.0;
+    T->a[5][4] = 1.0 / 5.0;
+    T->a[6][0] = -25.0 / 108.0;
+    T->a[6][3] = 125.0 / 108.0;
+    T->a[6][4] = -65.0 / 27.0;
+    T->a[6][5] = 125.0 / 54.0;
+    T->a[7][0] = 31.0 / 300.0;
+    T->a[7][4] = 61.0 / 225.0;
+    T->a[7][5] = -2.0 / 9.0;
+    T->a[7][6] = 13.0 / 900.0;
+    T->a[8][0] = 2.0;
+    T->a[8][3] = -53.0 / 6.0;
+    T->a[8][4] = 704.0 / 45.0;
+    T->a[8][5] = -107.0 / 9.0;
+    T->a[8][6] = 67.0 / 90.0;
+    T->a[8][7] = 3.0;
+    T->a[9][0] = -91.0 / 108.0;
+    T->a[9][3] = 23.0 / 108.0;
+    T->a[9][4] = -976.0 / 135.0;
+    T->a[9][5] = 311.0 / 54.0;
+    T->a[9][6] = -19.0 / 60.0;
+    T->a[9][7] = 17.0 / 6.0;
+    T->a[9][8] = -1.0 / 12.0;
+    T->a[10][0] = 2383.0 / 4100.0;
+    T->a[10][3] = -341.0 / 164.0;
+    T->a[10][4] = 4496.0 / 1025.0;
+    T->a[10][5] = -301.0 / 82.0;
+    T->a[10][6] = 2133.0 / 4100.0;
+    T->a[10][7] = 45.0 / 82.0;
+    T->a[10][8] = 45.0 / 164.0;
+    T->a[10][9] = 18.0 / 41.0;
+    T->a[11][0] = 3.0 / 205.0;
+    T->a[11][5] = -6.0 / 41.0;
+    T->a[11][6] = -3.0 / 205.0;
+    T->a[11][7] = -3.0 / 41.0;
+    T->a[11][8] = 3.0 / 41.0;
+    T->a[11][9] = 6.0 / 41.0;
+    T->a[12][0] = -1777.0 / 4100.0;
+    T->a[12][3] = -341.0 / 164.0;
+    T->a[12][4] = 4496.0 / 1025.0;
+    T->a[12][5] = -289.0 / 82.0;
+    T->a[12][6] = 2193.0 / 4100.0;
+    T->a[12][7] = 51.0 / 82.0;
+    T->a[12][8] = 33.0 / 164.0;
+    T->a[12][9] = 12.0 / 41.0;
+    T->a[12][11] = 1.0;
+    T->b[5] = 34.0 / 105.0;
+    T->b[6] = 9.0 / 35.0;
+    T->b[7] = 9.0 / 35.0;
+    T->b[8] = 9.0 / 280.0;
+    T->b[9] = 9.0 / 280.0;
+    T->b[11] = 41.0 / 840.0;
+    T->b[12] = 41.0 / 840.0;
+    T->c[1] = 2.0 / 27.0;
+    T->c[2] = 1.0 / 9.0;
+    T->c[3] = 1.0 / 6.0;
+    T->c[4] = 5.0 / 12.0;
+    T->c[5] = 1.0 / 2.0;
+    T->c[6] = 5.0 / 6.0;
+    T->c[7] = 1.0 / 6.0;
+    T->c[8] = 2.0 / 3.0;
+    T->c[9] = 1.0 / 3.0;
+    T->c[10] = 1.0;
+    T->c[12] = 1.0;
+    T->e[0] = -41.0 / 840.0;
+    T->e[10] = -41.0 / 840.0;
+    T->e[11] = 41.0 / 840.0;
+    T->e[12] = 41.0 / 840.0;
+    T->e_new = 0.0;
+    T->error_order = 7;
+    T->stepper_order = 8;
+}
+
 static int get_tableau(int id, tableau *T)
 {
     if (id == ORC_TAB_DOPRI5) {
@@ -127,6 +219,10 @@ static int get_tableau(int id, tableau *T)
     }
     if (id == ORC_TAB_CK54) {
         tab_ck54(T);
+        return 0;
+    }
+    if (id == ORC_TAB_RKF78) {
+        tab_rkf78(T);
         return 0;
     }
     return -1;
@@ -337,8 +433,11 @@ static double decrease_step(double dt, double err, int error_order, int pow_mode
 static double increase_step(double dt, double err, int stepper_order, int pow_mode)
 {
     if (err < 0.5) {
-        /* pow(5.0, -5.0): 5^-5 = 1/3125 rounded */
-        double floor_ = stepper_order == 5 ? 1.0 / 3125.0 : pow(5.0, -(double)stepper_order);
+        /* pow(5.0, -p): 5^-5 = 1/3125 and 5^-8 = 1/390625, rounded (a
+         * correctly rounded pow returns the same quotients) */
+        double floor_ = stepper_order == 5   ? 1.0 / 3125.0
+                        : stepper_order == 8 ? 1.0 / 390625.0
+                                             : pow(5.0, -(double)stepper_order);
         if (err < floor_)
             err = floor_;
         dt *= 9.0 / 10.0 * inv_root(err, stepper_order, pow_mode);

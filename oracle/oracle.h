@@ -15,7 +15,9 @@
  *   - tableaux      : Cash-Karp 5(4) as in lib/include/ButcherTable.hpp:259-308
  *                     (coefficients from Cash & Karp 1990), Dormand-Prince 5(4)
  *                     (Dormand & Prince 1980; absent from the reference's
- *                      ButcherTable, added here from the published tableau)
+ *                      ButcherTable, added here from the published tableau),
+ *                     Fehlberg 7(8) as in ButcherTable.hpp:191-246 (odeint's
+ *                     runge_kutta_fehlberg78; coefficients from Fehlberg 1968)
  *   - adjoint       : lib/include/detail/backpropagation.hpp:24-81 (stage
  *                     recompute), :160-229 (back_prop_step), :256-278
  *                     (back_prop), :280-348 (seed / write-back semantics)
@@ -51,7 +53,7 @@ enum {
     ORC_MODEL_DECAY = 4      /* y_i' = -p_i y_i (analytic test model)          */
 };
 
-enum { ORC_TAB_DOPRI5 = 0, ORC_TAB_CK54 = 1 };
+enum { ORC_TAB_DOPRI5 = 0, ORC_TAB_CK54 = 1, ORC_TAB_RKF78 = 2 };
 
 enum { ORC_COST_SUMSQ = 0, ORC_COST_SUM = 1 };
 

@@ -156,30 +156,24 @@ template <class V> array<V, 6> rk54_ck_coefficients_c()
     return {V(0), V(1) / V(5), V(3) / V(10), V(3) / V(5), V(1), V(7) / V(8)};
 }
 
-// Fehlberg 7(8) is referenced by the reference's ButcherTable but not by the
-// configurations checked here: its coefficient functions exist so the header
-// compiles, and abort if ever called.
-#define VA_SHIM_RK78(name, n)                                                                      \
-    template <class V> array<V, n> name()                                                          \
-    {                                                                                              \
-        std::fprintf(stderr, "Fehlberg 7(8) coefficients are not provided by this shim\n");       \
-        std::abort();                                                                              \
-    }
-VA_SHIM_RK78(rk78_coefficients_a1, 1)
-VA_SHIM_RK78(rk78_coefficients_a2, 2)
-VA_SHIM_RK78(rk78_coefficients_a3, 3)
-VA_SHIM_RK78(rk78_coefficients_a4, 4)
-VA_SHIM_RK78(rk78_coefficients_a5, 5)
-VA_SHIM_RK78(rk78_coefficients_a6, 6)
-VA_SHIM_RK78(rk78_coefficients_a7, 7)
-VA_SHIM_RK78(rk78_coefficients_a8, 8)
-VA_SHIM_RK78(rk78_coefficients_a9, 9)
-VA_SHIM_RK78(rk78_coefficients_a10, 10)
-VA_SHIM_RK78(rk78_coefficients_a11, 11)
-VA_SHIM_RK78(rk78_coefficients_a12, 12)
-VA_SHIM_RK78(rk78_coefficients_b, 13)
-VA_SHIM_RK78(rk78_coefficients_c, 13)
-#undef VA_SHIM_RK78
+// Fehlberg 7(8) (E. Fehlberg, NASA TR R-287, 1968): the coefficient functions
+// odeint's runge_kutta_fehlberg78 provides and the reference's ButcherTable
+// reads (ButcherTable.hpp:191-246); b propagates (eighth order), db = b - b_hat.
+template <class V> array<V, 1> rk78_coefficients_a1() { return {V(2) / V(27)}; }
+template <class V> array<V, 2> rk78_coefficients_a2() { return {V(1) / V(36), V(1) / V(12)}; }
+template <class V> array<V, 3> rk78_coefficients_a3() { return {V(1) / V(24), V(0), V(1) / V(8)}; }
+template <class V> array<V, 4> rk78_coefficients_a4() { return {V(5) / V(12), V(0), V(-25) / V(16), V(25) / V(16)}; }
+template <class V> array<V, 5> rk78_coefficients_a5() { return {V(1) / V(20), V(0), V(0), V(1) / V(4), V(1) / V(5)}; }
+template <class V> array<V, 6> rk78_coefficients_a6() { return {V(-25) / V(108), V(0), V(0), V(125) / V(108), V(-65) / V(27), V(125) / V(54)}; }
+template <class V> array<V, 7> rk78_coefficients_a7() { return {V(31) / V(300), V(0), V(0), V(0), V(61) / V(225), V(-2) / V(9), V(13) / V(900)}; }
+template <class V> array<V, 8> rk78_coefficients_a8() { return {V(2) / V(1), V(0), V(0), V(-53) / V(6), V(704) / V(45), V(-107) / V(9), V(67) / V(90), V(3) / V(1)}; }
+template <class V> array<V, 9> rk78_coefficients_a9() { return {V(-91) / V(108), V(0), V(0), V(23) / V(108), V(-976) / V(135), V(311) / V(54), V(-19) / V(60), V(17) / V(6), V(-1) / V(12)}; }
+template <class V> array<V, 10> rk78_coefficients_a10() { return {V(2383) / V(4100), V(0), V(0), V(-341) / V(164), V(4496) / V(1025), V(-301) / V(82), V(2133) / V(4100), V(45) / V(82), V(45) / V(164), V(18) / V(41)}; }
+template <class V> array<V, 11> rk78_coefficients_a11() { return {V(3) / V(205), V(0), V(0), V(0), V(0), V(-6) / V(41), V(-3) / V(205), V(-3) / V(41), V(3) / V(41), V(6) / V(41), V(0)}; }
+template <class V> array<V, 12> rk78_coefficients_a12() { return {V(-1777) / V(4100), V(0), V(0), V(-341) / V(164), V(4496) / V(1025), V(-289) / V(82), V(2193) / V(4100), V(51) / V(82), V(33) / V(164), V(12) / V(41), V(0), V(1) / V(1)}; }
+template <class V> array<V, 13> rk78_coefficients_b() { return {V(0), V(0), V(0), V(0), V(0), V(34) / V(105), V(9) / V(35), V(9) / V(35), V(9) / V(280), V(9) / V(280), V(0), V(41) / V(840), V(41) / V(840)}; }
+template <class V> array<V, 13> rk78_coefficients_c() { return {V(0), V(2) / V(27), V(1) / V(9), V(1) / V(6), V(5) / V(12), V(1) / V(2), V(5) / V(6), V(1) / V(6), V(2) / V(3), V(1) / V(3), V(1) / V(1), V(0), V(1) / V(1)}; }
+template <class V> array<V, 13> rk78_coefficients_db() { return {V(-41) / V(840), V(0), V(0), V(0), V(0), V(0), V(0), V(0), V(0), V(0), V(-41) / V(840), V(41) / V(840), V(41) / V(840)}; }
 
 // ------------------------------------------------------------------ steppers
 // Explicit embedded pairs held as dense tables; do_step evaluates every sum
@@ -266,7 +260,40 @@ template <class State> struct runge_kutta4_classic {
 };
 template <class State> struct runge_kutta_fehlberg78 {
     typedef State state_type;
+    typedef double value_type;
     typedef explicit_error_stepper_tag stepper_category;
+    static shim_tableau tableau()
+    {
+        shim_tableau t;
+        t.s = 13;
+        t.fsal = false;
+        auto a1 = rk78_coefficients_a1<double>();
+        auto a2 = rk78_coefficients_a2<double>();
+        auto a3 = rk78_coefficients_a3<double>();
+        auto a4 = rk78_coefficients_a4<double>();
+        auto a5 = rk78_coefficients_a5<double>();
+        auto a6 = rk78_coefficients_a6<double>();
+        auto a7 = rk78_coefficients_a7<double>();
+        auto a8 = rk78_coefficients_a8<double>();
+        auto a9 = rk78_coefficients_a9<double>();
+        auto a10 = rk78_coefficients_a10<double>();
+        auto a11 = rk78_coefficients_a11<double>();
+        auto a12 = rk78_coefficients_a12<double>();
+        t.a = {{},
+               {a1.begin(), a1.end()},   {a2.begin(), a2.end()},   {a3.begin(), a3.end()},
+               {a4.begin(), a4.end()},   {a5.begin(), a5.end()},   {a6.begin(), a6.end()},
+               {a7.begin(), a7.end()},   {a8.begin(), a8.end()},   {a9.begin(), a9.end()},
+               {a10.begin(), a10.end()}, {a11.begin(), a11.end()}, {a12.begin(), a12.end()}};
+        auto b = rk78_coefficients_b<double>();
+        auto db = rk78_coefficients_db<double>();
+        auto c = rk78_coefficients_c<double>();
+        t.b.assign(b.begin(), b.end());
+        t.db.assign(db.begin(), db.end());
+        t.c.assign(c.begin(), c.end());
+        t.stepper_order = 8;
+        t.error_order = 7;
+        return t;
+    }
 };
 
 // controlled_runge_kutta<ErrorStepper> with odeint's default error checker

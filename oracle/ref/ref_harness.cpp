@@ -24,6 +24,7 @@ namespace odeint = boost::numeric::odeint;
 using State = std::vector<double>;
 using Dopri5 = odeint::runge_kutta_dopri5<State>;
 using CashKarp = odeint::runge_kutta_cash_karp54<State>;
+using Fehlberg78 = odeint::runge_kutta_fehlberg78<State>;
 
 template <>
 void ButcherTable::initialize<Dopri5>(Dopri5 stepper, odeint::error_stepper_tag)
@@ -125,17 +126,18 @@ static int run(System sys, int n, int nout, int npar, double atol, double rtol, 
 }
 
 // model: 0 VdP (Lienard), 1 VdP (reference example form), 2 damped
-// oscillator, 3 GLV; tableau: 0 DOPRI5, 1 Cash-Karp.  Returns 0 on success.
+// oscillator, 3 GLV; tableau: 0 DOPRI5, 1 Cash-Karp, 2 Fehlberg 7(8) (the
+// reference's own ButcherTable branch).  Returns 0 on success.
 extern "C" int ref_solve(int model, int tableau, int n, int nout, int npar, double atol, double rtol, double dt0,
                          const double *y0, const double *p, double t0, double t1, const double *lam_in,
                          const double *mu_in, long cap, double *times, double *states, long *T, double *yT,
                          double *lam_out, double *mu_out)
 {
+#define VA_ARGS n, nout, npar, atol, rtol, dt0, y0, p, t0, t1, lam_in, mu_in, cap, times, states, T, yT, lam_out, mu_out
 #define VA_RUN(SYS)                                                                                \
-    (tableau == 0 ? run<Dopri5>(SYS(), n, nout, npar, atol, rtol, dt0, y0, p, t0, t1, lam_in, mu_in, cap, \
-                                times, states, T, yT, lam_out, mu_out)                            \
-                  : run<CashKarp>(SYS(), n, nout, npar, atol, rtol, dt0, y0, p, t0, t1, lam_in, mu_in, cap, \
-                                  times, states, T, yT, lam_out, mu_out))
+    (tableau == 0   ? run<Dopri5>(SYS(), VA_ARGS)                                                  \
+     : tableau == 1 ? run<CashKarp>(SYS(), VA_ARGS)                                                \
+                    : run<Fehlberg78>(SYS(), VA_ARGS))
     switch (model) {
     case 0:
         return VA_RUN(VanDerPol);
@@ -149,4 +151,5 @@ extern "C" int ref_solve(int model, int tableau, int n, int nout, int npar, doub
         return 2;
     }
 #undef VA_RUN
+#undef VA_ARGS
 }

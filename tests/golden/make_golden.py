@@ -26,6 +26,7 @@ REF = "/root/reference"
 from vectorizedadjoint_gb300 import workloads as W  # noqa: E402
 
 MODEL_ID = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3}
+TABLEAU_ID = {"dopri5": 0, "ck54": 1, "rkf78": 2}
 
 
 def load():
@@ -44,7 +45,7 @@ def solve(L, model, tableau, n, npar, tol, y0, p, t1, lam, mu, cap=200000):
     mo = np.zeros((nout, npar))
     ptr = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(ctypes.c_void_p)
     keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (y0, p, lam, mu)]
-    rc = L.ref_solve(MODEL_ID[model], 0 if tableau == "dopri5" else 1, n, nout, npar, ctypes.c_double(tol),
+    rc = L.ref_solve(MODEL_ID[model], TABLEAU_ID[tableau], n, nout, npar, ctypes.c_double(tol),
                      ctypes.c_double(tol), ctypes.c_double(1e-3), ptr(keep[0]), ptr(keep[1]),
                      ctypes.c_double(0.0), ctypes.c_double(t1), ptr(keep[2]), ptr(keep[3]), ctypes.c_long(cap),
                      times.ctypes.data_as(ctypes.c_void_p), states.ctypes.data_as(ctypes.c_void_p),
@@ -57,10 +58,16 @@ def solve(L, model, tableau, n, npar, tol, y0, p, t1, lam, mu, cap=200000):
 def main():
     L = load()
     cases = []
-    # benchmark configurations: cost seeds from y(T) (sum of squares) or ones (sum)
-    for name, count in [("vdp1", 1), ("dho", 4), ("vdpb", 4), ("glv10", 3)]:
+    # benchmark configurations: cost seeds from y(T) (sum of squares) or ones
+    # (sum); then the same draws with the Fehlberg 7(8) pair (the reference's
+    # ButcherTable branch for runge_kutta_fehlberg78)
+    for name, count, tableau in [("vdp1", 1, None), ("dho", 4, None), ("vdpb", 4, None), ("glv10", 3, None),
+                                 ("vdpb", 2, "rkf78"), ("dho", 2, "rkf78"), ("glv10", 1, "rkf78")]:
         w = W.make(name, batch=count)
         c = w["cfg"]
+        if tableau:
+            c["tableau"] = tableau
+            name = f"{name}_{tableau}"
         for b in range(count):
             y0, p, t1 = w["y0"][b], w["params"][b], float(w["t1"][b])
             mu = np.zeros((1, c["npar"]))

@@ -153,13 +153,13 @@ int grid_for(va_handle *h, const void *fn, int block, int instances)
 // stride > 1.
 bool stages_now(const va_handle *h)
 {
-    return !h->bks && va::stage_records_on(h->ks, h->opt.precision, h->stride, h->stages_on);
+    return !h->bks && va::stage_records_on(h->ks, h->opt.tableau, h->opt.precision, h->stride, h->stages_on);
 }
 
 void record_layout(va_handle *h)
 {
     h->RS = h->bks ? va::record_doubles(h->N)
-                   : va::record_doubles_for(h->ks, h->opt.precision, h->stride, h->N, h->stages_on);
+                   : va::record_doubles_for(h->ks, h->opt.tableau, h->opt.precision, h->stride, h->N, h->stages_on);
     if (!h->pool_bytes)
         return;
     const int64_t chunk_bytes = (int64_t)h->RS * sizeof(double) * h->chunk_len;
@@ -172,7 +172,7 @@ void record_layout(va_handle *h)
 // double-word kernels keep stage records there)
 int scratch_record_doubles(const va_handle *h)
 {
-    return va::record_doubles_for(h->ks, h->opt.precision, 1, h->N, true);
+    return va::record_doubles_for(h->ks, h->opt.tableau, h->opt.precision, 1, h->N, true);
 }
 
 va_status ensure_buffers(va_handle *h)
@@ -183,7 +183,7 @@ va_status ensure_buffers(va_handle *h)
     // the pool is sized for the largest record layout of the handle; the
     // chunk links for the smallest (most chunks)
     const int rs_small = va::record_doubles(h->N);
-    const int rs_big = h->bks ? rs_small : va::record_doubles_for(h->ks, h->opt.precision, 1, h->N, h->stages_on);
+    const int rs_big = h->bks ? rs_small : va::record_doubles_for(h->ks, h->opt.tableau, h->opt.precision, 1, h->N, h->stages_on);
     int64_t budget = h->opt.ckpt_budget_bytes > 0 ? h->opt.ckpt_budget_bytes : kDefaultBudget;
     const int64_t per_inst_chunks = ((int64_t)h->opt.max_steps + 1 + h->chunk_len - 1) / h->chunk_len;
     h->worst_chunks = per_inst_chunks * B;
@@ -510,7 +510,7 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
         va_default_options(&o);
     if (prob->batch < 1 || prob->nout < 1 || prob->n < 1)
         return VA_BAD_ARGS;
-    if (o.tableau != VA_TAB_DOPRI5 && o.tableau != VA_TAB_CK54)
+    if (o.tableau < 0 || o.tableau >= va::kTableaux)
         return VA_BAD_ARGS;
     if (o.precision != VA_PREC_FP64 && o.precision != VA_PREC_MIXED && o.precision != VA_PREC_MIXED_DW)
         return VA_BAD_ARGS;
@@ -523,12 +523,13 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
     int N = 0, P = 0;
     if (prob->model == VA_MODEL_GLV_SHARED) {
         bks = va::kernels_glv_shared(prob->n);
-        if (!bks || prob->nout != 1)
+        // a (tableau, precision) pair without compiled kernels is rejected
+        if (!bks || prob->nout != 1 || !bks->fwd[o.tableau][o.precision])
             return VA_BAD_ARGS;
         N = P = prob->n;
     } else {
         ks = kernel_set(*prob);
-        if (!ks)
+        if (!ks || !ks->fwd[o.tableau][o.precision])
             return VA_BAD_ARGS;
         N = ks->N > 0 ? ks->N : prob->n;
         P = ks->P > 0 ? ks->P : prob->npar;

@@ -11,9 +11,11 @@ namespace va {
 
 void fill_fp64_glv5(KernelSet &k);
 void fill_fp64_glv10(KernelSet &k);
+void fill_rkf78_glv5(KernelSet &k);
+void fill_rkf78_glv10(KernelSet &k);
 
 template <int NN>
-static KernelSet make_glv(void (*fill_fp64)(KernelSet &))
+static KernelSet make_glv(void (*fill_fp64)(KernelSet &), void (*fill_rkf78)(KernelSet &))
 {
     using M = ModelGLVLane<NN>;
     KernelSet k{};
@@ -33,16 +35,17 @@ static KernelSet make_glv(void (*fill_fp64)(KernelSet &))
     k.fwd2[1][2] = (const void *)forward_group_kernel<M, TabCK54, dword>;
     k.bwd1[0][2] = (const void *)backward_group_kernel<M, TabDopri5, dword>;
     k.bwd1[1][2] = (const void *)backward_group_kernel<M, TabCK54, dword>;
-    static_assert(TabDopri5::S == TabCK54::S, "one stage-record size per model");
-    k.rs_stage = stage_record_doubles(NN, TabDopri5::S);
+    k.rs_stage[0] = stage_record_doubles(NN, TabDopri5::S);
+    k.rs_stage[1] = stage_record_doubles(NN, TabCK54::S);
     k.dw_records = false; // the [t, dt, y] records of the fallback sweeps are FP64
+    fill_rkf78(k);
     return k;
 }
 
 const KernelSet *kernels_glv(int n)
 {
-    static const KernelSet k5 = make_glv<5>(fill_fp64_glv5);
-    static const KernelSet k10 = make_glv<10>(fill_fp64_glv10);
+    static const KernelSet k5 = make_glv<5>(fill_fp64_glv5, fill_rkf78_glv5);
+    static const KernelSet k10 = make_glv<10>(fill_fp64_glv10, fill_rkf78_glv10);
     switch (n) {
     case 5:
         return &k5;

@@ -15,7 +15,7 @@ void fill_fp64_dho(KernelSet &k);
 void fill_fp64_decay(KernelSet &k);
 
 template <class M>
-static KernelSet make_set(void (*fill_fp64)(KernelSet &))
+static KernelSet make_set(void (*fill_fp64)(KernelSet &), void (*fill_rkf78)(KernelSet &))
 {
     KernelSet k{};
     k.N = M::N;
@@ -28,8 +28,8 @@ static KernelSet make_set(void (*fill_fp64)(KernelSet &))
     k.fwd[1][2] = (const void *)forward_kernel_dw<M, TabCK54, true>;
     k.fwd2[0][2] = (const void *)forward_kernel_dw<M, TabDopri5, false>;
     k.fwd2[1][2] = (const void *)forward_kernel_dw<M, TabCK54, false>;
-    static_assert(TabDopri5::S == TabCK54::S, "one stage-record size per model");
-    k.rs_stage = stage_record_doubles(M::N, TabDopri5::S);
+    k.rs_stage[0] = stage_record_doubles(M::N, TabDopri5::S);
+    k.rs_stage[1] = stage_record_doubles(M::N, TabCK54::S);
     k.bwd[0][1] = (const void *)backward_kernel<M, TabDopri5, float>;
     k.bwd[1][1] = (const void *)backward_kernel<M, TabCK54, float>;
     k.bwd[0][2] = (const void *)backward_kernel_dw<M, TabDopri5, true>;
@@ -41,27 +41,28 @@ static KernelSet make_set(void (*fill_fp64)(KernelSet &))
     k.bwd2[0][2] = (const void *)backward_kernel_2level_dw<M, TabDopri5>;
     k.bwd2[1][2] = (const void *)backward_kernel_2level_dw<M, TabCK54>;
     k.dw_records = true;
+    fill_rkf78(k);
     return k;
 }
 
 const KernelSet *kernels_vdp()
 {
-    static const KernelSet k = make_set<ModelVdP>(fill_fp64_vdp);
+    static const KernelSet k = make_set<ModelVdP>(fill_fp64_vdp, fill_rkf78_vdp);
     return &k;
 }
 const KernelSet *kernels_vdp_petsc()
 {
-    static const KernelSet k = make_set<ModelVdPPetsc>(fill_fp64_vdp_petsc);
+    static const KernelSet k = make_set<ModelVdPPetsc>(fill_fp64_vdp_petsc, fill_rkf78_vdp_petsc);
     return &k;
 }
 const KernelSet *kernels_dho()
 {
-    static const KernelSet k = make_set<ModelDHO>(fill_fp64_dho);
+    static const KernelSet k = make_set<ModelDHO>(fill_fp64_dho, fill_rkf78_dho);
     return &k;
 }
 const KernelSet *kernels_decay()
 {
-    static const KernelSet k = make_set<ModelDecay>(fill_fp64_decay);
+    static const KernelSet k = make_set<ModelDecay>(fill_fp64_decay, fill_rkf78_decay);
     return &k;
 }
 

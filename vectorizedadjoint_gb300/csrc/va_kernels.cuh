@@ -236,10 +236,9 @@ template <class Tab, class S = double>
 __host__ __device__ __forceinline__ double increase_step(double dt, double err)
 {
     if (err < 0.5) {
-        // 5^-5 = 1/3125, the rounding of pow(5.0, -5.0)
-        constexpr double floor_err = 1.0 / 3125.0;
-        static_assert(Tab::STEPPER_ORDER == 5, "floor constant assumes a fifth-order stepper");
-        err = fmax(floor_err, err);
+        // 5^-p as the correctly rounded quotient (1/3125, 1/390625), what
+        // pow(5.0, -p) returns
+        err = fmax(Tab::ERR_FLOOR, err);
         dt *= 9.0 / 10.0 * inv_root<Tab::STEPPER_ORDER, RootSteps<S>::value>(err);
     }
     return dt;

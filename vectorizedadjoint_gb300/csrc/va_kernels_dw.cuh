@@ -118,9 +118,8 @@ __host__ __device__ __forceinline__ dword decrease_dw(dword dt, dword err)
 template <class Tab>
 __host__ __device__ __forceinline__ dword increase_dw(dword dt, dword err)
 {
-    static_assert(Tab::STEPPER_ORDER == 5, "floor constant assumes a fifth-order stepper");
     if (dw_less(err, dword(0.5))) {
-        const dword fl = dword(1.0 / 3125.0);
+        const dword fl = dword(Tab::ERR_FLOOR);
         const dword e = dw_greater(fl, err) ? fl : err;
         return dt * (dword(9.0 / 10.0) * inv_root_dw<Tab::STEPPER_ORDER>(e));
     }

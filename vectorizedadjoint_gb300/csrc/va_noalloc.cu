@@ -85,9 +85,11 @@ extern "C" va_status va_gradient_noalloc(int32_t model, int32_t tableau, int32_t
     default:
         return VA_BAD_ARGS;
     }
-    if (tableau != VA_TAB_DOPRI5 && tableau != VA_TAB_CK54)
+    if (tableau < 0 || tableau >= va::kTableaux)
         return VA_BAD_ARGS;
     if (precision != VA_PREC_FP64 && precision != VA_PREC_MIXED && precision != VA_PREC_MIXED_DW)
+        return VA_BAD_ARGS;
+    if (!ks->fwd[tableau][precision])
         return VA_BAD_ARGS;
     if (cost != VA_COST_SUMSQ && cost != VA_COST_SUM)
         return VA_BAD_ARGS;
@@ -102,7 +104,7 @@ extern "C" va_status va_gradient_noalloc(int32_t model, int32_t tableau, int32_t
     // chunk; a batch whose metadata and first chunks do not fit is rejected.
     const size_t B = (size_t)batch;
     // every step is checkpointed: the double-word sweeps use stage records
-    const size_t rec_bytes = (size_t)va::record_doubles_for(ks, precision, 1, ks->N, true) * sizeof(double);
+    const size_t rec_bytes = (size_t)va::record_doubles_for(ks, tableau, precision, 1, ks->N, true) * sizeof(double);
     const size_t chunk_bytes = rec_bytes * kChunkLen;
     const size_t off_T = 256, off_last = off_T + align256(B * 4), off_st = off_last + align256(B * 4);
     const size_t off_prev = off_st + align256(B * 4);

@@ -1,36 +1,40 @@
 // Table of compiled sweep kernels per built-in model: one entry per
 // (tableau, precision).  Each model's kernels live in their own translation
-// unit so the library builds in parallel.
+// units so the library builds in parallel.  A null entry is a combination
+// that is not compiled (va_create rejects it).
 #pragma once
 
 namespace va {
 
+// tableaux: 0 Dormand-Prince 5(4), 1 Cash-Karp 5(4), 2 Fehlberg 7(8)
+constexpr int kTableaux = 3;
+
 struct KernelSet {
     int N, P;          // state and parameter counts (0 = runtime n)
     int tpi;           // threads that carry one instance
-    const void *fwd[2][3]; // [tableau][precision] -> __global__ void(FwdParams)
-    const void *bwd[2][3]; // [tableau][precision] -> __global__ void(AdjParams)
-    const void *fwd2[2][3]; // forward writing [t, dt, y] records when fwd writes stage
-                            // records; null: fwd handles every layout
-    const void *bwd1[2][3]; // every-step backward over [t, dt, y] records when bwd reads
-                            // stage records; null: bwd
-    const void *bwd2[2][3]; // two-level backward (checkpoint stride > 1); null if unsupported
-    bool dw_records;        // mixed_dw [t, dt, y] records hold double-words (t stays
-                            // FP64); stage records always do
-    int rs_stage;           // mixed_dw: doubles per stage record (0: no stage records)
+    const void *fwd[kTableaux][3]; // [tableau][precision] -> __global__ void(FwdParams)
+    const void *bwd[kTableaux][3]; // [tableau][precision] -> __global__ void(AdjParams)
+    const void *fwd2[kTableaux][3]; // forward writing [t, dt, y] records when fwd writes stage
+                                    // records; null: fwd handles every layout
+    const void *bwd1[kTableaux][3]; // every-step backward over [t, dt, y] records when bwd reads
+                                    // stage records; null: bwd
+    const void *bwd2[kTableaux][3]; // two-level backward (checkpoint stride > 1); null if unsupported
+    bool dw_records;                // mixed_dw [t, dt, y] records hold double-words (t stays
+                                    // FP64); stage records always do
+    int rs_stage[kTableaux];        // mixed_dw: doubles per stage record (0: no stage records)
 };
 
 // whether the sweeps keep stage records: mixed_dw kernels that have them,
 // every step checkpointed, and stage storage enabled
-inline bool stage_records_on(const KernelSet *ks, int precision, int stride, bool enabled)
+inline bool stage_records_on(const KernelSet *ks, int tableau, int precision, int stride, bool enabled)
 {
-    return enabled && ks && ks->rs_stage > 0 && precision == 2 && stride <= 1;
+    return enabled && ks && ks->rs_stage[tableau] > 0 && precision == 2 && stride <= 1;
 }
 
 // doubles per checkpoint record: the stage record, or [t, dt, y] padded to even
-inline int record_doubles_for(const KernelSet *ks, int precision, int stride, int n, bool enabled)
+inline int record_doubles_for(const KernelSet *ks, int tableau, int precision, int stride, int n, bool enabled)
 {
-    return stage_records_on(ks, precision, stride, enabled) ? ks->rs_stage : (2 + n + 1) & ~1;
+    return stage_records_on(ks, tableau, precision, stride, enabled) ? ks->rs_stage[tableau] : (2 + n + 1) & ~1;
 }
 
 const KernelSet *kernels_vdp();
@@ -39,12 +43,18 @@ const KernelSet *kernels_dho();
 const KernelSet *kernels_decay();
 const KernelSet *kernels_glv(int n); // nullptr when n has no compiled kernels
 
+// Fehlberg 7(8) entries of the one-thread models (their own translation units)
+void fill_rkf78_vdp(KernelSet &k);
+void fill_rkf78_vdp_petsc(KernelSet &k);
+void fill_rkf78_dho(KernelSet &k);
+void fill_rkf78_decay(KernelSet &k);
+
 // Shared-matrix GLV: bundles of kBundleNB instances per CTA of N threads.
 constexpr int kBundleNB = 4;
 struct BundleKernelSet {
     int N, nb;
-    const void *fwd[2][3]; // __global__ void(BundleParams), blockDim = N
-    const void *bwd[2][3];
+    const void *fwd[kTableaux][3]; // __global__ void(BundleParams), blockDim = N
+    const void *bwd[kTableaux][3];
     size_t smem_fwd[3], smem_bwd[3]; // dynamic shared memory per precision
     const void *prepare;   // prepare_A_kernel: A -> A^T and double-word copies
     const void *reduce;    // reduce_dA_kernel: CTA partials -> dA

@@ -1,8 +1,9 @@
 // Butcher tableaux of the embedded explicit Runge-Kutta pairs, as
 // compile-time constants that fold into the unrolled stage loops.
 //
-// Cash-Karp 5(4) (Cash & Karp 1990) is the pair the reference reads from
-// odeint in lib/include/ButcherTable.hpp:259-308.  Dormand-Prince 5(4)
+// Cash-Karp 5(4) (Cash & Karp 1990) and Fehlberg 7(8) (Fehlberg 1968) are
+// pairs the reference reads from odeint in lib/include/ButcherTable.hpp
+// (:259-308, :191-246).  Dormand-Prince 5(4)
 // (Dormand & Prince 1980) is not in the reference's ButcherTable
 // (ButcherTable.hpp:365-368 rejects it); it is added here from the published
 // tableau.  Each coefficient is the IEEE quotient of its two integers, and
@@ -17,6 +18,7 @@ struct TabDopri5 {
     static constexpr bool FSAL = true;    // f(y_{n+1}) is the next k_1
     static constexpr int ERROR_ORDER = 4; // odeint error_order_value
     static constexpr int STEPPER_ORDER = 5;
+    static constexpr double ERR_FLOOR = 1.0 / 3125.0; // 5^-STEPPER_ORDER (increase_step)
     __host__ __device__ static constexpr double a(int i, int j)
     {
         return i == 1 ? (j == 0 ? 1.0 / 5.0 : 0.0)
@@ -55,6 +57,7 @@ struct TabCK54 {
     static constexpr bool FSAL = false;
     static constexpr int ERROR_ORDER = 4;
     static constexpr int STEPPER_ORDER = 5;
+    static constexpr double ERR_FLOOR = 1.0 / 3125.0;
     __host__ __device__ static constexpr double a(int i, int j)
     {
         return i == 1 ? (j == 0 ? 1.0 / 5.0 : 0.0)
@@ -83,6 +86,49 @@ struct TabCK54 {
              : j == 3 ? 125.0 / 594.0 - 13525.0 / 55296.0
              : j == 4 ? -277.0 / 14336.0
              : j == 5 ? 512.0 / 1771.0 - 1.0 / 4.0 : 0.0;
+    }
+    static constexpr double E_NEW = 0.0;
+};
+
+// Fehlberg 7(8): E. Fehlberg, "Classical fifth-, sixth-, seventh-, and
+// eighth-order Runge-Kutta formulas with stepsize control", NASA TR R-287
+// (1968) -- odeint's runge_kutta_fehlberg78, which the reference's
+// ButcherTable reads (lib/include/ButcherTable.hpp:191-246).  13 stages, not
+// FSAL; the eighth-order weights propagate and the error estimate is
+// (b8 - b7) . k, nonzero on k_1, k_11, k_12, k_13.
+struct TabRKF78 {
+    static constexpr int S = 13;
+    static constexpr bool FSAL = false;
+    static constexpr int ERROR_ORDER = 7;
+    static constexpr int STEPPER_ORDER = 8;
+    static constexpr double ERR_FLOOR = 1.0 / 390625.0; // 5^-8
+    __host__ __device__ static constexpr double a(int i, int j)
+    {
+        return i == 1 ? (j == 0 ? 2.0 / 27.0 : 0.0)
+             : i == 2 ? (j == 0 ? 1.0 / 36.0 : j == 1 ? 1.0 / 12.0 : 0.0)
+             : i == 3 ? (j == 0 ? 1.0 / 24.0 : j == 2 ? 1.0 / 8.0 : 0.0)
+             : i == 4 ? (j == 0 ? 5.0 / 12.0 : j == 2 ? -25.0 / 16.0 : j == 3 ? 25.0 / 16.0 : 0.0)
+             : i == 5 ? (j == 0 ? 1.0 / 20.0 : j == 3 ? 1.0 / 4.0 : j == 4 ? 1.0 / 5.0 : 0.0)
+             : i == 6 ? (j == 0 ? -25.0 / 108.0 : j == 3 ? 125.0 / 108.0 : j == 4 ? -65.0 / 27.0 : j == 5 ? 125.0 / 54.0 : 0.0)
+             : i == 7 ? (j == 0 ? 31.0 / 300.0 : j == 4 ? 61.0 / 225.0 : j == 5 ? -2.0 / 9.0 : j == 6 ? 13.0 / 900.0 : 0.0)
+             : i == 8 ? (j == 0 ? 2.0 : j == 3 ? -53.0 / 6.0 : j == 4 ? 704.0 / 45.0 : j == 5 ? -107.0 / 9.0 : j == 6 ? 67.0 / 90.0 : j == 7 ? 3.0 : 0.0)
+             : i == 9 ? (j == 0 ? -91.0 / 108.0 : j == 3 ? 23.0 / 108.0 : j == 4 ? -976.0 / 135.0 : j == 5 ? 311.0 / 54.0 : j == 6 ? -19.0 / 60.0 : j == 7 ? 17.0 / 6.0 : j == 8 ? -1.0 / 12.0 : 0.0)
+             : i == 10 ? (j == 0 ? 2383.0 / 4100.0 : j == 3 ? -341.0 / 164.0 : j == 4 ? 4496.0 / 1025.0 : j == 5 ? -301.0 / 82.0 : j == 6 ? 2133.0 / 4100.0 : j == 7 ? 45.0 / 82.0 : j == 8 ? 45.0 / 164.0 : j == 9 ? 18.0 / 41.0 : 0.0)
+             : i == 11 ? (j == 0 ? 3.0 / 205.0 : j == 5 ? -6.0 / 41.0 : j == 6 ? -3.0 / 205.0 : j == 7 ? -3.0 / 41.0 : j == 8 ? 3.0 / 41.0 : j == 9 ? 6.0 / 41.0 : 0.0)
+             : i == 12 ? (j == 0 ? -1777.0 / 4100.0 : j == 3 ? -341.0 / 164.0 : j == 4 ? 4496.0 / 1025.0 : j == 5 ? -289.0 / 82.0 : j == 6 ? 2193.0 / 4100.0 : j == 7 ? 51.0 / 82.0 : j == 8 ? 33.0 / 164.0 : j == 9 ? 12.0 / 41.0 : j == 11 ? 1.0 : 0.0)
+             : 0.0;
+    }
+    __host__ __device__ static constexpr double b(int j)
+    {
+        return j == 5 ? 34.0 / 105.0 : j == 6 ? 9.0 / 35.0 : j == 7 ? 9.0 / 35.0 : j == 8 ? 9.0 / 280.0 : j == 9 ? 9.0 / 280.0 : j == 11 ? 41.0 / 840.0 : j == 12 ? 41.0 / 840.0 : 0.0;
+    }
+    __host__ __device__ static constexpr double c(int j)
+    {
+        return j == 1 ? 2.0 / 27.0 : j == 2 ? 1.0 / 9.0 : j == 3 ? 1.0 / 6.0 : j == 4 ? 5.0 / 12.0 : j == 5 ? 1.0 / 2.0 : j == 6 ? 5.0 / 6.0 : j == 7 ? 1.0 / 6.0 : j == 8 ? 2.0 / 3.0 : j == 9 ? 1.0 / 3.0 : j == 10 ? 1.0 : j == 12 ? 1.0 : 0.0;
+    }
+    __host__ __device__ static constexpr double e(int j)
+    {
+        return j == 0 ? -41.0 / 840.0 : j == 10 ? -41.0 / 840.0 : j == 11 ? 41.0 / 840.0 : j == 12 ? 41.0 / 840.0 : 0.0;
     }
     static constexpr double E_NEW = 0.0;
 };
