@@ -26,6 +26,7 @@ typedef struct {
     double e_new;          /* error weight on f(y_{n+1}) (FSAL stage)        */
     int error_order;       /* odeint error_order_value                        */
     int stepper_order;     /* odeint stepper_order_value                      */
+    int fixed;             /* no error estimate: fixed-step loop              */
 } tableau;
 
 /* Cash-Karp 5(4): Cash & Karp (1990), the coefficients the reference reads
@@ -211,6 +212,36 @@ static void tab_rkf78(tableau *T)
     T->stepper_order = 8;
 }
 
+/* Fixed-step steppers the reference's ButcherTable accepts
+ * (ButcherTable.hpp:39-125): odeint's runge_kutta4 (classic fourth-order
+ * tableau) and euler. */
+static void tab_rk4(tableau *T)
+{
+    memset(T, 0, sizeof(*T));
+    T->s = 4;
+    T->a[1][0] = 1.0 / 2.0;
+    T->a[2][1] = 1.0 / 2.0;
+    T->a[3][2] = 1.0;
+    T->b[0] = 1.0 / 6.0;
+    T->b[1] = 1.0 / 3.0;
+    T->b[2] = 1.0 / 3.0;
+    T->b[3] = 1.0 / 6.0;
+    T->c[1] = 1.0 / 2.0;
+    T->c[2] = 1.0 / 2.0;
+    T->c[3] = 1.0;
+    T->stepper_order = 4;
+    T->fixed = 1;
+}
+
+static void tab_euler(tableau *T)
+{
+    memset(T, 0, sizeof(*T));
+    T->s = 1;
+    T->b[0] = 1.0;
+    T->stepper_order = 1;
+    T->fixed = 1;
+}
+
 static int get_tableau(int id, tableau *T)
 {
     if (id == ORC_TAB_DOPRI5) {
@@ -223,6 +254,14 @@ static int get_tableau(int id, tableau *T)
     }
     if (id == ORC_TAB_RKF78) {
         tab_rkf78(T);
+        return 0;
+    }
+    if (id == ORC_TAB_RK4) {
+        tab_rk4(T);
+        return 0;
+    }
+    if (id == ORC_TAB_EULER) {
+        tab_euler(T);
         return 0;
     }
     return -1;
@@ -461,6 +500,42 @@ int orc_forward(const orc_problem *pb, const double *y0, const double *p, double
     int status = ORC_OK;
     int first_call = 1;
     int max_fail = pb->max_fail > 0 ? pb->max_fail : 500;
+
+    if (T.fixed) {
+        /* runge_kutta for non-controlled steppers (detail/runge_kutta.hpp:
+         * 37-72): t_n = t0 + n dt while (t_n + dt) - t1 <= eps (odeint's
+         * less_eq_with_sign for dt > 0), every step recorded; do_step is the
+         * tableau's stages and y + sum_j (b_j dt) k_j. */
+        while ((t + dt) - t1 <= DBL_EPSILON) {
+            if (count >= cap || count >= pb->max_steps) {
+                status = ORC_MAX_STEPS;
+                break;
+            }
+            times[count] = t;
+            memcpy(states + (size_t)count * n, y, sizeof(double) * n);
+            if (dt_trial)
+                dt_trial[count] = dt;
+            orc_rhs(pb, y, p, t, K[0]);
+            rk_error_step(pb, &T, y, t, dt, p, K, out, dxdt_new, xerr, xtmp);
+            memcpy(y, out, sizeof(double) * n);
+            count++;
+            t = t0 + (double)count * dt;
+        }
+        if (status == ORC_OK) {
+            times[count] = t;
+            memcpy(states + (size_t)count * n, y, sizeof(double) * n);
+            for (int i = 0; i < n; i++)
+                if (!isfinite(y[i]))
+                    status = ORC_NONFINITE;
+        }
+        if (yT)
+            memcpy(yT, y, sizeof(double) * n);
+        if (n_acc)
+            *n_acc = count;
+        if (n_rej)
+            *n_rej = 0;
+        return status;
+    }
 
     while (less_with_sign(t, t1)) {
         if (count >= cap) {

@@ -17,7 +17,9 @@
  *                     (Dormand & Prince 1980; absent from the reference's
  *                      ButcherTable, added here from the published tableau),
  *                     Fehlberg 7(8) as in ButcherTable.hpp:191-246 (odeint's
- *                     runge_kutta_fehlberg78; coefficients from Fehlberg 1968)
+ *                     runge_kutta_fehlberg78; coefficients from Fehlberg 1968);
+ *                     fixed-step runge_kutta4 and euler (ButcherTable.hpp:39-125)
+ *                     with the fixed-step loop of detail/runge_kutta.hpp:37-72
  *   - adjoint       : lib/include/detail/backpropagation.hpp:24-81 (stage
  *                     recompute), :160-229 (back_prop_step), :256-278
  *                     (back_prop), :280-348 (seed / write-back semantics)
@@ -53,7 +55,7 @@ enum {
     ORC_MODEL_DECAY = 4      /* y_i' = -p_i y_i (analytic test model)          */
 };
 
-enum { ORC_TAB_DOPRI5 = 0, ORC_TAB_CK54 = 1, ORC_TAB_RKF78 = 2 };
+enum { ORC_TAB_DOPRI5 = 0, ORC_TAB_CK54 = 1, ORC_TAB_RKF78 = 2, ORC_TAB_RK4 = 3, ORC_TAB_EULER = 4 };
 
 enum { ORC_COST_SUMSQ = 0, ORC_COST_SUM = 1 };
 

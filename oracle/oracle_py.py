@@ -17,7 +17,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _SO = os.path.join(_HERE, "_build", "liboracle.so")
 
 MODEL = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3, "decay": 4}
-TABLEAU = {"dopri5": 0, "ck54": 1, "rkf78": 2}
+TABLEAU = {"dopri5": 0, "ck54": 1, "rkf78": 2, "rk4": 3, "euler": 4}
 COST = {"sumsq": 0, "sum": 1}
 STATUS = {0: "OK", 1: "MAX_REJECTS", 2: "MAX_STEPS", 3: "NONFINITE", 5: "BAD_ARGS"}
 

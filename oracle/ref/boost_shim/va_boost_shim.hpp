@@ -245,18 +245,56 @@ template <class State> struct runge_kutta_dopri5 {
     }
 };
 
-// fixed-step steppers referenced by the ButcherTable's typeid checks
+// Fixed-step steppers for the reference's non-controlled loop
+// (detail/runge_kutta.hpp:37-72).  euler: out = 1 x + dt f(x) (odeint's
+// scale_sum2(1, dt)); runge_kutta4: odeint's generic explicit RK with the
+// rk4 coefficients, each stage x + (a_m0 dt) k_0 + ... left to right with
+// every coefficient of the row, then x + (b_0 dt) k_0 + ... + (b_3 dt) k_3.
 template <class State> struct euler {
     typedef State state_type;
     typedef stepper_tag stepper_category;
+    template <class System> void do_step(System system, State &x, double t, double dt)
+    {
+        State dxdt(x.size());
+        system(x, dxdt, t);
+        for (std::size_t i = 0; i < x.size(); i++)
+            x[i] = 1.0 * x[i] + dt * dxdt[i];
+    }
 };
 template <class State> struct runge_kutta4 {
     typedef State state_type;
     typedef stepper_tag stepper_category;
+    template <class System> void do_step(System system, State &x, double t, double dt)
+    {
+        const std::size_t n = x.size();
+        const auto a1 = rk4_coefficients_a1<double>();
+        const auto a2 = rk4_coefficients_a2<double>();
+        const auto a3 = rk4_coefficients_a3<double>();
+        const auto b = rk4_coefficients_b<double>();
+        const auto c = rk4_coefficients_c<double>();
+        const std::vector<std::vector<double>> a = {{}, {a1.begin(), a1.end()}, {a2.begin(), a2.end()},
+                                                    {a3.begin(), a3.end()}};
+        std::vector<State> K(4, State(n));
+        State xtmp(n);
+        system(x, K[0], t);
+        for (int m = 1; m < 4; m++) {
+            for (std::size_t i = 0; i < n; i++) {
+                double acc = 1.0 * x[i];
+                for (int j = 0; j < m; j++)
+                    acc = acc + (a[m][j] * dt) * K[j][i];
+                xtmp[i] = acc;
+            }
+            system(xtmp, K[m], t + c[m] * dt);
+        }
+        for (std::size_t i = 0; i < n; i++) {
+            double acc = 1.0 * x[i];
+            for (int j = 0; j < 4; j++)
+                acc = acc + (b[j] * dt) * K[j][i];
+            x[i] = acc;
+        }
+    }
 };
-template <class State> struct runge_kutta4_classic {
-    typedef State state_type;
-    typedef stepper_tag stepper_category;
+template <class State> struct runge_kutta4_classic : runge_kutta4<State> {
 };
 template <class State> struct runge_kutta_fehlberg78 {
     typedef State state_type;

@@ -25,6 +25,8 @@ using State = std::vector<double>;
 using Dopri5 = odeint::runge_kutta_dopri5<State>;
 using CashKarp = odeint::runge_kutta_cash_karp54<State>;
 using Fehlberg78 = odeint::runge_kutta_fehlberg78<State>;
+using RK4 = odeint::runge_kutta4<State>;
+using Euler = odeint::euler<State>;
 
 template <>
 void ButcherTable::initialize<Dopri5>(Dopri5 stepper, odeint::error_stepper_tag)
@@ -91,7 +93,10 @@ static int run(System sys, int n, int nout, int npar, double atol, double rtol, 
     State x0(y0, y0 + n), alphas(p, p + npar);
     size_t steps = 0;
     try {
-        steps = runge_kutta(odeint::make_controlled<Stepper>(atol, rtol), sys, x0, alphas, t0, t1, dt0, driver);
+        if constexpr (std::is_same<typename Stepper::stepper_category, odeint::stepper_tag>::value)
+            steps = runge_kutta(Stepper(), sys, x0, alphas, t0, t1, dt0, driver); // fixed step dt0
+        else
+            steps = runge_kutta(odeint::make_controlled<Stepper>(atol, rtol), sys, x0, alphas, t0, t1, dt0, driver);
     } catch (std::exception &e) {
         std::cerr << "runge_kutta: " << e.what() << std::endl;
         return 1;
@@ -127,7 +132,8 @@ static int run(System sys, int n, int nout, int npar, double atol, double rtol, 
 
 // model: 0 VdP (Lienard), 1 VdP (reference example form), 2 damped
 // oscillator, 3 GLV; tableau: 0 DOPRI5, 1 Cash-Karp, 2 Fehlberg 7(8) (the
-// reference's own ButcherTable branch).  Returns 0 on success.
+// reference's own ButcherTable branch), 3 fixed-step RK4, 4 fixed-step Euler
+// (step dt0).  Returns 0 on success.
 extern "C" int ref_solve(int model, int tableau, int n, int nout, int npar, double atol, double rtol, double dt0,
                          const double *y0, const double *p, double t0, double t1, const double *lam_in,
                          const double *mu_in, long cap, double *times, double *states, long *T, double *yT,
@@ -137,7 +143,9 @@ extern "C" int ref_solve(int model, int tableau, int n, int nout, int npar, doub
 #define VA_RUN(SYS)                                                                                \
     (tableau == 0   ? run<Dopri5>(SYS(), VA_ARGS)                                                  \
      : tableau == 1 ? run<CashKarp>(SYS(), VA_ARGS)                                                \
-                    : run<Fehlberg78>(SYS(), VA_ARGS))
+     : tableau == 2 ? run<Fehlberg78>(SYS(), VA_ARGS)                                              \
+     : tableau == 3 ? run<RK4>(SYS(), VA_ARGS)                                                     \
+                    : run<Euler>(SYS(), VA_ARGS))
     switch (model) {
     case 0:
         return VA_RUN(VanDerPol);

@@ -26,7 +26,7 @@ REF = "/root/reference"
 from vectorizedadjoint_gb300 import workloads as W  # noqa: E402
 
 MODEL_ID = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3}
-TABLEAU_ID = {"dopri5": 0, "ck54": 1, "rkf78": 2}
+TABLEAU_ID = {"dopri5": 0, "ck54": 1, "rkf78": 2, "rk4": 3, "euler": 4}
 
 
 def load():
@@ -35,7 +35,7 @@ def load():
     return L
 
 
-def solve(L, model, tableau, n, npar, tol, y0, p, t1, lam, mu, cap=200000):
+def solve(L, model, tableau, n, npar, tol, y0, p, t1, lam, mu, cap=200000, dt=1e-3):
     nout = lam.shape[0]
     times = np.zeros(cap + 1)
     states = np.zeros((cap + 1, n))
@@ -46,7 +46,7 @@ def solve(L, model, tableau, n, npar, tol, y0, p, t1, lam, mu, cap=200000):
     ptr = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(ctypes.c_void_p)
     keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (y0, p, lam, mu)]
     rc = L.ref_solve(MODEL_ID[model], TABLEAU_ID[tableau], n, nout, npar, ctypes.c_double(tol),
-                     ctypes.c_double(tol), ctypes.c_double(1e-3), ptr(keep[0]), ptr(keep[1]),
+                     ctypes.c_double(tol), ctypes.c_double(dt), ptr(keep[0]), ptr(keep[1]),
                      ctypes.c_double(0.0), ctypes.c_double(t1), ptr(keep[2]), ptr(keep[3]), ctypes.c_long(cap),
                      times.ctypes.data_as(ctypes.c_void_p), states.ctypes.data_as(ctypes.c_void_p),
                      ctypes.byref(T), yT.ctypes.data_as(ctypes.c_void_p), lo.ctypes.data_as(ctypes.c_void_p),
@@ -60,9 +60,12 @@ def main():
     cases = []
     # benchmark configurations: cost seeds from y(T) (sum of squares) or ones
     # (sum); then the same draws with the Fehlberg 7(8) pair (the reference's
-    # ButcherTable branch for runge_kutta_fehlberg78)
-    for name, count, tableau in [("vdp1", 1, None), ("dho", 4, None), ("vdpb", 4, None), ("glv10", 3, None),
-                                 ("vdpb", 2, "rkf78"), ("dho", 2, "rkf78"), ("glv10", 1, "rkf78")]:
+    # ButcherTable branch for runge_kutta_fehlberg78) and with the fixed-step
+    # loop (runge_kutta4 at dt = 0.01, euler at dt = 1e-3)
+    for name, count, tableau, dt in [("vdp1", 1, None, 1e-3), ("dho", 4, None, 1e-3), ("vdpb", 4, None, 1e-3),
+                                     ("glv10", 3, None, 1e-3), ("vdpb", 2, "rkf78", 1e-3), ("dho", 2, "rkf78", 1e-3),
+                                     ("glv10", 1, "rkf78", 1e-3), ("vdpb", 2, "rk4", 1e-2), ("dho", 1, "rk4", 1e-2),
+                                     ("glv10", 1, "rk4", 1e-2), ("vdpb", 1, "euler", 1e-3)]:
         w = W.make(name, batch=count)
         c = w["cfg"]
         if tableau:
@@ -73,12 +76,12 @@ def main():
             mu = np.zeros((1, c["npar"]))
             # forward first to get y(T) for the sum-of-squares seed
             T, times, states, yT, _, _ = solve(L, c["model"], c["tableau"], c["n"], c["npar"], c["tol"], y0, p, t1,
-                                               np.zeros((1, c["n"])), mu)
+                                               np.zeros((1, c["n"])), mu, dt=dt)
             lam = (2.0 * yT if c["cost"] == "sumsq" else np.ones(c["n"]))[None, :]
             T, times, states, yT, lo, mo = solve(L, c["model"], c["tableau"], c["n"], c["npar"], c["tol"], y0, p,
-                                                 t1, lam, mu)
+                                                 t1, lam, mu, dt=dt)
             cases.append(dict(name=f"{name}[{b}]", model=c["model"], tableau=c["tableau"], n=c["n"],
-                              npar=c["npar"], tol=c["tol"], y0=y0, p=p, t1=t1, lam=lam, mu=mu, T=T, yT=yT,
+                              npar=c["npar"], tol=c["tol"], dt=dt, y0=y0, p=p, t1=t1, lam=lam, mu=mu, T=T, yT=yT,
                               dy0=lo, dp=mo, times=times if name == "vdp1" else None,
                               states=states if name == "vdp1" else None))
     # the reference's GLV example on its own data, identity seeds (Nout = N)
@@ -91,7 +94,7 @@ def main():
         for tol in (1e-6, 1e-9):
             T, times, states, yT, lo, mo = solve(L, "glv", "ck54", N, N + N * N, tol, y0, vals, 10.0, lam, mu)
             cases.append(dict(name=f"glv_example_N{N}_tol{tol:g}", model="glv", tableau="ck54", n=N,
-                              npar=N + N * N, tol=tol, y0=y0, p=vals, t1=10.0, lam=lam, mu=mu, T=T, yT=yT,
+                              npar=N + N * N, tol=tol, dt=1e-3, y0=y0, p=vals, t1=10.0, lam=lam, mu=mu, T=T, yT=yT,
                               dy0=lo, dp=mo, times=None, states=None))
     out = {}
     for k, cs in enumerate(cases):

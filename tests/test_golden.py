@@ -23,7 +23,7 @@ def cases():
             c[s] = str(c[s])
         for s in ("n", "npar", "T"):
             c[s] = int(c[s])
-        c["tol"], c["t1"] = float(c["tol"]), float(c["t1"])
+        c["tol"], c["t1"], c["dt"] = float(c["tol"]), float(c["t1"]), float(c["dt"])
         out.append(c)
     return out
 
@@ -39,7 +39,7 @@ def rel(a, b):
 
 @pytest.mark.parametrize("c", CASES, ids=IDS)
 def test_oracle_matches_reference(oracle, c):
-    pb = oracle.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"], pow_mode=1)
+    pb = oracle.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"], dt0=c["dt"], pow_mode=1)
     fw = oracle.forward(pb, c["y0"], c["p"], 0.0, c["t1"])
     assert fw["status"] == 0
     assert fw["n_acc"] == c["T"]
@@ -66,7 +66,8 @@ def test_gpu_matches_reference(cuda, c):
     from vectorizedadjoint_gb300 import Solver
     dev = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
     Q = c["lam"].shape[0]
-    s = Solver(c["model"], c["n"], c["npar"], 1, nout=Q, tableau=c["tableau"], atol=c["tol"], rtol=c["tol"])
+    s = Solver(c["model"], c["n"], c["npar"], 1, nout=Q, tableau=c["tableau"], atol=c["tol"], rtol=c["tol"],
+               dt0=c["dt"])
     P = dev(c["p"][None, :])
     f = s.forward(dev(c["y0"][None, :]), P, dev([0.0]), dev([c["t1"]]))
     bw = s.backward(P, dev(c["lam"][None]), dev(c["mu"][None]))
