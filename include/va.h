@@ -56,10 +56,21 @@ typedef enum {
 } va_model;
 
 /* Embedded pairs (ButcherTable.hpp:259-308 for Cash-Karp, :191-246 for
- * Fehlberg 7(8); Dormand-Prince is added from the published tableau).
- * Fehlberg 7(8) is compiled for the one-thread models (VdP, damped
- * oscillator, decay); va_create rejects it for GLV. */
-typedef enum { VA_TAB_DOPRI5 = 0, VA_TAB_CK54 = 1, VA_TAB_RKF78 = 2 } va_tableau;
+ * Fehlberg 7(8); Dormand-Prince is added from the published tableau) and
+ * the fixed-step steppers (ButcherTable.hpp:39-125: runge_kutta4, euler),
+ * which run the reference's non-controlled loop
+ * (detail/runge_kutta.hpp:37-72) with step dt0: t_n = t0 + n dt0 while
+ * t_n + dt0 <= t1 (to within DBL_EPSILON), so the last record can lie short
+ * of t1, as in the reference.  Fehlberg 7(8) and the fixed-step steppers are
+ * compiled for the one-thread models and the per-instance GLV lane groups;
+ * va_create rejects them for VA_MODEL_GLV_SHARED. */
+typedef enum {
+    VA_TAB_DOPRI5 = 0,
+    VA_TAB_CK54 = 1,
+    VA_TAB_RKF78 = 2,
+    VA_TAB_RK4 = 3,  /* fixed step */
+    VA_TAB_EULER = 4 /* fixed step */
+} va_tableau;
 
 typedef enum {
     VA_PREC_FP64 = 0, /* all arithmetic FP64: the drop-in path                          */
@@ -96,7 +107,8 @@ typedef struct {
     int32_t tableau;     /* va_tableau                                            */
     int32_t precision;   /* va_precision                                          */
     double atol, rtol;   /* odeint make_controlled(abs, rel)                      */
-    double dt0;          /* initial step (runge_kutta(..., dt, ...))              */
+    double dt0;          /* initial step (runge_kutta(..., dt, ...)); the step of
+                            the fixed-step tableaux                               */
     int32_t max_steps;   /* accepted-step cap per instance                        */
     int32_t max_rejects; /* odeint failed_step_checker limit (500)                */
     int64_t ckpt_budget_bytes; /* HBM budget for checkpoints (0 = default 16 GiB) */

@@ -15,7 +15,7 @@ STATUS_NAMES = {0: "VA_OK", 1: "VA_MAX_REJECTS", 2: "VA_MAX_STEPS", 3: "VA_NONFI
                 8: "VA_RECOMPUTE_MISMATCH", 9: "VA_NOT_RUN"}
 
 MODELS = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3, "decay": 4, "glv_shared": 5}
-TABLEAUX = {"dopri5": 0, "ck54": 1, "rkf78": 2}
+TABLEAUX = {"dopri5": 0, "ck54": 1, "rkf78": 2, "rk4": 3, "euler": 4}
 PRECISIONS = {"fp64": 0, "mixed": 1, "mixed_dw": 2}
 COSTS = {"seeds": -1, "sumsq": 0, "sum": 1}
 

@@ -80,6 +80,7 @@ struct va_handle {
     // two-level checkpointing: stride, end times, re-integration scratch
     int stride = 1;
     double *inst_t1 = nullptr;
+    double *inst_t0 = nullptr; // start times (fixed-step two-level backward)
     double *scratch = nullptr;
     size_t scratch_doubles = 0;
 
@@ -203,6 +204,7 @@ va_status ensure_buffers(va_handle *h)
     VA_CUDA(h, cudaMalloc(&h->ctl, sizeof(va::Control)));
     VA_CUDA(h, cudaMemset(h->ctl, 0, sizeof(va::Control)));
     VA_CUDA(h, cudaMalloc(&h->inst_t1, (size_t)B * sizeof(double)));
+    VA_CUDA(h, cudaMalloc(&h->inst_t0, (size_t)B * sizeof(double)));
     if (!h->bks && h->opt.schedule == 0) {
         VA_CUDA(h, cudaMalloc(&h->order_fwd, (size_t)B * sizeof(int)));
         VA_CUDA(h, cudaMalloc(&h->order_bwd, (size_t)B * sizeof(int)));
@@ -330,6 +332,7 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
     a.inst_last = h->inst_last;
     a.inst_status = h->inst_status;
     a.inst_t1 = h->inst_t1;
+    a.inst_t0 = h->inst_t0;
     a.stride = h->stride;
     a.pool = pool_of(h);
     a.ctl = h->ctl;
@@ -416,9 +419,11 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
             return fail(h, VA_BAD_ARGS, "two-level scratch not sized for the stride%s");
         a.stride = h->stride;
         a.inst_t1 = h->inst_t1;
+        a.inst_t0 = h->inst_t0;
         a.scratch = h->scratch;
         a.atol = h->opt.atol;
         a.rtol = h->opt.rtol;
+        a.dt0 = h->opt.dt0;
         a.max_fail = h->opt.max_rejects;
         VA_CUDA(h, cudaMemsetAsync(&h->ctl->adj_next, 0, sizeof(unsigned int), s));
         VA_CUDA(h, launch(h->ks->bwd2[h->opt.tableau][h->opt.precision], two_level_grid(h), kTwoLevelBlock, &a, s));
@@ -538,7 +543,8 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
         return VA_BAD_ARGS;
     // checkpoint stride: -1 automatic, 0/1 every step, k > 1 every k-th step
     // (two-level checkpointing: one-thread-per-instance models only)
-    if (o.ckpt_stride < -1 || ((o.ckpt_stride > 1 || o.ckpt_stride == -1) && !(ks && ks->tpi == 1)))
+    if (o.ckpt_stride < -1 ||
+        ((o.ckpt_stride > 1 || o.ckpt_stride == -1) && !(ks && ks->tpi == 1 && ks->bwd2[o.tableau][o.precision])))
         return VA_BAD_ARGS;
     va_handle *h = new va_handle();
     h->stride = o.ckpt_stride > 1 ? o.ckpt_stride : 1;
@@ -575,7 +581,7 @@ va_status va_destroy(va_handle *h)
                     h->s_yT,     h->s_dy0,      h->s_dpar,  h->s_nacc,    h->s_status,
                     h->s_nrej,   h->s_lam,      h->s_mu,    h->At,        h->Aw,
                     h->Atw,      h->dA_part,    h->inst_t1, h->scratch, h->order_fwd,
-                    h->order_bwd, h->order_work, h->inst_work};
+                    h->order_bwd, h->order_work, h->inst_work, h->inst_t0};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);

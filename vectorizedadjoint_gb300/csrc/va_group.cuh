@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
     const int CH = a.pool.chunk_len;
 
     int b = -1;
-    double y[1], t = 0.0, t1 = 0.0, dt = 0.0;
+    double y[1], t = 0.0, t1 = 0.0, dt = 0.0, t_start = 0.0;
     S ys[1], k0[1], p[P];
     int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
     bool at_top = true;
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
             b = a.order[b];
         y[0] = a.y0[(size_t)b * NT + li];
         M::template load_params<S>(a.par + (size_t)b * PT, li, p);
-        t = a.t0[b];
+        t = t_start = a.t0[b];
         t1 = a.t1[b];
         dt = a.dt0;
         count = rej = fails = 0;
@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
             continue;
         }
         if (at_top) {
-            if (!(t1 - t > kDblEps)) {
+            if (Tab::FIXED ? !((t + dt) - t1 <= kDblEps) : !(t1 - t > kDblEps)) {
                 finish();
                 alive = fetch();
                 continue;
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
                 continue;
             }
             write();
-            if ((t + dt) - t1 > kDblEps)
+            if (!Tab::FIXED && (t + dt) - t1 > kDblEps)
                 dt = t1 - t;
             fails = 0;
             at_top = false;
@@ -274,8 +274,12 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
             rej++;
             ok = false;
         } else {
-            t += dt;
-            dt = increase_step<Tab, S>(dt, err);
+            if constexpr (Tab::FIXED) {
+                t = fixed_time(t_start, count + 1, dt);
+            } else {
+                t += dt;
+                dt = increase_step<Tab, S>(dt, err);
+            }
             ys[0] = ynew_s[0];
             if constexpr (std::is_same<S, dword>::value)
                 y[0] = to_d(ynew_s[0]);

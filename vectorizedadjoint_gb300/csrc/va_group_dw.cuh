@@ -96,6 +96,8 @@ __device__ __forceinline__ dword attempt_glv_dw(dword y, dword k0, const dword (
         K[m][0] = L::rhs(X[0], p, base, mask);
     }
     ynew = axpy_dw(y, dt, wsum_dw<NS>(typename BWeights::template of<Tab>(), K, 0));
+    if constexpr (Tab::FIXED)
+        return dword(0.0f, 0.0f); // no error estimate: every attempt is accepted
     if constexpr (Tab::FSAL)
         knew = L::rhs(ynew, p, base, mask);
     dacc e = wsum_dw<NS>(typename EWeights::template of<Tab>(), K, 0);
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
     const DwTol tol{dword(a.atol), dword(a.rtol)};
 
     int b = -1;
-    double t = 0.0, t1 = 0.0;
+    double t = 0.0, t1 = 0.0, t_start = 0.0;
     dword y, k0, dt, p[P];
     int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
     bool at_top = true, to_end = false;
@@ -149,7 +151,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
             b = a.order[b];
         y = dword(a.y0[(size_t)b * NN + li]);
         M::template load_params<dword>(a.par + (size_t)b * PT, li, p);
-        t = a.t0[b];
+        t = t_start = a.t0[b];
         t1 = a.t1[b];
         dt = dword(a.dt0);
         count = rej = fails = 0;
@@ -230,7 +232,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
             continue;
         }
         if (at_top) {
-            if (!(t1 - t > kDblEps)) {
+            if (Tab::FIXED ? !((t + a.dt0) - t1 <= kDblEps) : !(t1 - t > kDblEps)) {
                 finish();
                 alive = fetch();
                 continue;
@@ -244,7 +246,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
                 continue;
             }
             write();
-            to_end = (t + to_d_int(dt)) - t1 > kDblEps;
+            to_end = !Tab::FIXED && (t + to_d_int(dt)) - t1 > kDblEps;
             if (to_end)
                 dt = dword(t1 - t);
             fails = 0;
@@ -264,8 +266,12 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
             to_end = false;
             ok = false;
         } else {
-            t = to_end ? t1 : t + to_d_int(dt);
-            dt = increase_dw<Tab>(dt, err);
+            if constexpr (Tab::FIXED) {
+                t = fixed_time(t_start, count + 1, a.dt0);
+            } else {
+                t = to_end ? t1 : t + to_d_int(dt);
+                dt = increase_dw<Tab>(dt, err);
+            }
             y = ynew;
             if constexpr (Tab::FSAL)
                 k0 = knew;

@@ -15,7 +15,8 @@ void fill_fp64_dho(KernelSet &k);
 void fill_fp64_decay(KernelSet &k);
 
 template <class M>
-static KernelSet make_set(void (*fill_fp64)(KernelSet &), void (*fill_rkf78)(KernelSet &))
+static KernelSet make_set(void (*fill_fp64)(KernelSet &), void (*fill_rkf78)(KernelSet &),
+                          void (*fill_fixed)(KernelSet &))
 {
     KernelSet k{};
     k.N = M::N;
@@ -42,27 +43,29 @@ static KernelSet make_set(void (*fill_fp64)(KernelSet &), void (*fill_rkf78)(Ker
     k.bwd2[1][2] = (const void *)backward_kernel_2level_dw<M, TabCK54>;
     k.dw_records = true;
     fill_rkf78(k);
+    fill_fixed(k);
     return k;
 }
 
 const KernelSet *kernels_vdp()
 {
-    static const KernelSet k = make_set<ModelVdP>(fill_fp64_vdp, fill_rkf78_vdp);
+    static const KernelSet k = make_set<ModelVdP>(fill_fp64_vdp, fill_rkf78_vdp, fill_fixed_vdp);
     return &k;
 }
 const KernelSet *kernels_vdp_petsc()
 {
-    static const KernelSet k = make_set<ModelVdPPetsc>(fill_fp64_vdp_petsc, fill_rkf78_vdp_petsc);
+    static const KernelSet k = make_set<ModelVdPPetsc>(fill_fp64_vdp_petsc, fill_rkf78_vdp_petsc,
+                                                          fill_fixed_vdp_petsc);
     return &k;
 }
 const KernelSet *kernels_dho()
 {
-    static const KernelSet k = make_set<ModelDHO>(fill_fp64_dho, fill_rkf78_dho);
+    static const KernelSet k = make_set<ModelDHO>(fill_fp64_dho, fill_rkf78_dho, fill_fixed_dho);
     return &k;
 }
 const KernelSet *kernels_decay()
 {
-    static const KernelSet k = make_set<ModelDecay>(fill_fp64_decay, fill_rkf78_decay);
+    static const KernelSet k = make_set<ModelDecay>(fill_fp64_decay, fill_rkf78_decay, fill_fixed_decay);
     return &k;
 }
 

@@ -74,6 +74,8 @@ struct FwdParams {
     int *inst_last;  // [B] last checkpoint chunk
     int *inst_status;// [B]
     double *inst_t1; // [B] end times (kept for segment re-integration; may be null)
+    double *inst_t0; // [B] start times, written by the fixed-step sweeps (the
+                     // two-level backward re-forms t_0 + n dt from them; may be null)
     int stride;      // store every stride-th accepted step (and the last); 1 = all
     const int *order;// [B] work order (may be null = index order)
     int *inst_work;  // [B] attempts (accepted + rejected) of this sweep, the next
@@ -111,8 +113,10 @@ struct AdjParams {
     // two-level checkpointing (stride > 1): segment re-integration
     int stride;
     const double *inst_t1;   // [B]
+    const double *inst_t0;   // [B] start times (fixed-step tableaux)
     double *scratch;         // per thread: (stride + 1) records
     double atol, rtol;
+    double dt0;              // the step of the fixed-step tableaux
     int max_fail;
 };
 
@@ -223,11 +227,17 @@ struct RootSteps {
 
 // odeint default_step_adjuster::decrease_step:
 //   dt *= max(0.9 err^(-1/(q-1)), 0.2)
+// (fixed-step tableaux: dt unchanged; their sweeps never call it)
 template <class Tab, class S = double>
 __host__ __device__ __forceinline__ double decrease_step(double dt, double err)
 {
-    double f = 9.0 / 10.0 * inv_root<Tab::ERROR_ORDER - 1, RootSteps<S>::value>(err);
-    return dt * fmax(f, 1.0 / 5.0);
+    if constexpr (Tab::FIXED) {
+        (void)err;
+        return dt;
+    } else {
+        double f = 9.0 / 10.0 * inv_root<Tab::ERROR_ORDER - 1, RootSteps<S>::value>(err);
+        return dt * fmax(f, 1.0 / 5.0);
+    }
 }
 
 // odeint default_step_adjuster::increase_step:
@@ -235,6 +245,8 @@ __host__ __device__ __forceinline__ double decrease_step(double dt, double err)
 template <class Tab, class S = double>
 __host__ __device__ __forceinline__ double increase_step(double dt, double err)
 {
+    if constexpr (Tab::FIXED)
+        return dt;
     if (err < 0.5) {
         // 5^-p as the correctly rounded quotient (1/3125, 1/390625), what
         // pow(5.0, -p) returns
@@ -294,10 +306,10 @@ __host__ __device__ __forceinline__ void form_stage(int m, const double (&y)[N],
 // paths give ynew in FP64.  The double-word path leaves ynew to the caller,
 // which rounds ynew_s to FP64 once per accepted step.
 template <class M, class Tab, class S>
-__host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], const S (&ys)[M::N],
-                                                   const S (&k0)[M::N], const S (&p)[M::P], double t,
-                                                   double dt, double atol, double rtol, double (&ynew)[M::N],
-                                                   S (&ynew_s)[M::N], S (&knew)[M::N])
+__host__ __device__ __forceinline__ double attempt_pair(const double (&y)[M::N], const S (&ys)[M::N],
+                                                        const S (&k0)[M::N], const S (&p)[M::P], double t,
+                                                        double dt, double atol, double rtol,
+                                                        double (&ynew)[M::N], S (&ynew_s)[M::N], S (&knew)[M::N])
 {
     constexpr int N = M::N, NS = Tab::S;
     S K[NS][N];
@@ -425,6 +437,71 @@ __host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], cons
     return num / den;
 }
 
+// One step of a fixed-step tableau: the stages and
+// y_new = y + sum_j (b_j dt) K_j (odeint's explicit_generic_rk::do_step, the
+// same arithmetic as the embedded pairs' solution update); no error estimate.
+template <class M, class Tab, class S>
+__host__ __device__ __forceinline__ void step_fixed(const double (&y)[M::N], const S (&ys)[M::N],
+                                                    const S (&k0)[M::N], const S (&p)[M::P], double t,
+                                                    double dt, double (&ynew)[M::N], S (&ynew_s)[M::N])
+{
+    constexpr int N = M::N, NS = Tab::S;
+    S K[NS][N];
+    const S sdt = std::is_same<S, double>::value ? S(dt) : from_d<S>(dt);
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        K[0][i] = k0[i];
+#pragma unroll
+    for (int m = 1; m < NS; m++) {
+        S X[N];
+        form_stage<Tab, N, S>(m, y, ys, K, dt, sdt, X);
+        M::template rhs<S>(X, p, S(t + Tab::c(m) * dt), K[m]);
+    }
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        if constexpr (std::is_same<S, double>::value) {
+            double acc = y[i];
+#pragma unroll
+            for (int j = 0; j < NS; j++)
+                if (Tab::b(j) != 0.0)
+                    acc = acc + (Tab::b(j) * dt) * K[j][i];
+            ynew[i] = acc;
+            ynew_s[i] = acc;
+        } else {
+            S acc = S(0);
+#pragma unroll
+            for (int j = 0; j < NS; j++)
+                if (Tab::b(j) != 0.0)
+                    acc = madd(S(Tab::b(j)), K[j][i], acc);
+            if constexpr (std::is_same<S, float>::value) {
+                ynew[i] = fma(dt, (double)acc, y[i]);
+                ynew_s[i] = (float)ynew[i];
+            } else {
+                ynew_s[i] = madd(acc, sdt, ys[i]);
+            }
+        }
+    }
+}
+
+// attempt_pair for the embedded pairs; a fixed-step tableau's step, with
+// error 0 (always accepted)
+template <class M, class Tab, class S>
+__host__ __device__ __forceinline__ double attempt(const double (&y)[M::N], const S (&ys)[M::N],
+                                                   const S (&k0)[M::N], const S (&p)[M::P], double t,
+                                                   double dt, double atol, double rtol, double (&ynew)[M::N],
+                                                   S (&ynew_s)[M::N], S (&knew)[M::N])
+{
+    if constexpr (Tab::FIXED) {
+        (void)atol;
+        (void)rtol;
+        (void)knew;
+        step_fixed<M, Tab, S>(y, ys, k0, p, t, dt, ynew, ynew_s);
+        return 0.0;
+    } else {
+        return attempt_pair<M, Tab, S>(y, ys, k0, p, t, dt, atol, rtol, ynew, ynew_s, knew);
+    }
+}
+
 // State after an accepted attempt: y (FP64, what a checkpoint stores), its
 // stage-precision copy ys and k0 = f(y).  For double-word stages ys restarts
 // from the rounded FP64 value, exactly what a re-integration from a
@@ -531,7 +608,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
     const int CH = a.pool.chunk_len;
 
     int b = -1;
-    double y[N], t = 0.0, t1 = 0.0, dt = 0.0;
+    double y[N], t = 0.0, t1 = 0.0, dt = 0.0, t_start = 0.0;
     S ys[N], k0[N], p[P]; // ys: y in stage precision, carried across steps
     int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
     bool at_top = true;
@@ -549,7 +626,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
 #pragma unroll
         for (int k = 0; k < P; k++)
             p[k] = from_d<S>(a.par[(size_t)b * P + k]);
-        t = a.t0[b];
+        t = t_start = a.t0[b];
         t1 = a.t1[b];
         dt = a.dt0;
         count = rej = fails = 0;
@@ -614,6 +691,8 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
         note_work(a, b, count + rej);
         if (a.inst_t1)
             a.inst_t1[b] = t1;
+        if (Tab::FIXED && a.inst_t0)
+            a.inst_t0[b] = t_start;
         if (a.n_acc_out)
             a.n_acc_out[b] = count;
         if (a.n_rej_out)
@@ -630,8 +709,9 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
             continue;
         }
         if (at_top) {
-            // while (less_with_sign(t, t1, dt))  (runge_kutta.hpp:155)
-            if (!(t1 - t > kDblEps)) {
+            // while (less_with_sign(t, t1, dt))  (runge_kutta.hpp:155); fixed
+            // steps: while (less_eq_with_sign(t + dt, t1, dt))  (:54)
+            if (Tab::FIXED ? !((t + dt) - t1 <= kDblEps) : !(t1 - t > kDblEps)) {
                 finish();
                 alive = fetch();
                 continue;
@@ -650,7 +730,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
                 slot++;
             }
             // end clamp (runge_kutta.hpp:160-163)
-            if ((t + dt) - t1 > kDblEps)
+            if (!Tab::FIXED && (t + dt) - t1 > kDblEps)
                 dt = t1 - t;
             fails = 0;
             at_top = false;
@@ -668,8 +748,12 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
             rej++;
             ok = false;
         } else {
-            t += dt;
-            dt = increase_step<Tab, S>(dt, err);
+            if constexpr (Tab::FIXED) {
+                t = fixed_time(t_start, count + 1, dt); // t_0 + n dt (:61-62)
+            } else {
+                t += dt;
+                dt = increase_step<Tab, S>(dt, err);
+            }
             accept_state<M, Tab, S>(y, ys, k0, ynew, ynew_s, knew, p, t);
             ok = true;
         }
@@ -915,6 +999,8 @@ __global__ void __launch_bounds__(256) backward_kernel_2level(AdjParams a)
     double *scr = a.scratch + ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * (SK + 1) * RS;
 
     int b = -1, q = 0, T = 0, R = 0, k = 0, last = -1, chunk = -1, slot = 0, L = 0, done = 0, jb = 0, fails = 0;
+    int first = 0;          // step index of the segment's first record
+    double t_start = 0.0;   // t_0 (fixed-step tableaux)
     int phase = 0; // 0: re-integrate segment k, 1: back-step through it
     double lam[N], mu[P], t = 0.0, dt = 0.0, t1 = 0.0, y[N], t_end = 0.0, y_end[N];
     S p[P], ys[N], k0[N];
@@ -952,7 +1038,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level(AdjParams a)
         read_record<N>(r, rec_t, rec_y);
         t = rec_t;
         dt = r[1];
-        const int first = k * SK;
+        first = k * SK;
         L = (k == R - 2) ? T - first : SK;
 #pragma unroll
         for (int i = 0; i < N; i++) {
@@ -1023,6 +1109,8 @@ __global__ void __launch_bounds__(256) backward_kernel_2level(AdjParams a)
             R = (T + SK - 1) / SK + 1;
             last = a.inst_last[b];
             t1 = a.inst_t1[b];
+            if constexpr (Tab::FIXED)
+                t_start = a.inst_t0[b];
             q = 0;
             start_seed();
             return true;
@@ -1044,7 +1132,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level(AdjParams a)
         if (phase == 0) {
             // one attempt of the forward controller, as forward_kernel does
             if (at_top) {
-                if ((t + dt) - t1 > kDblEps)
+                if (!Tab::FIXED && (t + dt) - t1 > kDblEps)
                     dt = t1 - t;
                 fails = 0;
                 at_top = false;
@@ -1062,8 +1150,12 @@ __global__ void __launch_bounds__(256) backward_kernel_2level(AdjParams a)
                 dt = decrease_step<Tab, S>(dt, err);
                 continue;
             }
-            t += dt;
-            dt = increase_step<Tab, S>(dt, err);
+            if constexpr (Tab::FIXED) {
+                t = fixed_time(t_start, first + done + 1, dt);
+            } else {
+                t += dt;
+                dt = increase_step<Tab, S>(dt, err);
+            }
             accept_state<M, Tab, S>(y, ys, k0, ynew, ynew_s, knew, p, t);
             at_top = true;
             done++;

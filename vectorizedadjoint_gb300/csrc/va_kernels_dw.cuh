@@ -105,12 +105,18 @@ __host__ __device__ __forceinline__ dword inv_root_dw(dword a)
 }
 
 // odeint default_step_adjuster::decrease_step: dt * max(0.9 err^(-1/(q-1)), 0.2)
+// (fixed-step tableaux: dt unchanged; their sweeps never call it)
 template <class Tab>
 __host__ __device__ __forceinline__ dword decrease_dw(dword dt, dword err)
 {
-    const dword f = dword(9.0 / 10.0) * inv_root_dw<Tab::ERROR_ORDER - 1>(err);
-    const dword lim = dword(1.0 / 5.0);
-    return dt * (dw_greater(f, lim) ? f : lim);
+    if constexpr (Tab::FIXED) {
+        (void)err;
+        return dt;
+    } else {
+        const dword f = dword(9.0 / 10.0) * inv_root_dw<Tab::ERROR_ORDER - 1>(err);
+        const dword lim = dword(1.0 / 5.0);
+        return dt * (dw_greater(f, lim) ? f : lim);
+    }
 }
 
 // odeint default_step_adjuster::increase_step:
@@ -118,6 +124,8 @@ __host__ __device__ __forceinline__ dword decrease_dw(dword dt, dword err)
 template <class Tab>
 __host__ __device__ __forceinline__ dword increase_dw(dword dt, dword err)
 {
+    if constexpr (Tab::FIXED)
+        return dt;
     if (dw_less(err, dword(0.5))) {
         const dword fl = dword(Tab::ERR_FLOOR);
         const dword e = dw_greater(fl, err) ? fl : err;
@@ -235,6 +243,8 @@ __host__ __device__ __forceinline__ dword attempt_dw(const dword (&y)[M::N], con
 #pragma unroll
     for (int i = 0; i < N; i++)
         ynew[i] = axpy_dw(y[i], dt, wsum_dw<NS>(typename BWeights::template of<Tab>(), K, i));
+    if constexpr (Tab::FIXED)
+        return dword(0.0f, 0.0f); // no error estimate: every attempt is accepted
     if constexpr (Tab::FSAL)
         M::template rhs<dword>(ynew, p, t + dt, knew);
     const dword adt = dabs(dt);
@@ -334,7 +344,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
     const DwTol tol{dword(a.atol), dword(a.rtol)};
 
     int b = -1;
-    double t = 0.0, t1 = 0.0;
+    double t = 0.0, t1 = 0.0, t_start = 0.0;
     dword y[N], k0[N], p[P], dt;
     int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
     bool at_top = true, to_end = false;
@@ -352,7 +362,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
 #pragma unroll
         for (int k = 0; k < P; k++)
             p[k] = dword(a.par[(size_t)b * P + k]);
-        t = a.t0[b];
+        t = t_start = a.t0[b];
         t1 = a.t1[b];
         dt = dword(a.dt0);
         count = rej = fails = 0;
@@ -411,6 +421,8 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
         note_work(a, b, count + rej);
         if (a.inst_t1)
             a.inst_t1[b] = t1;
+        if (Tab::FIXED && a.inst_t0)
+            a.inst_t0[b] = t_start;
         if (a.n_acc_out)
             a.n_acc_out[b] = count;
         if (a.n_rej_out)
@@ -427,7 +439,8 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
             continue;
         }
         if (at_top) {
-            if (!(t1 - t > kDblEps)) {
+            // fixed steps: while ((t + dt) - t1 <= eps), dt the FP64 step
+            if (Tab::FIXED ? !((t + a.dt0) - t1 <= kDblEps) : !(t1 - t > kDblEps)) {
                 finish();
                 alive = fetch();
                 continue;
@@ -447,7 +460,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
                     xrec = r + 2 + N;
                 slot++;
             }
-            to_end = (t + to_d_int(dt)) - t1 > kDblEps;
+            to_end = !Tab::FIXED && (t + to_d_int(dt)) - t1 > kDblEps;
             if (to_end)
                 dt = dword(t1 - t);
             fails = 0;
@@ -466,8 +479,12 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
             to_end = false;
             ok = false;
         } else {
-            t = to_end ? t1 : t + to_d_int(dt);
-            dt = increase_dw<Tab>(dt, err);
+            if constexpr (Tab::FIXED) {
+                t = fixed_time(t_start, count + 1, a.dt0);
+            } else {
+                t = to_end ? t1 : t + to_d_int(dt);
+                dt = increase_dw<Tab>(dt, err);
+            }
 #pragma unroll
             for (int i = 0; i < N; i++)
                 y[i] = ynew[i];
@@ -769,7 +786,8 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
 
     int b = -1, q = 0, T = 0, R = 0, k = 0, last = -1, chunk = -1, slot = 0, L = 0, done = 0, jb = 0, fails = 0;
     int phase = 0; // 0: re-integrate segment k, 1: back-step through it
-    double t = 0.0, t1 = 0.0, t_end = 0.0;
+    int first = 0; // step index of the segment's first record
+    double t = 0.0, t1 = 0.0, t_end = 0.0, t_start = 0.0;
     dword lam[N], mu[P], p[P], y[N], k0[N], y_end[N], dt;
     bool at_top = true, to_end = false;
 
@@ -791,7 +809,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
     auto begin_segment = [&]() {
         step_back();
         read_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), t, dt, y);
-        const int first = k * SK;
+        first = k * SK;
         L = (k == R - 2) ? T - first : SK;
         write_record_dw<N>(scr, t, dt, y);
         M::template rhs<dword>(y, p, dword(t), k0);
@@ -833,6 +851,8 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
             R = (T + SK - 1) / SK + 1;
             last = a.inst_last[b];
             t1 = a.inst_t1[b];
+            if constexpr (Tab::FIXED)
+                t_start = a.inst_t0[b];
             q = 0;
             start_seed();
             return true;
@@ -854,7 +874,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
         if (phase == 0) {
             // one attempt of the forward controller, as forward_kernel_dw does
             if (at_top) {
-                to_end = (t + to_d_int(dt)) - t1 > kDblEps;
+                to_end = !Tab::FIXED && (t + to_d_int(dt)) - t1 > kDblEps;
                 if (to_end)
                     dt = dword(t1 - t);
                 fails = 0;
@@ -874,8 +894,12 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
                 to_end = false;
                 continue;
             }
-            t = to_end ? t1 : t + to_d_int(dt);
-            dt = increase_dw<Tab>(dt, err);
+            if constexpr (Tab::FIXED) {
+                t = fixed_time(t_start, first + done + 1, a.dt0);
+            } else {
+                t = to_end ? t1 : t + to_d_int(dt);
+                dt = increase_dw<Tab>(dt, err);
+            }
 #pragma unroll
             for (int i = 0; i < N; i++)
                 y[i] = ynew[i];

@@ -6,8 +6,9 @@
 
 namespace va {
 
-// tableaux: 0 Dormand-Prince 5(4), 1 Cash-Karp 5(4), 2 Fehlberg 7(8)
-constexpr int kTableaux = 3;
+// tableaux: 0 Dormand-Prince 5(4), 1 Cash-Karp 5(4), 2 Fehlberg 7(8),
+// 3 fixed-step runge_kutta4, 4 fixed-step euler
+constexpr int kTableaux = 5;
 
 struct KernelSet {
     int N, P;          // state and parameter counts (0 = runtime n)
@@ -48,6 +49,14 @@ void fill_rkf78_vdp(KernelSet &k);
 void fill_rkf78_vdp_petsc(KernelSet &k);
 void fill_rkf78_dho(KernelSet &k);
 void fill_rkf78_decay(KernelSet &k);
+
+// fixed-step runge_kutta4 and euler entries (their own translation units)
+void fill_fixed_vdp(KernelSet &k);
+void fill_fixed_vdp_petsc(KernelSet &k);
+void fill_fixed_dho(KernelSet &k);
+void fill_fixed_decay(KernelSet &k);
+void fill_fixed_glv5(KernelSet &k);
+void fill_fixed_glv10(KernelSet &k);
 
 // Shared-matrix GLV: bundles of kBundleNB instances per CTA of N threads.
 constexpr int kBundleNB = 4;

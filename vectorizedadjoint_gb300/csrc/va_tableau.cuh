@@ -19,6 +19,7 @@ struct TabDopri5 {
     static constexpr int ERROR_ORDER = 4; // odeint error_order_value
     static constexpr int STEPPER_ORDER = 5;
     static constexpr double ERR_FLOOR = 1.0 / 3125.0; // 5^-STEPPER_ORDER (increase_step)
+    static constexpr bool FIXED = false;  // controlled (embedded error estimate)
     __host__ __device__ static constexpr double a(int i, int j)
     {
         return i == 1 ? (j == 0 ? 1.0 / 5.0 : 0.0)
@@ -58,6 +59,7 @@ struct TabCK54 {
     static constexpr int ERROR_ORDER = 4;
     static constexpr int STEPPER_ORDER = 5;
     static constexpr double ERR_FLOOR = 1.0 / 3125.0;
+    static constexpr bool FIXED = false;
     __host__ __device__ static constexpr double a(int i, int j)
     {
         return i == 1 ? (j == 0 ? 1.0 / 5.0 : 0.0)
@@ -102,6 +104,7 @@ struct TabRKF78 {
     static constexpr int ERROR_ORDER = 7;
     static constexpr int STEPPER_ORDER = 8;
     static constexpr double ERR_FLOOR = 1.0 / 390625.0; // 5^-8
+    static constexpr bool FIXED = false;
     __host__ __device__ static constexpr double a(int i, int j)
     {
         return i == 1 ? (j == 0 ? 2.0 / 27.0 : 0.0)
@@ -132,5 +135,62 @@ struct TabRKF78 {
     }
     static constexpr double E_NEW = 0.0;
 };
+
+// Fixed-step steppers the reference's ButcherTable accepts
+// (lib/include/ButcherTable.hpp:39-125): odeint's runge_kutta4 (the classic
+// fourth-order tableau) and euler.  No error estimate: the sweeps run the
+// reference's non-controlled loop (lib/include/detail/runge_kutta.hpp:37-72),
+// t_n = t_0 + n dt while (t_n + dt) - t_1 <= eps, every attempt accepted.
+// The error weights are zero and the controller constants unused.
+struct TabRK4 {
+    static constexpr int S = 4;
+    static constexpr bool FSAL = false;
+    static constexpr int ERROR_ORDER = 4;
+    static constexpr int STEPPER_ORDER = 4;
+    static constexpr double ERR_FLOOR = 1.0 / 625.0;
+    static constexpr bool FIXED = true;
+    __host__ __device__ static constexpr double a(int i, int j)
+    {
+        return i == 1 ? (j == 0 ? 1.0 / 2.0 : 0.0)
+             : i == 2 ? (j == 1 ? 1.0 / 2.0 : 0.0)
+             : i == 3 ? (j == 2 ? 1.0 : 0.0)
+             : 0.0;
+    }
+    __host__ __device__ static constexpr double b(int j)
+    {
+        return j == 0 ? 1.0 / 6.0 : j == 1 ? 1.0 / 3.0 : j == 2 ? 1.0 / 3.0 : j == 3 ? 1.0 / 6.0 : 0.0;
+    }
+    __host__ __device__ static constexpr double c(int j)
+    {
+        return j == 1 ? 1.0 / 2.0 : j == 2 ? 1.0 / 2.0 : j == 3 ? 1.0 : 0.0;
+    }
+    __host__ __device__ static constexpr double e(int) { return 0.0; }
+    static constexpr double E_NEW = 0.0;
+};
+
+struct TabEuler {
+    static constexpr int S = 1;
+    static constexpr bool FSAL = false;
+    static constexpr int ERROR_ORDER = 1;
+    static constexpr int STEPPER_ORDER = 1;
+    static constexpr double ERR_FLOOR = 1.0 / 5.0;
+    static constexpr bool FIXED = true;
+    __host__ __device__ static constexpr double a(int, int) { return 0.0; }
+    __host__ __device__ static constexpr double b(int j) { return j == 0 ? 1.0 : 0.0; }
+    __host__ __device__ static constexpr double c(int) { return 0.0; }
+    __host__ __device__ static constexpr double e(int) { return 0.0; }
+    static constexpr double E_NEW = 0.0;
+};
+
+// t_0 + n dt of the fixed-step loop, rounded twice as the reference computes
+// it (no fused multiply-add, whatever the translation unit contracts)
+__host__ __device__ __forceinline__ double fixed_time(double t0, int n, double dt)
+{
+#ifdef __CUDA_ARCH__
+    return __dadd_rn(t0, __dmul_rn((double)n, dt));
+#else
+    return t0 + (double)n * dt;
+#endif
+}
 
 } // namespace va
