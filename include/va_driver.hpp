@@ -42,6 +42,19 @@ template <class State> struct runge_kutta_dopri5 {
 template <class State> struct runge_kutta_cash_karp54 {
     static constexpr int32_t tableau = VA_TAB_CK54;
 };
+template <class State> struct runge_kutta_fehlberg78 {
+    static constexpr int32_t tableau = VA_TAB_RKF78;
+};
+// Fixed-step steppers, passed to runge_kutta directly (no make_controlled),
+// as odeint's runge_kutta4 / euler are; the tolerances are unused.
+template <class State> struct runge_kutta4 {
+    static constexpr int32_t tableau = VA_TAB_RK4;
+    double atol = 1e-6, rtol = 1e-6;
+};
+template <class State> struct euler {
+    static constexpr int32_t tableau = VA_TAB_EULER;
+    double atol = 1e-6, rtol = 1e-6;
+};
 template <class ErrorStepper> struct controlled_runge_kutta {
     double atol, rtol;
     static constexpr int32_t tableau = ErrorStepper::tableau;

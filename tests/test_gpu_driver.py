@@ -12,21 +12,22 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_cpp_driver_matches_oracle(oracle, cuda, tmp_path):
+@pytest.mark.parametrize("stepper,dt", [("dopri5", 1e-3), ("rkf78", 1e-3), ("rk4", 0.01), ("euler", 1e-3)])
+def test_cpp_driver_matches_oracle(oracle, cuda, tmp_path, stepper, dt):
     exe = str(tmp_path / "driver_example")
     lib_dir = os.path.join(ROOT, "vectorizedadjoint_gb300")
     subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "driver_example.cpp"), "-o", exe,
                     "-L", lib_dir, "-lva_gb300", f"-Wl,-rpath,{lib_dir}"], check=True)
     mu, x0, v0, t1, tol = 1.3, 1.5, -0.4, 8.0, 1e-8
-    out = subprocess.run([exe, str(mu), str(x0), str(v0), str(t1), str(tol)], capture_output=True,
-                         text=True, check=True).stdout.split("\n")
+    out = subprocess.run([exe, str(mu), str(x0), str(v0), str(t1), str(tol), stepper, str(dt)],
+                         capture_output=True, text=True, check=True).stdout.split("\n")
     vals = {}
     for line in out:
         if line.strip():
             k, *v = line.split()
             vals.setdefault(k, []).append([float(x) for x in v])
-    pb = oracle.problem("vdp", "dopri5", 2, 1, tol, tol)
+    pb = oracle.problem("vdp", stepper, 2, 1, tol, tol, dt0=dt)
     fw = oracle.forward(pb, [x0, v0], [mu], 0.0, t1)
     assert int(vals["steps"][0][0]) == fw["n_acc"]
     np.testing.assert_array_equal(vals["x"][0], fw["yT"])
