@@ -248,6 +248,29 @@ VA_API va_status va_checkpoint_info(const va_handle *h, int64_t *capacity_bytes,
 VA_API va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double *t,
                                double *dt, double *y, int32_t *n_records);
 
+/* Adjoint history -- the reference's back_prop observer
+ * (detail/backpropagation.hpp:230-254), which sees (lambda_n, t_n) after
+ * every back step, n = T .. 0.  capacity > 0: every later backward sweep
+ * (va_backward, va_gradient) also stores lambda_n of every seed for record
+ * indices n < capacity, in a device buffer the handle owns
+ * (batch * nout * capacity * n doubles, NaN where nothing was stored);
+ * 0 turns the history off and frees the buffer.  Any checkpoint stride.
+ * VA_BAD_ARGS for VA_MODEL_GLV_SHARED. */
+VA_API va_status va_set_adjoint_history(va_handle *h, int32_t capacity);
+
+/* Copies one instance's adjoint history to HOST buffers (synchronous):
+ * lambda[q][k][i] (row stride `capacity`) = lambda_k of seed q for
+ * k < min(capacity, history capacity, T + 1), and, when t is not NULL, the
+ * record times t[k] (as va_trajectory; checkpoint stride 1 only).
+ * *n_records = T + 1.  VA_NOT_READY before a backward sweep with the
+ * history on. */
+VA_API va_status va_adjoint_history(va_handle *h, int32_t instance, int32_t capacity, double *t,
+                                    double *lambda, int32_t *n_records);
+
+/* The history buffer on the device, layout [batch][nout][capacity][n], and
+ * its capacity (NULL, 0 when off). */
+VA_API va_status va_adjoint_history_buffer(const va_handle *h, double **buf, int32_t *capacity);
+
 /* Shared parameters of VA_MODEL_GLV_SHARED (n = 64 or 256, npar = n, nout = 1):
  * A[n][n] row-major (DEVICE, read by every later sweep) and dA[n][n] (DEVICE,
  * may be NULL), which each backward sweep overwrites with the gradient of

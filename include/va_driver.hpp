@@ -158,6 +158,28 @@ size_t runge_kutta(Stepper stepper, System system, State &start_state, const Sta
     return (size_t)nacc;
 }
 
+// With observer (runge_kutta.hpp:16-29): observer(state, t) for every
+// record (t_n, y_n), n = 0 .. T, in order, as the reference's loop calls it
+// (detail/runge_kutta.hpp:94,113); here replayed from the checkpoint record
+// after the sweep.
+template <class Stepper, class System, class State, class Time, class Observer>
+size_t runge_kutta(Stepper stepper, System system, State &start_state, const State &alphas,
+                   Time start_time, const Time end_time, Time dt, Driver &driver, Observer observer)
+{
+    const size_t steps = runge_kutta(stepper, system, start_state, alphas, start_time, end_time, dt, driver);
+    va_handle *h = driver.handle();
+    const int n = driver.GetNin(), nrec = driver.GetT();
+    std::vector<double> t(nrec), y((size_t)nrec * n);
+    int32_t got = 0;
+    if (va_trajectory(h, 0, nrec, t.data(), nullptr, y.data(), &got) != VA_OK)
+        throw std::runtime_error(std::string("runge_kutta: ") + va_last_error(h));
+    for (int k = 0; k < nrec; k++) {
+        State x(y.begin() + (size_t)k * n, y.begin() + (size_t)(k + 1) * n);
+        observer(x, (Time)t[k]);
+    }
+    return steps;
+}
+
 inline void setCostGradients(Driver &driver, std::vector<std::vector<double>> &lambda,
                              std::vector<std::vector<double>> &mu)
 {
@@ -203,6 +225,35 @@ template <class State> void adjointSolve(Driver &driver, const State &parameters
     } catch (std::exception &e) {
         std::cout << e.what() << std::endl;
     }
+}
+
+// adjointSolve with the back_prop observer of detail/backpropagation.hpp:
+// 230-254 exposed: observer(lambda_n, t_n) with lambda_n = [Nout][Nin] after
+// every back step, n = T .. 0 (the reference passes null_observer there).
+template <class State, class Observer>
+void adjointSolve(Driver &driver, const State &parameters, Observer observer)
+{
+    va_handle *h = driver.handle();
+    const int nin = driver.GetNin(), nout = driver.GetNout(), nrec = driver.GetT();
+    if (!h || driver.m_T < 0 || va_set_adjoint_history(h, nrec) != VA_OK) {
+        std::cout << "Must call runge_kutta() first!" << std::endl;
+        return;
+    }
+    adjointSolve(driver, parameters);
+    std::vector<double> t(nrec), lam((size_t)nout * nrec * nin);
+    int32_t got = 0;
+    if (va_adjoint_history(h, 0, nrec, t.data(), lam.data(), &got) == VA_OK) {
+        std::vector<std::vector<double>> rows(nout, std::vector<double>(nin));
+        for (int k = nrec - 1; k >= 0; k--) {
+            for (int q = 0; q < nout; q++)
+                for (int i = 0; i < nin; i++)
+                    rows[q][i] = lam[((size_t)q * nrec + k) * nin + i];
+            observer(rows, t[k]);
+        }
+    } else {
+        std::cout << "adjointSolve: " << va_last_error(h) << std::endl;
+    }
+    va_set_adjoint_history(h, 0);
 }
 
 // d x_i(T) / d alpha_k (Nin x Npar), identity seeds (backpropagation.hpp:69-87).

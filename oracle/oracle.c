@@ -683,6 +683,12 @@ static void back_prop_step(const orc_problem *pb, const tableau *T, const double
 int orc_adjoint(const orc_problem *pb, const double *p, long T, const double *times,
                 const double *states, int nout, double *lambda, double *mu)
 {
+    return orc_adjoint_history(pb, p, T, times, states, nout, lambda, mu, NULL);
+}
+
+int orc_adjoint_history(const orc_problem *pb, const double *p, long T, const double *times,
+                        const double *states, int nout, double *lambda, double *mu, double *hist)
+{
     tableau tab;
     if (get_tableau(pb->tableau, &tab) != 0 || pb->n < 1 || pb->n > NMAX || nout < 1)
         return ORC_BAD_ARGS;
@@ -697,12 +703,18 @@ int orc_adjoint(const orc_problem *pb, const double *p, long T, const double *ti
         double *lam = lambda + (size_t)q * n;
         for (int k = 0; k < np; k++)
             alphabar[k] = 0.0;
-        /* back_prop (:256-278): n = T-1 .. 0 */
+        /* back_prop (:256-278): n = T-1 .. 0; its observer sees lambda_T,
+         * then lambda_n after each step (:268, :274) */
+        double *hq = hist ? hist + (size_t)q * (T + 1) * n : NULL;
+        if (hq)
+            memcpy(hq + (size_t)T * n, lam, sizeof(double) * n);
         for (long k = T - 1; k >= 0; k--) {
             double tn = times[k];
             double h = times[k + 1] - times[k];
             back_prop_step(pb, &tab, p, tn, h, states + (size_t)k * n, lam, alphabar, K, X, Kbar,
                            ybar, gx, gp);
+            if (hq)
+                memcpy(hq + (size_t)k * n, lam, sizeof(double) * n);
         }
         /* write-back (:317-321): mu += alphabar */
         for (int k = 0; k < np; k++)

@@ -102,6 +102,12 @@ void orc_forward_frozen(const orc_problem *pb, const double *y0, const double *p
 int orc_adjoint(const orc_problem *pb, const double *p, long T, const double *times,
                 const double *states, int nout, double *lambda, double *mu);
 
+/* orc_adjoint that also stores lambda_n of every seed, n = 0 .. T, in
+ * hist[nout][T+1][n] (the values back_prop's observer sees,
+ * detail/backpropagation.hpp:256-278); hist may be NULL. */
+int orc_adjoint_history(const orc_problem *pb, const double *p, long T, const double *times,
+                        const double *states, int nout, double *lambda, double *mu, double *hist);
+
 /* One gradient (forward + adjoint) for a built-in scalar cost. */
 int orc_gradient(const orc_problem *pb, int cost, const double *y0, const double *p, double t0,
                  double t1, double *yT, double *dy0, double *dp, long *n_acc, long *n_rej);

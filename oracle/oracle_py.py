@@ -62,6 +62,8 @@ def lib():
         L.orc_forward_frozen.restype = None
         L.orc_adjoint.argtypes = [P, dp, ctypes.c_long, dp, dp, ctypes.c_int, dp, dp]
         L.orc_adjoint.restype = ctypes.c_int
+        L.orc_adjoint_history.argtypes = [P, dp, ctypes.c_long, dp, dp, ctypes.c_int, dp, dp, dp]
+        L.orc_adjoint_history.restype = ctypes.c_int
         L.orc_gradient.argtypes = [P, ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double,
                                    dp, dp, dp, lp, lp]
         L.orc_gradient.restype = ctypes.c_int
@@ -121,6 +123,19 @@ def adjoint(pb, p, times, states, lam, mu):
     st = lib().orc_adjoint(ctypes.byref(pb), _d(p), len(times) - 1, _d(times), _d(states),
                            lam.shape[0], _d(lam), _d(mu))
     return lam, mu, st
+
+
+def adjoint_history(pb, p, times, states, lam, mu):
+    """adjoint() plus lambda_n of every seed: returns (dy0, dp, hist[nout, T+1, n], status)."""
+    lam = np.array(lam, dtype=np.float64, order="C", ndmin=2).copy()
+    mu = np.array(mu, dtype=np.float64, order="C", ndmin=2).copy()
+    times = np.ascontiguousarray(times, dtype=np.float64)
+    states = np.ascontiguousarray(states, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    hist = np.zeros((lam.shape[0], len(times), pb.n))
+    st = lib().orc_adjoint_history(ctypes.byref(pb), _d(p), len(times) - 1, _d(times), _d(states),
+                                   lam.shape[0], _d(lam), _d(mu), _d(hist))
+    return lam, mu, hist, st
 
 
 def gradient(pb, cost, y0, p, t0, t1):

@@ -130,6 +130,56 @@ static int run(System sys, int n, int nout, int npar, double atol, double rtol, 
     return 0;
 }
 
+// The reference's SIMD back_prop (detail/backpropagation.hpp:230-254) with
+// an observer that records what it is shown: (wbarend, t_n) for n = T .. 0,
+// the seeds of up to four costs in the lanes (as adjointSolve packs them).
+// hist[q][n][i] = lambda_n of seed q; times[n] = t_n.
+template <class Stepper, class System>
+static int run_history(System sys, int n, int nout, int npar, double atol, double rtol, double dt0,
+                       const double *y0, const double *p, double t0, double t1, const double *lam_in, long cap,
+                       double *times, double *hist, long *T)
+{
+    using namespace vectorizedadjoint;
+    const int lanes = (int)(sizeof(mmType) / sizeof(double));
+    if (nout < 1 || nout > lanes)
+        return 3;
+    Driver driver(n, nout, npar);
+    State x0(y0, y0 + n), alphas(p, p + npar);
+    size_t steps = 0;
+    try {
+        if constexpr (std::is_same<typename Stepper::stepper_category, odeint::stepper_tag>::value)
+            steps = runge_kutta(Stepper(), sys, x0, alphas, t0, t1, dt0, driver);
+        else
+            steps = runge_kutta(odeint::make_controlled<Stepper>(atol, rtol), sys, x0, alphas, t0, t1, dt0, driver);
+    } catch (std::exception &e) {
+        std::cerr << "runge_kutta: " << e.what() << std::endl;
+        return 1;
+    }
+    *T = (long)steps;
+    if ((long)steps + 1 > cap)
+        return 4;
+    std::vector<std::vector<double>> lambda(nout, std::vector<double>(n)), mu(nout, std::vector<double>(npar, 0.0));
+    setCostGradients(driver, lambda, mu);
+    constructDriverButcherTableau(driver, Stepper());
+    recordDriverRHSFunction(driver, sys);
+    aadc::mmVector<mmType> wbarend(n);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < lanes; j++)
+            wbarend[i][j] = j < nout ? lam_in[(size_t)j * n + i] : 0.0;
+    long k = (long)steps;
+    auto observer = [&](const aadc::mmVector<mmType> &w, double t) {
+        if (k < 0)
+            return;
+        times[k] = t;
+        for (int q = 0; q < nout; q++)
+            for (int i = 0; i < n; i++)
+                hist[((size_t)q * (steps + 1) + k) * n + i] = w[i][q];
+        k--;
+    };
+    detail::back_prop(driver, wbarend, alphas, observer);
+    return k == -1 ? 0 : 5;
+}
+
 // model: 0 VdP (Lienard), 1 VdP (reference example form), 2 damped
 // oscillator, 3 GLV; tableau: 0 DOPRI5, 1 Cash-Karp, 2 Fehlberg 7(8) (the
 // reference's own ButcherTable branch), 3 fixed-step RK4, 4 fixed-step Euler
@@ -146,6 +196,35 @@ extern "C" int ref_solve(int model, int tableau, int n, int nout, int npar, doub
      : tableau == 2 ? run<Fehlberg78>(SYS(), VA_ARGS)                                              \
      : tableau == 3 ? run<RK4>(SYS(), VA_ARGS)                                                     \
                     : run<Euler>(SYS(), VA_ARGS))
+    switch (model) {
+    case 0:
+        return VA_RUN(VanDerPol);
+    case 1:
+        return VA_RUN(VanDerPolPETSc);
+    case 2:
+        return VA_RUN(DampedOscillator);
+    case 3:
+        return VA_RUN(LotkaVolterra);
+    default:
+        return 2;
+    }
+#undef VA_RUN
+#undef VA_ARGS
+}
+
+// back_prop's observer record of one instance (run_history); same model and
+// tableau codes as ref_solve.  hist: [nout][T+1][n], nout <= 4.
+extern "C" int ref_history(int model, int tableau, int n, int nout, int npar, double atol, double rtol, double dt0,
+                           const double *y0, const double *p, double t0, double t1, const double *lam_in, long cap,
+                           double *times, double *hist, long *T)
+{
+#define VA_ARGS n, nout, npar, atol, rtol, dt0, y0, p, t0, t1, lam_in, cap, times, hist, T
+#define VA_RUN(SYS)                                                                                \
+    (tableau == 0   ? run_history<Dopri5>(SYS(), VA_ARGS)                                          \
+     : tableau == 1 ? run_history<CashKarp>(SYS(), VA_ARGS)                                        \
+     : tableau == 2 ? run_history<Fehlberg78>(SYS(), VA_ARGS)                                      \
+     : tableau == 3 ? run_history<RK4>(SYS(), VA_ARGS)                                             \
+                    : run_history<Euler>(SYS(), VA_ARGS))
     switch (model) {
     case 0:
         return VA_RUN(VanDerPol);

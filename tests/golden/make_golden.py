@@ -11,6 +11,10 @@ vectorizedadjoint_gb300.workloads), and the reference's own GLV example
 [0, 10], dt = 1e-3, identity seeds Nout = N) on its data files
 data/N5/alphasfile_cpp.csv and data/N10/alphasfile_cpp.csv.
 
+A second file, history_cases.npz, holds adjoint histories: the values the
+reference's back_prop observer is shown (lambda_n after every back step)
+for three instances.
+
 Usage:  make -C oracle/ref && python tests/golden/make_golden.py
 """
 import ctypes
@@ -32,6 +36,7 @@ TABLEAU_ID = {"dopri5": 0, "ck54": 1, "rkf78": 2, "rk4": 3, "euler": 4}
 def load():
     L = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libvaref.so"))
     L.ref_solve.restype = ctypes.c_int
+    L.ref_history.restype = ctypes.c_int
     return L
 
 
@@ -53,6 +58,52 @@ def solve(L, model, tableau, n, npar, tol, y0, p, t1, lam, mu, cap=200000, dt=1e
                      mo.ctypes.data_as(ctypes.c_void_p))
     assert rc == 0, rc
     return T.value, times[:T.value + 1], states[:T.value + 1], yT, lo, mo
+
+
+def history(L, model, tableau, n, npar, tol, y0, p, t1, lam, dt=1e-3, cap=200000):
+    """The reference's back_prop observer record: (times[T+1], hist[nout][T+1][n])."""
+    nout = lam.shape[0]
+    times = np.zeros(cap)
+    hist = np.zeros(nout * cap * n)
+    T = ctypes.c_long()
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (y0, p, lam)]
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    rc = L.ref_history(MODEL_ID[model], TABLEAU_ID[tableau], n, nout, npar, ctypes.c_double(tol),
+                       ctypes.c_double(tol), ctypes.c_double(dt), ptr(keep[0]), ptr(keep[1]), ctypes.c_double(0.0),
+                       ctypes.c_double(t1), ptr(keep[2]), ctypes.c_long(cap), ptr(times), ptr(hist), ctypes.byref(T))
+    assert rc == 0, rc
+    k = T.value + 1
+    return times[:k], hist[:nout * k * n].reshape(nout, k, n)
+
+
+def main_history(L):
+    """Adjoint histories (lambda_n after every back step, the values the
+    reference's back_prop observer sees) -> tests/golden/history_cases.npz."""
+    out = {}
+    specs = [("vdp1", None, 1e-3, "eye"), ("vdpb", "rk4", 1e-2, "cost"), ("glv10", "ck54", 1e-3, "rand3")]
+    for k, (name, tableau, dt, seeds) in enumerate(specs):
+        w = W.make(name, batch=1)
+        c = w["cfg"]
+        tab = tableau or c["tableau"]
+        y0, p, t1 = w["y0"][0], w["params"][0], float(w["t1"][0])
+        n = c["n"]
+        if seeds == "eye":
+            lam = np.eye(n)
+        elif seeds == "cost":
+            _, _, _, yT, _, _ = solve(L, c["model"], tab, n, c["npar"], c["tol"], y0, p, t1, np.zeros((1, n)),
+                                      np.zeros((1, c["npar"])), dt=dt)
+            lam = 2.0 * yT[None, :]
+        else:
+            lam = np.random.Generator(np.random.PCG64(11)).standard_normal((3, n))
+        times, hist = history(L, c["model"], tab, n, c["npar"], c["tol"], y0, p, t1, lam, dt=dt)
+        case = dict(name=f"{name}_{tab}", model=c["model"], tableau=tab, n=n, npar=c["npar"], tol=c["tol"], dt=dt,
+                    y0=y0, p=p, t1=t1, lam=lam, times=times, hist=hist)
+        for key, v in case.items():
+            out[f"c{k}_{key}"] = np.asarray(v)
+    out["count"] = np.array(len(specs))
+    path = os.path.join(ROOT, "tests", "golden", "history_cases.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {len(specs)} history cases to {path} ({os.path.getsize(path)} bytes)")
 
 
 def main():
@@ -105,6 +156,7 @@ def main():
     path = os.path.join(ROOT, "tests", "golden", "reference_cases.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {len(cases)} cases to {path} ({os.path.getsize(path)} bytes)")
+    main_history(L)
 
 
 if __name__ == "__main__":

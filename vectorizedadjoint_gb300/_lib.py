@@ -24,7 +24,8 @@ EXPORTS = ["va_default_options", "va_create", "va_destroy", "va_forward", "va_ba
            "va_gradient", "va_gradient_host", "va_forward_host", "va_backward_host", "va_gradient_noalloc",
            "va_autotune",
            "va_get_launch", "va_checkpoint_info",
-           "va_trajectory", "va_set_shared", "va_last_error", "va_status_string"]
+           "va_trajectory", "va_set_adjoint_history", "va_adjoint_history", "va_adjoint_history_buffer",
+           "va_set_shared", "va_last_error", "va_status_string"]
 
 
 class VaProblem(ctypes.Structure):
@@ -80,6 +81,9 @@ def load():
     L.va_checkpoint_info.argtypes = [H, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                      ctypes.POINTER(ctypes.c_int32)]
     L.va_trajectory.argtypes = [H, ctypes.c_int32, ctypes.c_int32, dp, dp, dp, ctypes.POINTER(ctypes.c_int32)]
+    L.va_set_adjoint_history.argtypes = [H, ctypes.c_int32]
+    L.va_adjoint_history.argtypes = [H, ctypes.c_int32, ctypes.c_int32, dp, dp, ctypes.POINTER(ctypes.c_int32)]
+    L.va_adjoint_history_buffer.argtypes = [H, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int32)]
     L.va_set_shared.argtypes = [H, dp, dp]
     L.va_last_error.argtypes = [H]
     L.va_last_error.restype = ctypes.c_char_p

@@ -81,6 +81,10 @@ struct va_handle {
     int stride = 1;
     double *inst_t1 = nullptr;
     double *inst_t0 = nullptr; // start times (fixed-step two-level backward)
+    // adjoint history (va_set_adjoint_history): [batch][nout][hist_cap][N]
+    double *hist = nullptr;
+    int hist_cap = 0;
+    bool hist_done = false; // a backward sweep has been enqueued with the history on
     double *scratch = nullptr;
     size_t scratch_doubles = 0;
 
@@ -413,6 +417,10 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
         h->bwd_block = h->N;
         return VA_OK;
     }
+    a.hist = h->hist;
+    a.hist_cap = h->hist_cap;
+    if (h->hist)
+        h->hist_done = true;
     if (h->stride > 1) {
         if (h->scratch_doubles <
             (size_t)two_level_grid(h) * kTwoLevelBlock * (h->stride + 1) * scratch_record_doubles(h))
@@ -581,7 +589,7 @@ va_status va_destroy(va_handle *h)
                     h->s_yT,     h->s_dy0,      h->s_dpar,  h->s_nacc,    h->s_status,
                     h->s_nrej,   h->s_lam,      h->s_mu,    h->At,        h->Aw,
                     h->Atw,      h->dA_part,    h->inst_t1, h->scratch, h->order_fwd,
-                    h->order_bwd, h->order_work, h->inst_work, h->inst_t0};
+                    h->order_bwd, h->order_work, h->inst_work, h->inst_t0, h->hist};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -894,6 +902,74 @@ va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double
         chunk = prev;
         first_in_chunk -= CH;
     }
+    return VA_OK;
+}
+
+va_status va_set_adjoint_history(va_handle *h, int32_t capacity)
+{
+    if (!h || capacity < 0)
+        return VA_BAD_ARGS;
+    if (capacity > 0 && h->bks)
+        return fail(h, VA_BAD_ARGS, "va_set_adjoint_history: not available for the shared-matrix model%s");
+    drop_graph(h); // captured sweeps hold the old buffer
+    if (h->hist) {
+        VA_CUDA(h, cudaDeviceSynchronize());
+        VA_CUDA(h, cudaFree(h->hist));
+        h->hist = nullptr;
+    }
+    h->hist_cap = 0;
+    h->hist_done = false;
+    if (capacity == 0)
+        return VA_OK;
+    const size_t n = (size_t)h->prob.batch * h->prob.nout * capacity * h->N;
+    VA_CUDA(h, cudaMalloc(&h->hist, n * sizeof(double)));
+    // all-ones bytes: a NaN in every slot no sweep writes
+    VA_CUDA(h, cudaMemset(h->hist, 0xff, n * sizeof(double)));
+    h->hist_cap = capacity;
+    return VA_OK;
+}
+
+va_status va_adjoint_history(va_handle *h, int32_t instance, int32_t capacity, double *t, double *lambda,
+                             int32_t *n_records)
+{
+    if (!h || instance < 0 || instance >= h->prob.batch || capacity < 0)
+        return VA_BAD_ARGS;
+    if (!h->hist)
+        return fail(h, VA_NOT_READY, "va_adjoint_history: call va_set_adjoint_history first%s");
+    if (!h->hist_done)
+        return fail(h, VA_NOT_READY, "va_adjoint_history: no backward sweep has run with the history on%s");
+    int32_t nrec = 0;
+    if (t) { // the record times, as va_trajectory reads them (stride 1)
+        const va_status st = va_trajectory(h, instance, capacity, t, nullptr, nullptr, &nrec);
+        if (st != VA_OK)
+            return st;
+    } else {
+        VA_CUDA(h, cudaDeviceSynchronize());
+        int T = 0;
+        VA_CUDA(h, cudaMemcpy(&T, h->inst_T + instance, sizeof(int), cudaMemcpyDeviceToHost));
+        nrec = T + 1;
+    }
+    if (n_records)
+        *n_records = nrec;
+    const int N = h->N, Q = h->prob.nout;
+    const int k = std::min(std::min(capacity, h->hist_cap), nrec);
+    if (lambda && k > 0) {
+        for (int q = 0; q < Q; q++)
+            VA_CUDA(h, cudaMemcpy(lambda + (size_t)q * capacity * N,
+                                  h->hist + (((size_t)instance * Q + q) * h->hist_cap) * N,
+                                  (size_t)k * N * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    return VA_OK;
+}
+
+va_status va_adjoint_history_buffer(const va_handle *h, double **buf, int32_t *capacity)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    if (buf)
+        *buf = h->hist;
+    if (capacity)
+        *capacity = h->hist_cap;
     return VA_OK;
 }
 

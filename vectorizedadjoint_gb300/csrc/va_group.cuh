@@ -334,6 +334,7 @@ __global__ void __launch_bounds__(256) backward_group_kernel(AdjParams a)
 #pragma unroll
         for (int k = 0; k < PG; k++)
             mu[k] = 0.0;
+        note_lambda_lane(a, b, q, T, NT, li, lam[0]);
         j = T - 1;
     };
 
@@ -404,6 +405,7 @@ __global__ void __launch_bounds__(256) backward_group_kernel(AdjParams a)
         double y[1] = {r[2 + li]};
         const double h = t_next - tn;
         back_step<M, Tab, S>(y, tn, h, p, lam, mu);
+        note_lambda_lane(a, b, q, j, NT, li, lam[0]);
         t_next = tn;
         j--;
     }

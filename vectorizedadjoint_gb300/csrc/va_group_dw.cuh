@@ -340,6 +340,7 @@ __global__ void __launch_bounds__(256) backward_group_dw_kernel(AdjParams a)
 #pragma unroll
         for (int k = 0; k < PG; k++)
             dm[k] = dacc{0.0f, 0.0f};
+        note_lambda_lane(a, b, q, T, NN, li, lam);
         j = T - 1;
         if (j >= 0)
             step_back_load();
@@ -440,6 +441,7 @@ __global__ void __launch_bounds__(256) backward_group_dw_kernel(AdjParams a)
 #pragma unroll
         for (int k = 0; k < PG; k++)
             dm[k] = dacc_of(dacc_get(dm[k]));
+        note_lambda_lane(a, b, q, j, NN, li, lam);
         t_next = tn;
         j--;
     }

@@ -118,6 +118,10 @@ struct AdjParams {
     double atol, rtol;
     double dt0;              // the step of the fixed-step tableaux
     int max_fail;
+    // adjoint history (may be null): lambda_n of seed q at
+    // hist[((b * nout + q) * hist_cap + n) * N + i] for record n < hist_cap
+    double *hist;
+    int hist_cap;
 };
 
 __host__ __device__ constexpr int record_doubles(int n) { return (2 + n + 1) & ~1; }
@@ -131,6 +135,29 @@ __host__ __device__ __forceinline__ S from_d(double v)
 __host__ __device__ __forceinline__ double to_d(double v) { return v; }
 __host__ __device__ __forceinline__ double to_d(float v) { return (double)v; }
 __host__ __device__ __forceinline__ double to_d(dword v) { return (double)v; }
+
+// The reference's back_prop observer (detail/backpropagation.hpp:243,250)
+// sees (lambda_n, t_n) after every back step, n = T .. 0; the sweeps store
+// lambda_n instead, at its record index (t_n is the forward's record).
+template <int N, class V>
+__device__ __forceinline__ void note_lambda(const AdjParams &a, int b, int q, int n, const V (&lam)[N])
+{
+    if (a.hist && n < a.hist_cap) {
+        double *d = a.hist + (((size_t)b * a.nout + q) * a.hist_cap + n) * N;
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            d[i] = to_d(lam[i]);
+    }
+}
+
+// the same for lane i of a lane group (component i of an NT-state)
+template <class V>
+__device__ __forceinline__ void note_lambda_lane(const AdjParams &a, int b, int q, int n, int NT, int li, V lam)
+{
+    if (a.hist && n < a.hist_cap)
+        a.hist[(((size_t)b * a.nout + q) * a.hist_cap + n) * NT + li] = to_d(lam);
+}
+
 // a * b + c (for double: fused only where the translation unit contracts;
 // the FP64 kernels are built without contraction)
 __host__ __device__ __forceinline__ double madd(double a, double b, double c) { return a * b + c; }
@@ -898,6 +925,7 @@ __global__ void __launch_bounds__(256) backward_kernel(AdjParams a)
 #pragma unroll
         for (int k = 0; k < P; k++)
             mu[k] = 0.0;
+        note_lambda<N>(a, b, q, T, lam);
         j = T - 1;
     };
 
@@ -975,6 +1003,7 @@ __global__ void __launch_bounds__(256) backward_kernel(AdjParams a)
         read_record<N>(record_ptr<RS>(a.pool, chunk, slot), tn, y);
         const double h = t_next - tn;
         back_step<M, Tab, S>(y, tn, h, p, lam, mu);
+        note_lambda<N>(a, b, q, j, lam);
         t_next = tn;
         j--;
     }
@@ -1068,6 +1097,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level(AdjParams a)
 #pragma unroll
         for (int kk = 0; kk < P; kk++)
             mu[kk] = 0.0;
+        note_lambda<N>(a, b, q, T, lam);
         k = R - 2;
         if (k >= 0)
             begin_segment();
@@ -1190,6 +1220,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level(AdjParams a)
             const double tn = r[0];
             const double h = scr[(size_t)(jb + 1) * RS] - tn;
             back_step<M, Tab, S>(yj, tn, h, p, lam, mu);
+            note_lambda<N>(a, b, q, first + jb, lam);
             jb--;
             if (jb < 0) {
                 // the segment's start becomes the next segment's end

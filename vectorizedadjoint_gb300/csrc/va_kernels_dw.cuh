@@ -697,6 +697,7 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
 #pragma unroll
         for (int k = 0; k < P; k++)
             mu[k] = dword(0.0f, 0.0f);
+        note_lambda<N>(a, b, q, T, lam);
         j = T - 1;
         if (j >= 0)
             step_back_load();
@@ -760,6 +761,7 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
                 y[i] = dw_unpack(cv[2 + i]);
             back_step_dw<M, Tab>(y, dword(tn), dword(t_next - tn), p, lam, mu);
         }
+        note_lambda<N>(a, b, q, j, lam);
         t_next = tn;
         j--;
     }
@@ -828,6 +830,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
 #pragma unroll
         for (int kk = 0; kk < P; kk++)
             mu[kk] = dword(0.0f, 0.0f);
+        note_lambda<N>(a, b, q, T, lam);
         k = R - 2;
         if (k >= 0)
             begin_segment();
@@ -936,6 +939,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
             read_stage_record_dw<N, NS>(scr + (size_t)jb * RX, tn, X);
             tn1 = scr[(size_t)(jb + 1) * RX];
             back_step_dw_x<M, Tab>(X, dword(tn), dword(tn1 - tn), p, lam, mu);
+            note_lambda<N>(a, b, q, first + jb, lam);
             jb--;
             if (jb < 0) {
                 // the segment's start becomes the next segment's end

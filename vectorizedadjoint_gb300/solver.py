@@ -154,6 +154,29 @@ class Solver:
                                          ctypes.byref(nrec)), "va_trajectory")
         return t[:nrec.value], dt[:nrec.value], y[:nrec.value]
 
+    def set_adjoint_history(self, capacity):
+        """Keep lambda_n (every seed, record indices n < capacity) in later
+        backward sweeps -- the reference's back_prop observer; 0 turns it off."""
+        self._check(self.L.va_set_adjoint_history(self.h, capacity), "va_set_adjoint_history")
+        self._hist_cap = capacity
+
+    def adjoint_history(self, instance, capacity=None, times=True):
+        """(t[k], lambda[nout, k, n]) for k = 0..T of one instance (t is None
+        when times=False, e.g. with a checkpoint stride > 1)."""
+        import numpy as np
+        nrec = ctypes.c_int32()
+        self._check(self.L.va_adjoint_history(self.h, instance, 0, None, None, ctypes.byref(nrec)),
+                    "va_adjoint_history")
+        cap = nrec.value if capacity is None else capacity
+        t = np.zeros(cap) if times else None
+        lam = np.zeros((self.nout, cap, self.n))
+        self._check(self.L.va_adjoint_history(self.h, instance, cap,
+                                              ctypes.c_void_p(t.ctypes.data) if times else None,
+                                              ctypes.c_void_p(lam.ctypes.data), ctypes.byref(nrec)),
+                    "va_adjoint_history")
+        k = min(cap, nrec.value, getattr(self, "_hist_cap", 0))
+        return (t[:k] if times else None), lam[:, :k]
+
     def checkpoint_info(self):
         cap, used, stride = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()
         self.L.va_checkpoint_info(self.h, ctypes.byref(cap), ctypes.byref(used), ctypes.byref(stride))
