@@ -61,7 +61,7 @@ def flops(model, tableau, n, attempts, accepted):
 # Double-word arithmetic is FADD-heavy (2Sum chains), so its FLOP ceiling
 # sits near half the FFMA peak.
 DW_FP32_FLOPS = {
-    ("vdp", "dopri5"): (1562.9, 1644.8),
+    ("vdp", "dopri5"): (1574.8, 1686.2),
     ("dho", "ck54"): (1357.5, 1566.8),
 }
 
@@ -219,7 +219,7 @@ def gemm_tflops(torch, dtype, n):
 # DRAM bytes per launch of the one-thread double-word kernels on the Van der
 # Pol batch (262,144 instances), one ncu capture each: the forward writes the
 # stage records (112 B per accepted step), the backward reads them back.
-DW_TRAFFIC = {("vdpb", "forward"): 453.99e6 + 5110.17e6, ("vdpb", "backward"): 4894.20e6 + 11.09e6}
+DW_TRAFFIC = {("vdpb", "forward"): 108.0e6 + 5555.8e6, ("vdpb", "backward"): 5656.3e6 + 22.5e6}
 
 
 def roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted):

@@ -1015,11 +1015,13 @@ va_status va_autotune(va_handle *h, int32_t cost, const double *y0, const double
         int occf = 0, occb = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occf, ffn, blk, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occb, bfn, blk, 0);
+        // every resident-block count: the best differs between the sweeps and
+        // between workloads (stage-record traffic favours fewer warps in the
+        // backward, issue rate more in the forward)
         int maxocc = std::max(1, std::max(occf, occb));
         std::vector<int> cands;
-        for (int c = 1; c < maxocc; c *= 2)
+        for (int c = 1; c <= maxocc; c++)
             cands.push_back(c);
-        cands.push_back(maxocc);
         for (int bps : cands) {
             h->fwd_block = h->bwd_block = blk;
             long need = ((long)h->prob.batch * h->ks->tpi + blk - 1) / blk;

@@ -40,9 +40,20 @@
 
 namespace va {
 
-// doubles per stage record: t, dt, X_0 = y, X_1 .. X_{s-1}; even, so every
-// record (and every 2-state group in it) starts on a 16-byte boundary
-__host__ __device__ constexpr int stage_record_doubles(int n, int s) { return (2 + n * s + 1) & ~1; }
+// doubles per stage record: t, dt, X_0 = y, X_1 .. X_{s-1}, padded to a
+// multiple of four: every record starts on a 32-byte boundary and is moved
+// with whole-sector (256-bit) loads and stores
+__host__ __device__ constexpr int stage_record_doubles(int n, int s) { return (2 + n * s + 3) & ~3; }
+
+// 256-bit global store / streaming load of four doubles (p 32-byte aligned)
+__device__ __forceinline__ void st_v4(double *p, double a, double b, double c, double d)
+{
+    asm volatile("st.global.v4.f64 [%0], {%1, %2, %3, %4};" ::"l"(p), "d"(a), "d"(b), "d"(c), "d"(d) : "memory");
+}
+__device__ __forceinline__ void ld_v4_cs(const double *p, double &a, double &b, double &c, double &d)
+{
+    asm volatile("ld.global.cs.v4.f64 {%0, %1, %2, %3}, [%4];" : "=d"(a), "=d"(b), "=d"(c), "=d"(d) : "l"(p));
+}
 
 struct DwTol {
     dword atol, rtol;
@@ -220,12 +231,12 @@ __host__ __device__ __forceinline__ void store_dw(double *r, const dword (&X)[N]
 // f(y_new) (FSAL pairs) and the error norm
 //   max_i |dt e_i| / (atol + rtol (|y_i| + |dt| |k0_i|))
 // (odeint's default_error_checker with a_x = a_dxdt = 1), NaN if any ratio is.
-// xrec (may be null): where the stage values X_1 .. X_{s-1} go, N each.
-template <class M, class Tab>
-__host__ __device__ __forceinline__ dword attempt_dw(const dword (&y)[M::N], const dword (&k0)[M::N],
-                                                     const dword (&p)[M::P], dword t, dword dt,
-                                                     const DwTol &tol, dword (&ynew)[M::N],
-                                                     dword (&knew)[M::N], double *xrec = nullptr)
+// sink(m, X_m) sees the stage values X_1 .. X_{s-1} as they are formed.
+template <class M, class Tab, class Sink>
+__host__ __device__ __forceinline__ dword attempt_dw_sink(const dword (&y)[M::N], const dword (&k0)[M::N],
+                                                          const dword (&p)[M::P], dword t, dword dt,
+                                                          const DwTol &tol, dword (&ynew)[M::N],
+                                                          dword (&knew)[M::N], Sink &&sink)
 {
     constexpr int N = M::N, NS = Tab::S;
     dword K[NS][N];
@@ -236,8 +247,7 @@ __host__ __device__ __forceinline__ dword attempt_dw(const dword (&y)[M::N], con
     for (int m = 1; m < NS; m++) {
         dword X[N];
         stage_dw<Tab, N>(m, y, K, dt, X);
-        if (xrec)
-            store_dw<N>(xrec + (m - 1) * N, X);
+        sink(m, X);
         M::template rhs<dword>(X, p, t + dt * dword(Tab::c(m)), K[m]);
     }
 #pragma unroll
@@ -266,6 +276,19 @@ __host__ __device__ __forceinline__ dword attempt_dw(const dword (&y)[M::N], con
             worst = r;
     }
     return nan ? dw_nan() : worst;
+}
+
+// attempt_dw_sink with the stage values stored at xrec (N each; may be null)
+template <class M, class Tab>
+__host__ __device__ __forceinline__ dword attempt_dw(const dword (&y)[M::N], const dword (&k0)[M::N],
+                                                     const dword (&p)[M::P], dword t, dword dt,
+                                                     const DwTol &tol, dword (&ynew)[M::N],
+                                                     dword (&knew)[M::N], double *xrec = nullptr)
+{
+    return attempt_dw_sink<M, Tab>(y, k0, p, t, dt, tol, ynew, knew, [&](int m, const dword (&X)[M::N]) {
+        if (xrec)
+            store_dw<M::N>(xrec + (m - 1) * M::N, X);
+    });
 }
 
 // ----------------------------------------------------------------- records
@@ -326,6 +349,31 @@ __device__ __forceinline__ void read_stage_record_dw(const double *r, double &t,
             X[m][i] = dw_unpack(v[2 + m * N + i]);
 }
 
+// a whole stage record [t, dt, y, X_1 .. X_{S-1}], in 256-bit stores
+template <int N, int S>
+__device__ __forceinline__ void write_stage_record_dw(double *r, double t, dword dt, const dword (&y)[N],
+                                                      const dword (&X)[S > 1 ? S - 1 : 1][N])
+{
+    constexpr int RS = stage_record_doubles(N, S);
+    double v[RS];
+    v[0] = t;
+    v[1] = dw_pack(dt);
+#pragma unroll
+    for (int i = 0; i < N; i++)
+        v[2 + i] = dw_pack(y[i]);
+#pragma unroll
+    for (int m = 0; m < S - 1; m++)
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            v[2 + N + m * N + i] = dw_pack(X[m][i]);
+#pragma unroll
+    for (int i = 2 + N * S; i < RS; i++)
+        v[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < RS; i += 4)
+        st_v4(r + i, v[i], v[i + 1], v[i + 2], v[i + 3]);
+}
+
 __host__ __device__ __forceinline__ bool dw_same(dword x, dword y) { return x.hi == y.hi && x.lo == y.lo; }
 
 // ------------------------------------------------------------ forward sweep
@@ -348,7 +396,10 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
     dword y[N], k0[N], p[P], dt;
     int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
     bool at_top = true, to_end = false;
-    double *xrec = nullptr; // stage values of the current step (STAGES)
+    // STAGES: the current step's record slot and its trial step at the top;
+    // the record is written once, by the accepted attempt
+    double *rec = nullptr;
+    dword dt_top;
 
     auto fetch = [&]() -> bool {
         b = (int)atomicAdd(&a.ctl->fwd_next, 1u);
@@ -455,9 +506,12 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
                     continue;
                 }
                 double *r = record_ptr<RS>(a.pool, chunk, slot);
-                write_record_dw<N>(r, t, dt, y);
-                if (STAGES)
-                    xrec = r + 2 + N;
+                if (STAGES) {
+                    rec = r;
+                    dt_top = dt;
+                } else {
+                    write_record_dw<N>(r, t, dt, y);
+                }
                 slot++;
             }
             to_end = !Tab::FIXED && (t + to_d_int(dt)) - t1 > kDblEps;
@@ -467,7 +521,16 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
             at_top = false;
         }
         dword ynew[N], knew[N];
-        const dword err = attempt_dw<M, Tab>(y, k0, p, dword(t), dt, tol, ynew, knew, xrec);
+        constexpr int XS = Tab::S > 1 ? Tab::S - 1 : 1;
+        dword xs[XS][N]; // stage values X_1 .. X_{s-1} of this attempt (STAGES)
+        const dword err = attempt_dw_sink<M, Tab>(y, k0, p, dword(t), dt, tol, ynew, knew,
+                                                  [&](int m, const dword (&X)[N]) {
+                                                      if constexpr (STAGES) {
+#pragma unroll
+                                                          for (int i = 0; i < N; i++)
+                                                              xs[m - 1][i] = X[i];
+                                                      }
+                                                  });
         bool ok;
         if (err.hi != err.hi) {
             status = ST_NONFINITE;
@@ -479,6 +542,8 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
             to_end = false;
             ok = false;
         } else {
+            if constexpr (STAGES)
+                write_stage_record_dw<N, Tab::S>(rec, t, dt_top, y, xs);
             if constexpr (Tab::FIXED) {
                 t = fixed_time(t_start, count + 1, a.dt0);
             } else {
@@ -668,11 +733,14 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
     int b = -1, q = 0, j = -1, chunk = -1, slot = 0, T = 0, last = -1;
     double t_next = 0.0;
     dword lam[N], mu[P], p[P];
-    // record j, loaded one step ahead: its loads are in flight while the
-    // previous step's VJPs run
-    double nv[RS];
+    // records j-1 .. j-PF, loaded PF steps ahead: their loads are in flight
+    // while the VJPs of the steps before run (two steps measured no faster
+    // than one)
+    constexpr int PF = 1;
+    double nv[PF][RS];
 
-    auto step_back_load = [&]() {
+    // move the load walk one record back and load it into dst
+    auto step_back_load = [&](double (&dst)[RS]) {
         if (slot == 0) {
             chunk = a.pool.chunk_prev[chunk];
             slot = CH - 1;
@@ -680,11 +748,17 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
             slot--;
         }
         const double *r = record_ptr<RS>(a.pool, chunk, slot);
+        if constexpr (STAGES) {
 #pragma unroll
-        for (int i = 0; i < RS; i += 2) {
-            const double2 v = __ldcs(reinterpret_cast<const double2 *>(r + i));
-            nv[i] = v.x;
-            nv[i + 1] = v.y;
+            for (int i = 0; i < RS; i += 4)
+                ld_v4_cs(r + i, dst[i], dst[i + 1], dst[i + 2], dst[i + 3]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < RS; i += 2) {
+                const double2 v = __ldcs(reinterpret_cast<const double2 *>(r + i));
+                dst[i] = v.x;
+                dst[i + 1] = v.y;
+            }
         }
     };
 
@@ -699,8 +773,10 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
             mu[k] = dword(0.0f, 0.0f);
         note_lambda<N>(a, b, q, T, lam);
         j = T - 1;
-        if (j >= 0)
-            step_back_load();
+#pragma unroll
+        for (int d = 0; d < PF; d++)
+            if (j - d >= 0)
+                step_back_load(nv[d]);
     };
 
     auto fetch = [&]() -> bool {
@@ -742,9 +818,14 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
         double cv[RS];
 #pragma unroll
         for (int i = 0; i < RS; i++)
-            cv[i] = nv[i];
-        if (j > 0)
-            step_back_load();
+            cv[i] = nv[0][i];
+#pragma unroll
+        for (int d = 1; d < PF; d++)
+#pragma unroll
+            for (int i = 0; i < RS; i++)
+                nv[d - 1][i] = nv[d][i];
+        if (j - PF >= 0)
+            step_back_load(nv[PF - 1]);
         const double tn = cv[0];
         if constexpr (STAGES) {
             dword X[NS][N];
