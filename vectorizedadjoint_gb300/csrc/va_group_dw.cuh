@@ -128,6 +128,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
 
     int b = -1;
     double t = 0.0, t1 = 0.0, t_start = 0.0;
+    EndTests et{}; // the loop and end-clamp tests as integer comparisons
     dword y, k0, dt, p[P];
     int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
     bool at_top = true, to_end = false;
@@ -153,6 +154,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
         M::template load_params<dword>(a.par + (size_t)b * PT, li, p);
         t = t_start = a.t0[b];
         t1 = a.t1[b];
+        et = end_tests(t1);
         dt = dword(a.dt0);
         count = rej = fails = 0;
         status = ST_OK;
@@ -232,7 +234,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
             continue;
         }
         if (at_top) {
-            if (Tab::FIXED ? !((t + a.dt0) - t1 <= kDblEps) : !(t1 - t > kDblEps)) {
+            if (Tab::FIXED ? !((t + a.dt0) - t1 <= kDblEps) : !end_loop(et, t, t1)) {
                 finish();
                 alive = fetch();
                 continue;
@@ -246,7 +248,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
                 continue;
             }
             write();
-            to_end = !Tab::FIXED && (t + to_d_int(dt)) - t1 > kDblEps;
+            to_end = !Tab::FIXED && end_clamp(et, t + to_d_int(dt), t1);
             if (to_end)
                 dt = dword(t1 - t);
             fails = 0;

@@ -36,6 +36,7 @@
 // give the same bits.
 #pragma once
 
+#include "va_endtests.h"
 #include "va_kernels.cuh"
 
 namespace va {
@@ -393,6 +394,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
 
     int b = -1;
     double t = 0.0, t1 = 0.0, t_start = 0.0;
+    EndTests et{}; // the loop and end-clamp tests as integer comparisons
     dword y[N], k0[N], p[P], dt;
     int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
     bool at_top = true, to_end = false;
@@ -415,6 +417,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
             p[k] = dword(a.par[(size_t)b * P + k]);
         t = t_start = a.t0[b];
         t1 = a.t1[b];
+        et = end_tests(t1);
         dt = dword(a.dt0);
         count = rej = fails = 0;
         status = ST_OK;
@@ -491,7 +494,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
         }
         if (at_top) {
             // fixed steps: while ((t + dt) - t1 <= eps), dt the FP64 step
-            if (Tab::FIXED ? !((t + a.dt0) - t1 <= kDblEps) : !(t1 - t > kDblEps)) {
+            if (Tab::FIXED ? !((t + a.dt0) - t1 <= kDblEps) : !end_loop(et, t, t1)) {
                 finish();
                 alive = fetch();
                 continue;
@@ -514,7 +517,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
                 }
                 slot++;
             }
-            to_end = !Tab::FIXED && (t + to_d_int(dt)) - t1 > kDblEps;
+            to_end = !Tab::FIXED && end_clamp(et, t + to_d_int(dt), t1);
             if (to_end)
                 dt = dword(t1 - t);
             fails = 0;
@@ -871,6 +874,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
     int phase = 0; // 0: re-integrate segment k, 1: back-step through it
     int first = 0; // step index of the segment's first record
     double t = 0.0, t1 = 0.0, t_end = 0.0, t_start = 0.0;
+    EndTests et{};
     dword lam[N], mu[P], p[P], y[N], k0[N], y_end[N], dt;
     bool at_top = true, to_end = false;
 
@@ -935,6 +939,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
             R = (T + SK - 1) / SK + 1;
             last = a.inst_last[b];
             t1 = a.inst_t1[b];
+            et = end_tests(t1);
             if constexpr (Tab::FIXED)
                 t_start = a.inst_t0[b];
             q = 0;
@@ -958,7 +963,7 @@ __global__ void __launch_bounds__(256) backward_kernel_2level_dw(AdjParams a)
         if (phase == 0) {
             // one attempt of the forward controller, as forward_kernel_dw does
             if (at_top) {
-                to_end = !Tab::FIXED && (t + to_d_int(dt)) - t1 > kDblEps;
+                to_end = !Tab::FIXED && end_clamp(et, t + to_d_int(dt), t1);
                 if (to_end)
                     dt = dword(t1 - t);
                 fails = 0;
