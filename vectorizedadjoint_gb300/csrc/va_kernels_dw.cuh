@@ -27,8 +27,10 @@
 // instead: when every step is checkpointed, the record of step n is
 //   [t_n (FP64), dt_n, y_n, X_1 .. X_{s-1} (double-words)]
 // (stage_record_doubles), each double-word packed into one 8-byte slot
-// (dw_pack).  Every attempt of step n writes its stage values into the
-// record; the accepted one is the last to write.  The backward step reads
+// (dw_pack), padded to whole 32-byte sectors.  Each attempt keeps its stage
+// values in registers; the accepted one writes the record, once, in 256-bit
+// stores (partial-sector writes spread over the attempts cost the forward
+// 11% and capped its occupancy).  The backward step reads
 // X_0 = y_n .. X_{s-1} and runs only the VJPs: the adjoint differentiates
 // the stages the forward computed, bit for bit.  The two-level backward
 // (checkpoints every k-th step, records [t, dt, y]) keeps the stage values
