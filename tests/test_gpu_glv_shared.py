@@ -27,8 +27,8 @@ def make_small(N, B, seed=11):
     return A, r, x0
 
 
-def run(N, B, A, r, x0, T, precision, tol=1e-7):
-    s = Solver("glv_shared", N, N, B, tableau="dopri5", precision=precision, atol=tol, rtol=tol)
+def run(N, B, A, r, x0, T, precision, tol=1e-7, traj=None, **kw):
+    s = Solver("glv_shared", N, N, B, tableau="dopri5", precision=precision, atol=tol, rtol=tol, **kw)
     dA = torch.empty(N, N, dtype=torch.float64, device="cuda")
     Ad = dev(A)
     s.set_shared(Ad, dA)
@@ -36,6 +36,8 @@ def run(N, B, A, r, x0, T, precision, tol=1e-7):
     torch.cuda.synchronize()
     res = {k: v.cpu().numpy() for k, v in out.items()}
     res["dA"] = dA.cpu().numpy()
+    if traj is not None:
+        res["traj"] = [s.trajectory(b) for b in traj]
     s.close()
     return res
 
@@ -67,11 +69,21 @@ def test_shared_glv_fp64_bit_exact(oracle, cuda, N, B, T):
     assert np.abs(res["dA"] - dA).max() <= 1e-12 * scale
 
 
+@pytest.mark.parametrize("stage_records", [1, 0])
 @pytest.mark.parametrize("N,B,T", [(64, 10, 10.0), (256, 6, 10.0)])
-def test_shared_glv_mixed_dw(oracle, cuda, N, B, T):
+def test_shared_glv_mixed_dw(oracle, cuda, N, B, T, stage_records):
+    """Double-word bundles against FP64, with stage records (the backward
+    reads the forward's stage points and A X products) and without (the
+    reference's recompute); the record read-back decodes either layout."""
     A, r, x0 = make_small(N, B)
-    r64 = run(N, B, A, r, x0, T, "fp64")
-    rdw = run(N, B, A, r, x0, T, "mixed_dw")
+    r64 = run(N, B, A, r, x0, T, "fp64", traj=[0, B - 1])
+    rdw = run(N, B, A, r, x0, T, "mixed_dw", traj=[0, B - 1], stage_records=stage_records)
+    for (t64, dt64, y64), (tdw, dtdw, ydw) in zip(r64["traj"], rdw["traj"]):
+        # the double-word step sizes follow FP64 to ~1e-9 (the records decode
+        # to the states, not to packed bits)
+        assert len(t64) == len(tdw)
+        np.testing.assert_allclose(tdw, t64, rtol=1e-7, atol=0)
+        np.testing.assert_allclose(ydw, y64, rtol=1e-7, atol=1e-10)
     assert (rdw["status"] == 0).all()
     for b in range(B):
         g = np.concatenate([r64["dy0"][b], r64["dp"][b]])

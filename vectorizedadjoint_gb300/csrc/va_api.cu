@@ -158,12 +158,26 @@ int grid_for(va_handle *h, const void *fn, int block, int instances)
 // stride > 1.
 bool stages_now(const va_handle *h)
 {
-    return !h->bks && va::stage_records_on(h->ks, h->opt.tableau, h->opt.precision, h->stride, h->stages_on);
+    if (h->bks)
+        return h->stages_on && h->opt.precision == VA_PREC_MIXED_DW && h->bks->rs_stage[h->opt.tableau] > 0;
+    return va::stage_records_on(h->ks, h->opt.tableau, h->opt.precision, h->stride, h->stages_on);
+}
+
+// the bundle sweep for the current record layout
+const void *bundle_fwd(const va_handle *h)
+{
+    const int t = h->opt.tableau, p = h->opt.precision;
+    return !stages_now(h) && h->bks->fwd1[t][p] ? h->bks->fwd1[t][p] : h->bks->fwd[t][p];
+}
+const void *bundle_bwd(const va_handle *h)
+{
+    const int t = h->opt.tableau, p = h->opt.precision;
+    return !stages_now(h) && h->bks->bwd1[t][p] ? h->bks->bwd1[t][p] : h->bks->bwd[t][p];
 }
 
 void record_layout(va_handle *h)
 {
-    h->RS = h->bks ? va::record_doubles(h->N)
+    h->RS = h->bks ? (stages_now(h) ? h->bks->rs_stage[h->opt.tableau] : va::record_doubles(h->N))
                    : va::record_doubles_for(h->ks, h->opt.tableau, h->opt.precision, h->stride, h->N, h->stages_on);
     if (!h->pool_bytes)
         return;
@@ -188,7 +202,8 @@ va_status ensure_buffers(va_handle *h)
     // the pool is sized for the largest record layout of the handle; the
     // chunk links for the smallest (most chunks)
     const int rs_small = va::record_doubles(h->N);
-    const int rs_big = h->bks ? rs_small : va::record_doubles_for(h->ks, h->opt.tableau, h->opt.precision, 1, h->N, h->stages_on);
+    const int rs_big = h->bks ? (stages_now(h) ? h->bks->rs_stage[h->opt.tableau] : rs_small)
+                              : va::record_doubles_for(h->ks, h->opt.tableau, h->opt.precision, 1, h->N, h->stages_on);
     int64_t budget = h->opt.ckpt_budget_bytes > 0 ? h->opt.ckpt_budget_bytes : kDefaultBudget;
     const int64_t per_inst_chunks = ((int64_t)h->opt.max_steps + 1 + h->chunk_len - 1) / h->chunk_len;
     h->worst_chunks = per_inst_chunks * B;
@@ -226,10 +241,11 @@ va_status ensure_buffers(va_handle *h)
         VA_CUDA(h, cudaMalloc(&h->dA_part, grid * NN * sizeof(double)));
         for (int t = 0; t < 2; t++)
             for (int p = 0; p < 3; p++) {
-                VA_CUDA(h, cudaFuncSetAttribute(h->bks->fwd[t][p], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)h->bks->smem_fwd[p]));
-                VA_CUDA(h, cudaFuncSetAttribute(h->bks->bwd[t][p], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                (int)h->bks->smem_bwd[p]));
+                const void *fns[4] = {h->bks->fwd[t][p], h->bks->fwd1[t][p], h->bks->bwd[t][p], h->bks->bwd1[t][p]};
+                for (int f = 0; f < 4; f++)
+                    if (fns[f])
+                        VA_CUDA(h, cudaFuncSetAttribute(fns[f], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        (int)(f < 2 ? h->bks->smem_fwd[p] : h->bks->smem_bwd[p])));
             }
     }
     return VA_OK;
@@ -351,7 +367,7 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
         bp.f = a;
         void *args[] = {&bp};
         const int p = h->opt.precision;
-        VA_CUDA(h, cudaLaunchKernel(h->bks->fwd[h->opt.tableau][p], dim3(bundle_grid(h)), dim3(h->N), args,
+        VA_CUDA(h, cudaLaunchKernel(bundle_fwd(h), dim3(bundle_grid(h)), dim3(h->N), args,
                                     h->bks->smem_fwd[p], s));
         h->fwd_grid = bundle_grid(h);
         h->fwd_block = h->N;
@@ -406,7 +422,7 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
         void *args[] = {&bp};
         const int p = h->opt.precision;
         const int grid = bundle_grid(h);
-        VA_CUDA(h, cudaLaunchKernel(h->bks->bwd[h->opt.tableau][p], dim3(grid), dim3(h->N), args,
+        VA_CUDA(h, cudaLaunchKernel(bundle_bwd(h), dim3(grid), dim3(h->N), args,
                                     h->bks->smem_bwd[p], s));
         if (h->shared_dA) {
             const int NN = h->N * h->N;
@@ -871,10 +887,10 @@ va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double
     const int CH = h->chunk_len, RS = h->RS, N = h->N;
     // mixed_dw stage records, and the one-thread kernels' [t, dt, y] records,
     // hold double-words (float pairs {hi, lo} in 8 bytes) after the FP64 time
+    // (bundle stage records: t and dt FP64, the state as double-words)
     const bool dw = h->ks && h->opt.precision == VA_PREC_MIXED_DW && (h->ks->dw_records || stages_now(h));
-    auto field = [dw](double v) {
-        if (!dw)
-            return v;
+    const bool ydw = dw || (h->bks && stages_now(h));
+    auto unpack = [](double v) {
         const va::dword d = va::dw_unpack(v);
         return (double)d.hi + (double)d.lo;
     };
@@ -892,10 +908,12 @@ va_status va_trajectory(va_handle *h, int32_t instance, int32_t capacity, double
             if (t)
                 t[j] = buf[(size_t)k * RS];
             if (dt)
-                dt[j] = field(buf[(size_t)k * RS + 1]);
+                dt[j] = dw ? unpack(buf[(size_t)k * RS + 1]) : buf[(size_t)k * RS + 1];
             if (y)
-                for (int i = 0; i < N; i++)
-                    y[(size_t)j * N + i] = field(buf[(size_t)k * RS + 2 + i]);
+                for (int i = 0; i < N; i++) {
+                    const double v = buf[(size_t)k * RS + 2 + i];
+                    y[(size_t)j * N + i] = ydw ? unpack(v) : v;
+                }
         }
         int prev = -1;
         VA_CUDA(h, cudaMemcpy(&prev, h->chunk_prev + chunk, sizeof(int), cudaMemcpyDeviceToHost));

@@ -15,6 +15,15 @@
 // into a private N x N partial of the CTA in global memory, and a final
 // kernel adds the partials in a fixed order -- no atomics on any result.
 //
+// Stage records (double-word sweeps, the default): the forward also stores,
+// per accepted step, the stage points X_m and the products z_m = A X_m it
+// formed, so the backward reads them instead of redoing the s matrix-vector
+// products of the stage recompute -- a third of its arithmetic.  Record of
+// a step: [t, dt (FP64), X_0 .. X_{s-1}, z_0 .. z_{s-1} (packed
+// double-words, component i at offset i)], 24.6 KB per instance-step at
+// N = 256; the sweeps with [t, dt, y] records and the recompute remain
+// (stage records off, FP64 and FP32 modes).
+//
 // The arithmetic per component follows the reference's GLV functor
 // (examples/GeneralizedLotkaVolterra/main.cpp:109-118: sum_j in ascending
 // order, then x_i (r_i + sum)) and the same back_prop_step recurrence as the
@@ -25,6 +34,9 @@
 #include "va_kernels.cuh"
 
 namespace va {
+
+// doubles per stage record of a bundle instance (padded to 32 bytes)
+__host__ __device__ constexpr int bundle_stage_record_doubles(int nt, int s) { return (2 + 2 * s * nt + 3) & ~3; }
 
 struct BundleParams {
     FwdParams f;          // batch, inputs (par = r[B][N]), tolerances, outputs, pool
@@ -126,11 +138,12 @@ __device__ __forceinline__ void bundle_matvec(const double *Mt, const dword *Mtw
 
 // ------------------------------------------------------------ forward sweep
 
-template <int NT, int NB, class Tab, class S>
+template <int NT, int NB, class Tab, class S, bool STAGES = false>
 __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
 {
     constexpr int NS = Tab::S;
-    constexpr int RS = record_doubles(NT);
+    constexpr bool ST = STAGES && std::is_same<S, dword>::value; // stage records
+    constexpr int RS = ST ? bundle_stage_record_doubles(NT, NS) : record_doubles(NT);
     const FwdParams &a = bp.f;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     S *xs = reinterpret_cast<S *>(smem_raw);                               // [NT][NB]
@@ -141,6 +154,8 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
 
     double y[NB], t[NB], t1[NB], dt[NB];
     S ys[NB], r[NB], K[NS][NB], knew[NB];
+    S z0[NB];           // ST: z_0 = A y of the current state
+    double *rec_cur[NB]; // ST: the current step's record
     int count[NB], rej[NB], fails[NB], status[NB], chunk[NB], slot[NB], inst[NB];
     bool active[NB], at_top[NB];
 
@@ -159,6 +174,8 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
         dt[b] = a.dt0;
         ys[b] = S(0);
         r[b] = S(0);
+        z0[b] = S(0);
+        rec_cur[b] = nullptr;
         if (active[b]) {
             y[b] = a.y0[(size_t)inst[b] * NT + i];
             r[b] = from_d<S>(a.par[(size_t)inst[b] * NT + i]);
@@ -198,8 +215,10 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
         S z[NB];
         bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, z);
 #pragma unroll
-        for (int b = 0; b < NB; b++)
+        for (int b = 0; b < NB; b++) {
             K[0][b] = ys[b] * (r[b] + z[b]);
+            z0[b] = z[b];
+        }
     }
     __syncthreads();
 
@@ -263,7 +282,13 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
                 double *rec = record_ptr<RS>(a.pool, chunk[b], slot[b]);
                 if (i == 0)
                     *reinterpret_cast<double2 *>(rec) = make_double2(t[b], dt[b]);
-                rec[2 + i] = y[b];
+                if constexpr (ST) {
+                    rec[2 + i] = dw_pack(ys[b]);
+                    rec[2 + NS * NT + i] = dw_pack(z0[b]);
+                    rec_cur[b] = rec;
+                } else {
+                    rec[2 + i] = y[b];
+                }
                 slot[b]++;
             }
             if (status[b] != ST_OK || !(t1[b] - t[b] > kDblEps)) {
@@ -328,8 +353,18 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
             S z[NB];
             bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, z);
 #pragma unroll
-            for (int b = 0; b < NB; b++)
-                K[m][b] = xs[i * NB + b] * (r[b] + z[b]);
+            for (int b = 0; b < NB; b++) {
+                const S X = xs[i * NB + b];
+                K[m][b] = X * (r[b] + z[b]);
+                if constexpr (ST) {
+                    // every attempt rewrites the step's stage values: the
+                    // accepted one is the last
+                    if (active[b] && !at_top[b]) {
+                        rec_cur[b][2 + m * NT + i] = dw_pack(X);
+                        rec_cur[b][2 + (NS + m) * NT + i] = dw_pack(z[b]);
+                    }
+                }
+            }
             __syncthreads();
         }
         // y_new, f(y_new), error estimate
@@ -356,13 +391,13 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
             }
             xs[i * NB + b] = ynew_s[b];
         }
+        S znew[NB];
         if constexpr (Tab::FSAL) {
             __syncthreads();
-            S z[NB];
-            bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, z);
+            bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, znew);
 #pragma unroll
             for (int b = 0; b < NB; b++)
-                knew[b] = ynew_s[b] * (r[b] + z[b]);
+                knew[b] = ynew_s[b] * (r[b] + znew[b]);
             __syncthreads();
         }
         double ratio[NB];
@@ -419,8 +454,10 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
                 dt[b] = increase_step<Tab, S>(dt[b], err);
                 y[b] = ynew[b];
                 ys[b] = ynew_s[b];
-                if constexpr (Tab::FSAL)
+                if constexpr (Tab::FSAL) {
                     K[0][b] = knew[b];
+                    z0[b] = znew[b];
+                }
                 ok = true;
             }
             if (fails[b] >= a.max_fail) {
@@ -446,8 +483,10 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
             S z[NB];
             bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, z);
 #pragma unroll
-            for (int b = 0; b < NB; b++)
+            for (int b = 0; b < NB; b++) {
                 K[0][b] = ys[b] * (r[b] + z[b]);
+                z0[b] = z[b];
+            }
             __syncthreads();
         }
     }
@@ -455,11 +494,12 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
 
 // ----------------------------------------------------------- backward sweep
 
-template <int NT, int NB, class Tab, class S>
+template <int NT, int NB, class Tab, class S, bool STAGES = false>
 __global__ void __launch_bounds__(NT) backward_bundle_kernel(BundleParams bp)
 {
     constexpr int NS = Tab::S;
-    constexpr int RS = record_doubles(NT);
+    constexpr bool ST = STAGES && std::is_same<S, dword>::value; // stage records
+    constexpr int RS = ST ? bundle_stage_record_doubles(NT, NS) : record_doubles(NT);
     const AdjParams &a = bp.g;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     S *xall = reinterpret_cast<S *>(smem_raw);      // [NS][NT][NB] stage points
@@ -501,7 +541,7 @@ __global__ void __launch_bounds__(NT) backward_bundle_kernel(BundleParams bp)
         slot[b] = T[b] % CH;
         const double *rec = record_ptr<RS>(a.pool, chunk[b], slot[b]);
         t_next[b] = rec[0];
-        const double yT = rec[2 + i];
+        const double yT = ST ? to_d(dw_unpack(rec[2 + i])) : rec[2 + i];
         lam[b] = a.cost == 0 ? 2.0 * yT : a.cost == 1 ? 1.0 : a.lambdaT[(size_t)inst[b] * NT + i];
         j[b] = T[b] - 1;
     }
@@ -520,6 +560,7 @@ __global__ void __launch_bounds__(NT) backward_bundle_kernel(BundleParams bp)
         bool step[NB];
         double y[NB], h[NB], tn[NB];
         S ys[NB], sh[NB];
+        const double *srec[NB]; // ST: the step's stage record
 #pragma unroll
         for (int b = 0; b < NB; b++) {
             step[b] = live[b] && j[b] >= 0;
@@ -534,17 +575,35 @@ __global__ void __launch_bounds__(NT) backward_bundle_kernel(BundleParams bp)
                     slot[b]--;
                 }
                 const double *rec = record_ptr<RS>(a.pool, chunk[b], slot[b]);
+                srec[b] = rec;
                 tn[b] = rec[0];
-                y[b] = rec[2 + i];
+                if constexpr (!ST)
+                    y[b] = rec[2 + i];
                 h[b] = t_next[b] - tn[b];
             }
             ys[b] = from_d<S>(y[b]);
             sh[b] = from_d<S>(h[b]);
         }
+        if constexpr (ST) {
+            // the forward's stage points and products A X_m
+#pragma unroll
+            for (int m = 0; m < NS; m++)
+#pragma unroll
+                for (int b = 0; b < NB; b++) {
+                    S X = S(0), z = S(0);
+                    if (step[b]) {
+                        X = dw_unpack(__ldcs(srec[b] + 2 + m * NT + i));
+                        z = dw_unpack(__ldcs(srec[b] + 2 + (NS + m) * NT + i));
+                    }
+                    xall[((size_t)m * NT + i) * NB + b] = X;
+                    zall[((size_t)m * NT + i) * NB + b] = z;
+                }
+            __syncthreads();
+        }
         // recompute the stages (compute_intermediate_states)
         S K[NS][NB];
 #pragma unroll
-        for (int m = 0; m < NS; m++) {
+        for (int m = 0; m < NS && !ST; m++) {
 #pragma unroll
             for (int b = 0; b < NB; b++) {
                 S X;

@@ -1,5 +1,6 @@
 // Shared-matrix GLV bundle kernels (N = 64, 256; 4 instances per CTA):
-// reduced-precision sweeps and the helper kernels.  FP64 sweeps come from
+// reduced-precision sweeps (double-word: with and without stage records) and
+// the helper kernels.  FP64 sweeps come from
 // va_inst_bundle_fp64.cu, built without FMA contraction.
 #include "va_bundle.cuh"
 #include "va_registry.h"
@@ -18,13 +19,19 @@ static BundleKernelSet make_bundle(void (*fill_fp64)(BundleKernelSet &))
     k.nb = NB;
     fill_fp64(k);
     k.fwd[0][1] = (const void *)forward_bundle_kernel<NT, NB, TabDopri5, float>;
-    k.fwd[0][2] = (const void *)forward_bundle_kernel<NT, NB, TabDopri5, dword>;
+    k.fwd[0][2] = (const void *)forward_bundle_kernel<NT, NB, TabDopri5, dword, true>;
+    k.fwd1[0][2] = (const void *)forward_bundle_kernel<NT, NB, TabDopri5, dword>;
     k.fwd[1][1] = (const void *)forward_bundle_kernel<NT, NB, TabCK54, float>;
-    k.fwd[1][2] = (const void *)forward_bundle_kernel<NT, NB, TabCK54, dword>;
+    k.fwd[1][2] = (const void *)forward_bundle_kernel<NT, NB, TabCK54, dword, true>;
+    k.fwd1[1][2] = (const void *)forward_bundle_kernel<NT, NB, TabCK54, dword>;
     k.bwd[0][1] = (const void *)backward_bundle_kernel<NT, NB, TabDopri5, float>;
-    k.bwd[0][2] = (const void *)backward_bundle_kernel<NT, NB, TabDopri5, dword>;
+    k.bwd[0][2] = (const void *)backward_bundle_kernel<NT, NB, TabDopri5, dword, true>;
+    k.bwd1[0][2] = (const void *)backward_bundle_kernel<NT, NB, TabDopri5, dword>;
     k.bwd[1][1] = (const void *)backward_bundle_kernel<NT, NB, TabCK54, float>;
-    k.bwd[1][2] = (const void *)backward_bundle_kernel<NT, NB, TabCK54, dword>;
+    k.bwd[1][2] = (const void *)backward_bundle_kernel<NT, NB, TabCK54, dword, true>;
+    k.bwd1[1][2] = (const void *)backward_bundle_kernel<NT, NB, TabCK54, dword>;
+    k.rs_stage[0] = bundle_stage_record_doubles(NT, TabDopri5::S);
+    k.rs_stage[1] = bundle_stage_record_doubles(NT, TabCK54::S);
     const size_t sz[3] = {sizeof(double), sizeof(float), sizeof(dword)};
     for (int p = 0; p < 3; p++) {
         k.smem_fwd[p] = sz[p] * NT * NB + sizeof(double) * (NT / 32) * NB + sizeof(int) * NB;

@@ -62,8 +62,11 @@ void fill_fixed_glv10(KernelSet &k);
 constexpr int kBundleNB = 4;
 struct BundleKernelSet {
     int N, nb;
-    const void *fwd[kTableaux][3]; // __global__ void(BundleParams), blockDim = N
+    const void *fwd[kTableaux][3]; // __global__ void(BundleParams), blockDim = N (mixed_dw: stage records)
     const void *bwd[kTableaux][3];
+    const void *fwd1[kTableaux][3]; // mixed_dw sweeps over [t, dt, y] records (stage records off); null: fwd
+    const void *bwd1[kTableaux][3];
+    int rs_stage[kTableaux];        // mixed_dw: doubles per stage record (0: none)
     size_t smem_fwd[3], smem_bwd[3]; // dynamic shared memory per precision
     const void *prepare;   // prepare_A_kernel: A -> A^T and double-word copies
     const void *reduce;    // reduce_dA_kernel: CTA partials -> dA
