@@ -94,8 +94,10 @@ __device__ __forceinline__ void bundle_max(double (&v)[NB], double *red /* [NT/3
 // memory (thread i).  Mt is the matrix read as Mt[j][i] (consecutive i are
 // consecutive addresses).  One pass over the matrix serves all NB vectors.
 // (Double-word path: the dot products run through the compensated
-// accumulator dacc, ~12 FP32 operations per term.)
-template <int NT, int NB, class S>
+// accumulator dacc, ~12 FP32 operations per term.)  UNR: matrix rows in
+// flight per thread (the loads come from L2; measured at N = 256: 16 rows
+// suit the forward, 8 the backward, which holds more registers).
+template <int NT, int NB, class S, int UNR = 8>
 __device__ __forceinline__ void bundle_matvec_acc(const double *Mt, const dword *Mtw,
                                                   const S *xs /* [NT][NB] */, S (&z)[NB])
 {
@@ -105,7 +107,7 @@ __device__ __forceinline__ void bundle_matvec_acc(const double *Mt, const dword 
 #pragma unroll
         for (int b = 0; b < NB; b++)
             zc[b] = dacc_of(z[b]);
-#pragma unroll 4
+#pragma unroll UNR
         for (int j = 0; j < NT; j++) {
             const dword a = Mtw[(size_t)j * NT + i];
 #pragma unroll
@@ -126,14 +128,14 @@ __device__ __forceinline__ void bundle_matvec_acc(const double *Mt, const dword 
     }
 }
 
-template <int NT, int NB, class S>
+template <int NT, int NB, class S, int UNR = 8>
 __device__ __forceinline__ void bundle_matvec(const double *Mt, const dword *Mtw, const S *xs /* [NT][NB] */,
                                               S (&z)[NB])
 {
 #pragma unroll
     for (int b = 0; b < NB; b++)
         z[b] = S(0);
-    bundle_matvec_acc<NT, NB, S>(Mt, Mtw, xs, z);
+    bundle_matvec_acc<NT, NB, S, UNR>(Mt, Mtw, xs, z);
 }
 
 // ------------------------------------------------------------ forward sweep
@@ -213,7 +215,7 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
     }
     {
         S z[NB];
-        bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, z);
+        bundle_matvec<NT, NB, S, 16>(bp.At, bp.Atw, xs, z);
 #pragma unroll
         for (int b = 0; b < NB; b++) {
             K[0][b] = ys[b] * (r[b] + z[b]);
@@ -351,7 +353,7 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
             }
             __syncthreads();
             S z[NB];
-            bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, z);
+            bundle_matvec<NT, NB, S, 16>(bp.At, bp.Atw, xs, z);
 #pragma unroll
             for (int b = 0; b < NB; b++) {
                 const S X = xs[i * NB + b];
@@ -394,7 +396,7 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
         S znew[NB];
         if constexpr (Tab::FSAL) {
             __syncthreads();
-            bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, znew);
+            bundle_matvec<NT, NB, S, 16>(bp.At, bp.Atw, xs, znew);
 #pragma unroll
             for (int b = 0; b < NB; b++)
                 knew[b] = ynew_s[b] * (r[b] + znew[b]);
@@ -481,7 +483,7 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
                 xs[i * NB + b] = ys[b];
             __syncthreads();
             S z[NB];
-            bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xs, z);
+            bundle_matvec<NT, NB, S, 16>(bp.At, bp.Atw, xs, z);
 #pragma unroll
             for (int b = 0; b < NB; b++) {
                 K[0][b] = ys[b] * (r[b] + z[b]);
