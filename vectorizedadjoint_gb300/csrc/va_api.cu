@@ -426,7 +426,8 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
                                     h->bks->smem_bwd[p], s));
         if (h->shared_dA) {
             const int NN = h->N * h->N;
-            void *rargs[] = {(void *)&h->dA_part, (void *)&grid, (void *)&h->shared_dA};
+            int dw = p == VA_PREC_MIXED_DW;
+            void *rargs[] = {(void *)&h->dA_part, (void *)&grid, (void *)&dw, (void *)&h->shared_dA};
             VA_CUDA(h, cudaLaunchKernel(h->bks->reduce, dim3((NN + 255) / 256), dim3(256), rargs, 0, s));
         }
         h->bwd_grid = grid;

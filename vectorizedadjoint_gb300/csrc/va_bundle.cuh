@@ -699,13 +699,17 @@ __global__ void __launch_bounds__(NT) backward_bundle_kernel(BundleParams bp)
                     vi[m][b] = vall[((size_t)m * NT + i) * NB + b];
             for (int jj = 0; jj < NT; jj++) {
                 if constexpr (std::is_same<S, dword>::value) {
+                    // the partial stays a double-word (packed in the 8-byte
+                    // slot): accumulating it in FP64 cost four FP64-pipe
+                    // operations per element and step
                     dacc acc{0.0f, 0.0f};
 #pragma unroll
                     for (int m = NS - 1; m >= 0; m--)
 #pragma unroll
                         for (int b = 0; b < NB; b++)
                             dacc_fma(acc, vi[m][b], xall[((size_t)m * NT + jj) * NB + b]);
-                    part[(size_t)jj * NT + i] += to_d(dacc_get(acc));
+                    double &pe = part[(size_t)jj * NT + i];
+                    pe = dw_pack(dw_unpack(pe) + dacc_get(acc));
                 } else {
                     S acc = S(0);
 #pragma unroll
@@ -743,16 +747,19 @@ __global__ void __launch_bounds__(NT) backward_bundle_kernel(BundleParams bp)
     }
 }
 
-// dA = sum over CTAs of the transposed partials, in CTA order.
+// dA = sum over CTAs of the transposed partials, in CTA order (FP64 sum of
+// the partials; dw: the partials are packed double-words).
 template <int NT>
-__global__ void reduce_dA_kernel(const double *part, int nparts, double *dA)
+__global__ void reduce_dA_kernel(const double *part, int nparts, int dw, double *dA)
 {
     const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; // k = jj * NT + i
     if (k >= (size_t)NT * NT)
         return;
     double s = 0.0;
-    for (int c = 0; c < nparts; c++)
-        s += part[(size_t)c * NT * NT + k];
+    for (int c = 0; c < nparts; c++) {
+        const double v = part[(size_t)c * NT * NT + k];
+        s += dw ? to_d(dw_unpack(v)) : v; // double-word sweeps keep packed partials
+    }
     const size_t jj = k / NT, i = k % NT;
     dA[i * NT + jj] = s;
 }
