@@ -9,16 +9,23 @@
 // group maximum of the per-lane double-word ratios (odeint's max norm over
 // components), compared exactly, and every lane runs the controller on the
 // same values.  Records are stage records, lane i writing its components:
-//   [t_n, dt_n, y_n[0..NN), X_1[0..NN), ..., X_{s-1}[0..NN)]
-// so the backward step reads X_m instead of recomputing it, and fuses each
-// stage's VJP with the mu accumulation (dr_i += w_i x_i, dA_ij += w_i x_i x_j)
-// through compensated accumulators.
+//   [t_n, dt_n, y_n[0..NN), X_1[0..NN), ..., X_{s-1}[0..NN),
+//    s_0[0..NN), ..., s_{s-1}[0..NN)]
+// with s_m = r + A X_m the rates of the stage points, so the backward step
+// reads X_m and s_m instead of recomputing them (the rates were a quarter
+// of the backward's time at N = 10), and fuses each stage's VJP with the mu
+// accumulation (dr_i += w_i x_i, dA_ij += w_i x_i x_j) through compensated
+// accumulators.
 #pragma once
 
 #include "va_group.cuh"
 #include "va_kernels_dw.cuh"
 
 namespace va {
+
+// doubles per lane-group stage record: t, dt, X_0 .. X_{s-1}, s_0 .. s_{s-1}
+// (NN each), padded to 32 bytes
+__host__ __device__ constexpr int group_stage_record_doubles(int nn, int s) { return (2 + 2 * nn * s + 3) & ~3; }
 
 // Group maximum of non-negative double-word ratios, NaN if any lane's is.
 template <int G>
@@ -42,31 +49,36 @@ template <int NN>
 struct GLVLaneDw {
     static constexpr int P = 1 + 2 * NN, PG = 1 + NN;
 
-    __device__ __forceinline__ static dword rhs(dword x, const dword (&p)[P], int base, unsigned mask)
+    // f_i, and the rate rate = r_i + sum_j A_ij x_j with f_i = x_i rate
+    __device__ __forceinline__ static dword rhs(dword x, const dword (&p)[P], int base, unsigned mask,
+                                                dword &rate)
     {
         dacc s = dacc_of(p[0]);
 #pragma unroll
         for (int j = 0; j < NN; j++)
             dacc_fma(s, p[1 + j], shfl(x, base + j, mask));
-        return x * dacc_get(s);
+        rate = dacc_get(s);
+        return x * rate;
+    }
+    __device__ __forceinline__ static dword rhs(dword x, const dword (&p)[P], int base, unsigned mask)
+    {
+        dword rate;
+        return rhs(x, p, base, mask, rate);
     }
 
     // (J^T w)_i = w_i (r_i + sum_j A_ij x_j) + sum_k A_ki w_k x_k, returned;
     // the parameter adjoint (dr_i, dA_i.) += (v_i, v_i x_.) with v = w x,
     // added into dm
-    __device__ __forceinline__ static dword vjp_acc(dword w, dword x, const dword (&p)[P], int base,
+    // (the rate of x, r_i + sum_j A_ij x_j, comes from the stage record)
+    __device__ __forceinline__ static dword vjp_acc(dword w, dword x, dword rate, const dword (&p)[P], int base,
                                                     unsigned mask, dacc (&dm)[PG])
     {
         const dword v = w * x;
-        dacc s = dacc_of(p[0]);
 #pragma unroll
-        for (int j = 0; j < NN; j++) {
-            const dword xj = shfl(x, base + j, mask);
-            dacc_fma(s, p[1 + j], xj);
-            dacc_fma(dm[1 + j], v, xj);
-        }
+        for (int j = 0; j < NN; j++)
+            dacc_fma(dm[1 + j], v, shfl(x, base + j, mask));
         dacc_add(dm[0], v);
-        dacc g = dacc_mul(w, dacc_get(s));
+        dacc g = dacc_mul(w, rate);
 #pragma unroll
         for (int k = 0; k < NN; k++)
             dacc_fma(g, p[1 + NN + k], shfl(v, base + k, mask));
@@ -75,12 +87,13 @@ struct GLVLaneDw {
 };
 
 // One attempt on lane i's component (the group runs it in lockstep):
-// y_new, k_new and this lane's error ratio; xrec (may be null) receives
-// X_1 .. X_{s-1} with stride NN.
+// y_new, k_new (and its rate) and this lane's error ratio; xrec (may be
+// null) receives X_m at xrec + (m - 1) NN and its rate s_m at
+// xrec + (s + m - 1) NN, m = 1 .. s-1.
 template <int NN, class Tab>
 __device__ __forceinline__ dword attempt_glv_dw(dword y, dword k0, const dword (&p)[GLVLaneDw<NN>::P], dword dt,
                                                 const DwTol &tol, int base, unsigned mask, dword &ynew,
-                                                dword &knew, double *xrec)
+                                                dword &knew, dword &rate_new, double *xrec)
 {
     constexpr int NS = Tab::S;
     using L = GLVLaneDw<NN>;
@@ -91,15 +104,18 @@ __device__ __forceinline__ dword attempt_glv_dw(dword y, dword k0, const dword (
     for (int m = 1; m < NS; m++) {
         dword X[1];
         stage_dw<Tab, 1>(m, ys, K, dt, X);
-        if (xrec)
+        dword rate;
+        K[m][0] = L::rhs(X[0], p, base, mask, rate);
+        if (xrec) {
             xrec[(m - 1) * NN] = dw_pack(X[0]);
-        K[m][0] = L::rhs(X[0], p, base, mask);
+            xrec[(NS + m - 1) * NN] = dw_pack(rate);
+        }
     }
     ynew = axpy_dw(y, dt, wsum_dw<NS>(typename BWeights::template of<Tab>(), K, 0));
     if constexpr (Tab::FIXED)
         return dword(0.0f, 0.0f); // no error estimate: every attempt is accepted
     if constexpr (Tab::FSAL)
-        knew = L::rhs(ynew, p, base, mask);
+        knew = L::rhs(ynew, p, base, mask, rate_new);
     dacc e = wsum_dw<NS>(typename EWeights::template of<Tab>(), K, 0);
     if constexpr (Tab::FSAL)
         dacc_fma_k(e, Tab::E_NEW, knew);
@@ -117,7 +133,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
     using M = ModelGLVLane<NN>;
     using L = GLVLaneDw<NN>;
     constexpr int G = NN, PT = M::PTOT, P = L::P;
-    constexpr int RS = stage_record_doubles(NN, Tab::S);
+    constexpr int RS = group_stage_record_doubles(NN, Tab::S);
     const LaneGroup<G> grp;
     if (!grp.active())
         return;
@@ -130,6 +146,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
     double t = 0.0, t1 = 0.0, t_start = 0.0;
     EndTests et{}; // the loop and end-clamp tests as integer comparisons
     dword y, k0, dt, p[P];
+    dword rate0; // r_i + (A y)_i of the current state (stage record slot s_0)
     int count = 0, rej = 0, fails = 0, status = ST_OK, chunk = -1, slot = 0;
     bool at_top = true, to_end = false;
     double *xrec = nullptr;
@@ -169,7 +186,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
         } else if (li == 0) {
             a.pool.chunk_prev[chunk] = -1;
         }
-        k0 = L::rhs(y, p, src, mask);
+        k0 = L::rhs(y, p, src, mask, rate0);
         return true;
     };
 
@@ -198,6 +215,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
             *reinterpret_cast<double2 *>(r) = make_double2(t, dw_pack(dt));
         r[2 + li] = dw_pack(y);
         xrec = r + 2 + NN + li;
+        r[2 + Tab::S * NN + li] = dw_pack(rate0);
         slot++;
     };
 
@@ -254,8 +272,9 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
             fails = 0;
             at_top = false;
         }
-        dword ynew, knew;
-        const dword err = group_max_dw<G>(attempt_glv_dw<NN, Tab>(y, k0, p, dt, tol, src, mask, ynew, knew, xrec),
+        dword ynew, knew, rate_new;
+        const dword err = group_max_dw<G>(attempt_glv_dw<NN, Tab>(y, k0, p, dt, tol, src, mask, ynew, knew, rate_new,
+                                                                  xrec),
                                           mask);
         bool ok;
         if (err.hi != err.hi) {
@@ -275,10 +294,12 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
                 dt = increase_dw<Tab>(dt, err);
             }
             y = ynew;
-            if constexpr (Tab::FSAL)
+            if constexpr (Tab::FSAL) {
                 k0 = knew;
-            else
-                k0 = L::rhs(y, p, src, mask);
+                rate0 = rate_new;
+            } else {
+                k0 = L::rhs(y, p, src, mask, rate0);
+            }
             ok = true;
         }
         if (fails >= a.max_fail) {
@@ -301,7 +322,7 @@ __global__ void __launch_bounds__(256) backward_group_dw_kernel(AdjParams a)
     using M = ModelGLVLane<NN>;
     using L = GLVLaneDw<NN>;
     constexpr int G = NN, PT = M::PTOT, P = L::P, PG = L::PG, NS = Tab::S;
-    constexpr int RS = stage_record_doubles(NN, NS);
+    constexpr int RS = group_stage_record_doubles(NN, NS);
     const LaneGroup<G> grp;
     if (!grp.active())
         return;
@@ -313,8 +334,9 @@ __global__ void __launch_bounds__(256) backward_group_dw_kernel(AdjParams a)
     double t_next = 0.0;
     dword lam, p[P];
     dacc dm[PG];
-    // this lane's part of record j (t, X_0 .. X_{s-1}), loaded one step ahead
-    double nt, nx[NS];
+    // this lane's part of record j (t, X_0 .. X_{s-1}, s_0 .. s_{s-1}),
+    // loaded one step ahead
+    double nt, nx[NS], ns[NS];
 
     auto step_back_load = [&]() {
         if (slot == 0) {
@@ -326,8 +348,10 @@ __global__ void __launch_bounds__(256) backward_group_dw_kernel(AdjParams a)
         const double *r = record_ptr<RS>(a.pool, chunk, slot);
         nt = __ldcs(r);
 #pragma unroll
-        for (int m = 0; m < NS; m++)
+        for (int m = 0; m < NS; m++) {
             nx[m] = __ldcs(r + 2 + m * NN + li);
+            ns[m] = __ldcs(r + 2 + (NS + m) * NN + li);
+        }
     };
 
     auto start_seed = [&]() {
@@ -410,10 +434,12 @@ __global__ void __launch_bounds__(256) backward_group_dw_kernel(AdjParams a)
             continue;
         }
         const double tn = nt;
-        dword X[NS];
+        dword X[NS], rate[NS];
 #pragma unroll
-        for (int m = 0; m < NS; m++)
+        for (int m = 0; m < NS; m++) {
             X[m] = dw_unpack(nx[m]);
+            rate[m] = dw_unpack(ns[m]);
+        }
         if (j > 0)
             step_back_load();
         // back_prop_step (backpropagation.hpp:160-229) on lane i's components
@@ -429,7 +455,7 @@ __global__ void __launch_bounds__(256) backward_group_dw_kernel(AdjParams a)
         dacc dl = dacc_of(lam);
 #pragma unroll
         for (int m = NS - 1; m >= 0; m--) {
-            const dword gx = L::vjp_acc(dacc_get(Kb[m]), X[m], p, src, mask, dm);
+            const dword gx = L::vjp_acc(dacc_get(Kb[m]), X[m], rate[m], p, src, mask, dm);
             dacc_add(dl, gx);
             if (m > 0) {
                 const dword gh = gx * h;

@@ -48,7 +48,7 @@ static void fill_group_one(KernelSet &k)
     k.bwd[I][2] = (const void *)backward_group_dw_kernel<NN, Tab>;
     k.fwd2[I][2] = (const void *)forward_group_kernel<M, Tab, dword>;
     k.bwd1[I][2] = (const void *)backward_group_kernel<M, Tab, dword>;
-    k.rs_stage[I] = stage_record_doubles(NN, Tab::S);
+    k.rs_stage[I] = group_stage_record_doubles(NN, Tab::S);
 }
 
 void fill_fixed_vdp(KernelSet &k)

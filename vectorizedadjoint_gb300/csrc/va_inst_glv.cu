@@ -36,8 +36,8 @@ static KernelSet make_glv(void (*fill_fp64)(KernelSet &), void (*fill_rkf78)(Ker
     k.fwd2[1][2] = (const void *)forward_group_kernel<M, TabCK54, dword>;
     k.bwd1[0][2] = (const void *)backward_group_kernel<M, TabDopri5, dword>;
     k.bwd1[1][2] = (const void *)backward_group_kernel<M, TabCK54, dword>;
-    k.rs_stage[0] = stage_record_doubles(NN, TabDopri5::S);
-    k.rs_stage[1] = stage_record_doubles(NN, TabCK54::S);
+    k.rs_stage[0] = group_stage_record_doubles(NN, TabDopri5::S);
+    k.rs_stage[1] = group_stage_record_doubles(NN, TabCK54::S);
     k.dw_records = false; // the [t, dt, y] records of the fallback sweeps are FP64
     fill_rkf78(k);
     fill_fixed(k);

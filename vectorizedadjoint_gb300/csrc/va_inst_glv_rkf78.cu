@@ -20,7 +20,7 @@ static void fill(KernelSet &k)
     k.bwd[2][2] = (const void *)backward_group_dw_kernel<NN, T>;
     k.fwd2[2][2] = (const void *)forward_group_kernel<M, T, dword>;
     k.bwd1[2][2] = (const void *)backward_group_kernel<M, T, dword>;
-    k.rs_stage[2] = stage_record_doubles(NN, T::S);
+    k.rs_stage[2] = group_stage_record_doubles(NN, T::S);
 }
 
 void fill_rkf78_glv5(KernelSet &k)
