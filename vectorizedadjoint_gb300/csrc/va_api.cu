@@ -1046,7 +1046,9 @@ va_status va_autotune(va_handle *h, int32_t cost, const double *y0, const double
             long need = ((long)h->prob.batch * h->ks->tpi + blk - 1) / blk;
             h->fwd_grid = (int)std::max(1L, std::min((long)h->sm_count * std::min(bps, std::max(occf, 1)), need));
             h->bwd_grid = (int)std::max(1L, std::min((long)h->sm_count * std::min(bps, std::max(occb, 1)), need));
-            for (int rep = 0; rep < 2; rep++) {
+            // a warm-up run, then the best of two timed runs
+            float cand_f = 1e30f, cand_b = 1e30f;
+            for (int rep = 0; rep < 3; rep++) {
                 VA_CUDA(h, cudaEventRecord(e0, s));
                 st = enqueue_forward(h, y0, params, t0, t1, h->s_yT, nullptr, nullptr, h->s_status, s);
                 if (st != VA_OK)
@@ -1060,18 +1062,20 @@ va_status va_autotune(va_handle *h, int32_t cost, const double *y0, const double
                 float tf = 0, tb = 0;
                 cudaEventElapsedTime(&tf, e0, e1);
                 cudaEventElapsedTime(&tb, e1, e2);
-                if (rep == 1) {
-                    if (tf < best_f) {
-                        best_f = tf;
-                        bf_block = blk;
-                        bf_grid = h->fwd_grid;
-                    }
-                    if (tb < best_b) {
-                        best_b = tb;
-                        bb_block = blk;
-                        bb_grid = h->bwd_grid;
-                    }
+                if (rep > 0) {
+                    cand_f = std::min(cand_f, tf);
+                    cand_b = std::min(cand_b, tb);
                 }
+            }
+            if (cand_f < best_f) {
+                best_f = cand_f;
+                bf_block = blk;
+                bf_grid = h->fwd_grid;
+            }
+            if (cand_b < best_b) {
+                best_b = cand_b;
+                bb_block = blk;
+                bb_grid = h->bwd_grid;
             }
         }
     }
