@@ -228,6 +228,7 @@ va_status ensure_buffers(va_handle *h)
         VA_CUDA(h, cudaMalloc(&h->order_fwd, (size_t)B * sizeof(int)));
         VA_CUDA(h, cudaMalloc(&h->order_bwd, (size_t)B * sizeof(int)));
         VA_CUDA(h, cudaMalloc(&h->order_work, va::order_work_ints() * sizeof(int)));
+        VA_CUDA(h, cudaMemset(h->order_work, 0, va::order_work_ints() * sizeof(int)));
         // attempts per instance of the last forward sweep, then its valid flag
         VA_CUDA(h, cudaMalloc(&h->inst_work, ((size_t)B + 1) * sizeof(int)));
         VA_CUDA(h, cudaMemset(h->inst_work + B, 0, sizeof(int)));
@@ -412,7 +413,7 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
     a.pool = pool_of(h);
     a.ctl = h->ctl;
     if (h->order_bwd) {
-        va::OrderArgs o{a.B, h->inst_T, nullptr, nullptr, nullptr, nullptr, h->order_work, h->order_bwd};
+        va::OrderArgs o{a.B, h->inst_T, nullptr, nullptr, nullptr, nullptr, h->order_work, h->order_bwd, h->order_fwd};
         VA_CUDA(h, va::enqueue_order(o, s));
         a.order = h->order_bwd;
     }

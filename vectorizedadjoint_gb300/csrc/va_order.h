@@ -16,6 +16,8 @@ struct OrderArgs {
     const int *prev_valid; //   and its flag (device int, 1 once written); may be null
     int *work;         // order_work_ints() scratch ints
     int *order;        // [B] output permutation, longest first
+    const int *reuse;  // backward: the forward's order, copied instead of sorting when
+                       //   that order came from counts (flag in work); may be null
 };
 
 size_t order_work_ints();
