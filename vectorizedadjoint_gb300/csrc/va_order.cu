@@ -12,11 +12,11 @@
 // of their warp.  A counting sort over 4096
 // buckets (descending) builds the permutation on the device, so it can sit
 // inside the captured graph.  The atomics here only decide the order; each
-// instance's result does not depend on it.  The backward takes the
+// instance's result does not depend on it.  The backward can take the
 // forward's order when that one came from step counts (the previous sweep's
 // attempts, nearly the same ranking as this sweep's accepted steps): no
 // second sort, and the backward then visits the checkpoint chunks in the
-// order the forward allocated them (VdP batch: 3% per gradient).
+// order the forward allocated them (the caller decides; one-thread models).
 #include <cuda_runtime.h>
 
 #include <cstdint>
