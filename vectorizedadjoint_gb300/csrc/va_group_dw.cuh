@@ -281,8 +281,10 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
             status = ST_NONFINITE;
             continue;
         }
-        if (dw_greater(err, dword(1.0f, 0.0f))) {
-            dt = decrease_dw<Tab>(dt, err);
+        const bool reject = dw_greater(err, dword(1.0f, 0.0f));
+        const dword dt_next = adjust_dw<Tab>(dt, err, reject); // groups of a warp may differ
+        if (reject) {
+            dt = dt_next;
             rej++;
             to_end = false;
             ok = false;
@@ -291,7 +293,7 @@ __global__ void __launch_bounds__(256) forward_group_dw_kernel(FwdParams a)
                 t = fixed_time(t_start, count + 1, a.dt0);
             } else {
                 t = to_end ? t1 : t + to_d_int(dt);
-                dt = increase_dw<Tab>(dt, err);
+                dt = dt_next;
             }
             y = ynew;
             if constexpr (Tab::FSAL) {

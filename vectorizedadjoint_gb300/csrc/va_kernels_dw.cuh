@@ -118,6 +118,58 @@ __host__ __device__ __forceinline__ dword inv_root_dw(dword a)
     return z;
 }
 
+// inv_root_f32<KA> (first) or inv_root_f32<KB> (!first) with the same
+// operations in the same order, without a branch: the powers are formed up
+// to the larger order and the wanted one selected, so a warp whose lanes
+// need different orders runs one evaluation instead of both.
+template <int KA, int KB>
+__host__ __device__ __forceinline__ float inv_root_f32_sel(float af, bool first)
+{
+    constexpr int KM = KA > KB ? KA : KB;
+    constexpr int32_t ca = (int32_t)(((int64_t)(KA + 1) * 0x3F800000LL) / KA);
+    constexpr int32_t cb = (int32_t)(((int64_t)(KB + 1) * 0x3F800000LL) / KB);
+    const int32_t bits = f32_bits(af);
+    float x = f32_from_bits(first ? ca - bits / KA : cb - bits / KB);
+    const float rk = first ? 1.0f / (float)KA : 1.0f / (float)KB;
+#pragma unroll
+    for (int it = 0; it < 4; it++) {
+        float pw[KM];
+        pw[0] = x;
+#pragma unroll
+        for (int k = 1; k < KM; k++)
+            pw[k] = pw[k - 1] * x;
+        const float r = fmaf(-af, first ? pw[KA - 1] : pw[KB - 1], 1.0f);
+        x = fmaf(x * r, rk, x);
+    }
+    return x;
+}
+
+// inv_root_dw<KA> (first) or inv_root_dw<KB> (!first), bit for bit, branch-free
+template <int KA, int KB>
+__host__ __device__ __forceinline__ dword inv_root_dw_sel(dword a, bool first)
+{
+    if (!(a.hi < 1e30f))
+        return dword(0.0f, 0.0f);
+    constexpr int KM = KA > KB ? KA : KB;
+    const float x = inv_root_f32_sel<KA, KB>(a.hi, first);
+    dword pw(x, 0.0f), xa = pw, xb = pw;
+#pragma unroll
+    for (int k = 1; k < KM; k++) {
+        pw = pw * x;
+        if (k == KA - 1)
+            xa = pw;
+        if (k == KB - 1)
+            xb = pw;
+    }
+    dacc r{1.0f, 0.0f};
+    dacc_fma(r, -a, first ? xa : xb);
+    const dword res = dacc_get(r);
+    const float corr = fmul_rn(fmul_rn(x, res.hi), first ? 1.0f / (float)KA : 1.0f / (float)KB);
+    dword z;
+    fast_two_sum(x, corr, z.hi, z.lo);
+    return z;
+}
+
 // odeint default_step_adjuster::decrease_step: dt * max(0.9 err^(-1/(q-1)), 0.2)
 // (fixed-step tableaux: dt unchanged; their sweeps never call it)
 template <class Tab>
@@ -146,6 +198,26 @@ __host__ __device__ __forceinline__ dword increase_dw(dword dt, dword err)
         return dt * (dword(9.0 / 10.0) * inv_root_dw<Tab::STEPPER_ORDER>(e));
     }
     return dt;
+}
+
+// decrease_dw (reject) or increase_dw (accept), bit for bit, as one
+// branch-free evaluation: the accept / reject split of a warp's lanes then
+// costs one inverse root instead of two (~6% of a VdP forward attempt).
+template <class Tab>
+__host__ __device__ __forceinline__ dword adjust_dw(dword dt, dword err, bool reject)
+{
+    if constexpr (Tab::FIXED) {
+        (void)err;
+        (void)reject;
+        return dt;
+    } else {
+        const dword fl = dword(Tab::ERR_FLOOR);
+        const dword e = reject ? err : (dw_greater(fl, err) ? fl : err);
+        const dword f = dword(9.0 / 10.0) * inv_root_dw_sel<Tab::ERROR_ORDER - 1, Tab::STEPPER_ORDER>(e, reject);
+        const dword lim = dword(1.0 / 5.0);
+        const dword scaled = dt * (reject ? (dw_greater(f, lim) ? f : lim) : f);
+        return (reject || dw_less(err, dword(0.5))) ? scaled : dt;
+    }
 }
 
 // ---------------------------------------------------------- stage algebra
@@ -541,8 +613,10 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
             status = ST_NONFINITE;
             continue;
         }
-        if (dw_greater(err, dword(1.0f, 0.0f))) {
-            dt = decrease_dw<Tab>(dt, err);
+        const bool reject = dw_greater(err, dword(1.0f, 0.0f));
+        const dword dt_next = adjust_dw<Tab>(dt, err, reject); // both branches' step, one evaluation
+        if (reject) {
+            dt = dt_next;
             rej++;
             to_end = false;
             ok = false;
@@ -553,7 +627,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
                 t = fixed_time(t_start, count + 1, a.dt0);
             } else {
                 t = to_end ? t1 : t + to_d_int(dt);
-                dt = increase_dw<Tab>(dt, err);
+                dt = dt_next;
             }
 #pragma unroll
             for (int i = 0; i < N; i++)
