@@ -61,8 +61,8 @@ def flops(model, tableau, n, attempts, accepted):
 # Double-word arithmetic is FADD-heavy (2Sum chains), so its FLOP ceiling
 # sits near half the FFMA peak.
 DW_FP32_FLOPS = {
-    ("vdp", "dopri5"): (1574.8, 1686.2),
-    ("dho", "ck54"): (1339.2, 1558.9),
+    ("vdp", "dopri5"): (1611.2, 1682.2),
+    ("dho", "ck54"): (1414.5, 1566.0),
 }
 
 
@@ -219,7 +219,7 @@ def gemm_tflops(torch, dtype, n):
 # DRAM bytes per launch of the one-thread double-word kernels on the Van der
 # Pol batch (262,144 instances), one ncu capture each: the forward writes the
 # stage records (112 B per accepted step), the backward reads them back.
-DW_TRAFFIC = {("vdpb", "forward"): 108.0e6 + 5555.8e6, ("vdpb", "backward"): 5656.3e6 + 22.5e6}
+DW_TRAFFIC = {("vdpb", "forward"): 100.6e6 + 5552.3e6, ("vdpb", "backward"): 5655.6e6 + 22.5e6}
 
 
 def roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted):
