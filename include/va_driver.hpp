@@ -12,6 +12,7 @@
 //   recordDriverRHSFunction(driver, system)        Driver.hpp:95-100
 //   adjointSolve(driver, alphas)                   backpropagation.hpp:18-43
 //   computeSensitivityMatrix(driver, alphas)       backpropagation.hpp:69-87
+//   computeSensitivityMatrixNoSIMD(driver, alphas) backpropagation.hpp:46-66
 //
 // Differences, by design: the right-hand side must be one of the built-in
 // device models (VanDerPol, VanDerPolPETSc, DampedOscillator,
@@ -270,6 +271,13 @@ template <class State> std::vector<std::vector<double>> computeSensitivityMatrix
     driver.p_lambda = pl;
     driver.p_mu = pm;
     return mu;
+}
+
+// The reference's one-cost-at-a-time variant (backpropagation.hpp:46-66):
+// the same matrix; here every seed row shares one backward sweep either way.
+template <class State> std::vector<std::vector<double>> computeSensitivityMatrixNoSIMD(Driver &driver, const State &parameters)
+{
+    return computeSensitivityMatrix(driver, parameters);
 }
 
 } // namespace vectorizedadjoint_gb300

@@ -51,6 +51,9 @@ static int run(Stepper stepper, StepperTag tag, State mu, State x0, double t1, d
     auto S = computeSensitivityMatrix(driver, mu);
     for (int i = 0; i < N; i++)
         std::printf("sens %.17g\n", S[i][0]);
+    auto S1 = computeSensitivityMatrixNoSIMD(driver, mu);
+    for (int i = 0; i < N; i++)
+        std::printf("sens1 %.17g\n", S1[i][0]);
     return 0;
 }
 

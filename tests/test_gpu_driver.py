@@ -36,6 +36,7 @@ def test_cpp_driver_matches_oracle(oracle, cuda, tmp_path, stepper, dt, observe)
     np.testing.assert_array_equal(np.array(vals["lambda"]), L)
     np.testing.assert_array_equal(np.array(vals["mu"]), M)
     np.testing.assert_array_equal(np.array(vals["sens"]).ravel(), M.ravel())
+    np.testing.assert_array_equal(np.array(vals["sens1"]).ravel(), M.ravel())
     if observe:
         # forward observer: (t_n, x_n), n = 0 .. T in order; adjoint observer:
         # (t_n, lambda_n rows), n = T .. 0 (the reference's back_prop order)
