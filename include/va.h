@@ -119,23 +119,25 @@ typedef struct {
                             from its checkpoint into scratch (bit-identical steps,
                             checked; one extra forward evaluation per step).  -1:
                             automatic -- va_forward checks the pool after the sweep
-                            (synchronously) and reruns with a 4x larger stride
-                            until the checkpoints fit (up to 1024).  Strides > 1 and
-                            -1: one-thread-per-instance models only              */
+                            (synchronously) and, if it overflowed, reruns: first
+                            without stage records, then with a 4x larger stride
+                            until the checkpoints fit (up to 1024).  Strides > 1:
+                            one-thread-per-instance models; the lane-group and
+                            shared-matrix models take -1 for its first rung only */
     int32_t block_size;  /* 0 = autotuned / default                               */
     int32_t blocks_per_sm; /* 0 = occupancy limit                                 */
     int32_t chunk_len;   /* records per checkpoint chunk (0 = 64)                 */
     int32_t schedule;    /* 0: longest instances first (forward: by the previous
                             forward's attempt counts, else by t1 - t0; backward:
                             by accepted steps), 1: index order                    */
-    int32_t stage_records; /* mixed_dw, one-thread models, every step checkpointed:
-                            1 (default) -- each record also holds the step's RK
-                            stage values and the backward sweep reads them instead
-                            of recomputing them (records of 2 + 6N doubles instead
-                            of 2 + N); 0 -- [t, dt, y] records and stage recompute,
-                            the reference's scheme.  With ckpt_stride = -1 a pool
-                            overflow first drops the stage values, then thins the
-                            checkpoints                                           */
+    int32_t stage_records; /* mixed_dw, every step checkpointed: 1 (default) --
+                            each record also holds the step's RK stage values
+                            (GLV: also their rates r + A X_m) and the backward
+                            sweep reads them instead of recomputing them (one-thread
+                            models: 2 + 6N doubles instead of 2 + N); 0 -- [t, dt, y]
+                            records and stage recompute, the reference's scheme.
+                            With ckpt_stride = -1 a pool overflow first drops the
+                            stage values, then thins the checkpoints              */
     int32_t reserved[4];
 } va_options;
 

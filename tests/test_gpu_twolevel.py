@@ -137,3 +137,34 @@ def test_ladder_drops_stage_values_first(cuda):
     np.testing.assert_array_equal(bw["dy0"].cpu().numpy()[:, 0], ref["dy0"])
     np.testing.assert_array_equal(bw["dp"].cpu().numpy()[:, 0], ref["dp"])
     s.close()
+
+
+def test_ladder_first_rung_lane_groups(cuda):
+    """GLV-10 lane groups (no two-level backward): with ckpt_stride = -1 and a
+    pool too small for stage records (2 + 12N doubles a step) but large
+    enough for [t, dt, y] records, the forward reruns without stage records;
+    the gradients are the recompute path's, bit for bit."""
+    B = 96
+    ref, _ = grads("glv10", B, precision="mixed_dw", stage_records=0)
+    w = W.make("glv10", batch=B)
+    c = w["cfg"]
+    plain = int((ref["n_acc"].sum() + 3 * B) * 12 * 8)
+    s = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision="mixed_dw", atol=c["tol"],
+               rtol=c["tol"], ckpt_stride=-1, ckpt_budget_bytes=3 * plain, chunk_len=8)
+    P = dev(w["params"])
+    s.forward(dev(w["y0"]), P, dev(w["t0"]), dev(w["t1"]))
+    bw = s.backward(P, torch.ones(B, 1, c["n"], dtype=torch.float64, device="cuda"))
+    torch.cuda.synchronize()
+    info = s.checkpoint_info()
+    assert info["stride"] == 1 and info["capacity_bytes"] <= 3 * plain
+    assert (bw["status"].cpu().numpy() == 0).all()
+    np.testing.assert_array_equal(bw["dy0"].cpu().numpy()[:, 0], ref["dy0"])
+    np.testing.assert_array_equal(bw["dp"].cpu().numpy()[:, 0], ref["dp"])
+    s.close()
+
+
+def test_strides_rejected_without_two_level(cuda):
+    with pytest.raises(Exception):
+        Solver("glv", 10, 110, 8, ckpt_stride=4)
+    with pytest.raises(Exception):
+        Solver("glv_shared", 64, 64, 8, ckpt_stride=4)

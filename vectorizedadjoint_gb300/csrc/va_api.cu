@@ -573,8 +573,10 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
         return VA_BAD_ARGS;
     // checkpoint stride: -1 automatic, 0/1 every step, k > 1 every k-th step
     // (two-level checkpointing: one-thread-per-instance models only)
+    // strides > 1 need a two-level backward (one-thread models); -1 also
+    // serves the others, whose ladder stops after dropping the stage records
     if (o.ckpt_stride < -1 ||
-        ((o.ckpt_stride > 1 || o.ckpt_stride == -1) && !(ks && ks->tpi == 1 && ks->bwd2[o.tableau][o.precision])))
+        (o.ckpt_stride > 1 && !(ks && ks->tpi == 1 && ks->bwd2[o.tableau][o.precision])))
         return VA_BAD_ARGS;
     va_handle *h = new va_handle();
     h->stride = o.ckpt_stride > 1 ? o.ckpt_stride : 1;
@@ -641,10 +643,13 @@ va_status va_forward(va_handle *h, const double *y0, const double *params, const
         if (!c.pool_fail || h->stride >= kMaxAutoStride)
             break;
         // the ladder: drop the stage values first, then thin the checkpoints
+        // (where a two-level backward exists)
         if (stages_now(h))
             h->stages_on = false;
-        else
+        else if (h->ks && h->ks->tpi == 1 && h->ks->bwd2[h->opt.tableau][h->opt.precision])
             h->stride *= 4;
+        else
+            break;
         record_layout(h);
         drop_graph(h);
     }
