@@ -61,9 +61,10 @@ typedef enum {
  * which run the reference's non-controlled loop
  * (detail/runge_kutta.hpp:37-72) with step dt0: t_n = t0 + n dt0 while
  * t_n + dt0 <= t1 (to within DBL_EPSILON), so the last record can lie short
- * of t1, as in the reference.  Fehlberg 7(8) and the fixed-step steppers are
- * compiled for the one-thread models and the per-instance GLV lane groups;
- * va_create rejects them for VA_MODEL_GLV_SHARED. */
+ * of t1, as in the reference.  Every tableau is compiled for the one-thread
+ * models and the per-instance GLV lane groups; VA_MODEL_GLV_SHARED takes the
+ * 5(4) pairs and the fixed-step steppers (va_create rejects Fehlberg 7(8),
+ * whose 13 stages do not fit the bundle sweeps' shared memory). */
 typedef enum {
     VA_TAB_DOPRI5 = 0,
     VA_TAB_CK54 = 1,

@@ -108,6 +108,44 @@ def test_fixed_trajectory_times(oracle, cuda):
     s.close()
 
 
-def test_fixed_rejected_for_shared_matrix(cuda):
+@pytest.mark.parametrize("tableau", ["rk4", "euler"])
+def test_fixed_shared_matrix(oracle, cuda, tableau):
+    """GLV with one shared A (bundle sweeps), fixed steps: FP64 per instance
+    equals the oracle bit for bit (steps, y(T), dy0, dr), dA equals the sum
+    of the oracle's per-instance dA to rounding; double-word within 1e-9."""
+    N, B, T = 64, 6, 3.0
+    rng = np.random.Generator(np.random.PCG64(17))
+    A = rng.normal(0.0, 0.5 / np.sqrt(N), (N, N))
+    A[np.arange(N), np.arange(N)] = -1.0
+    r = rng.uniform(0.5, 1.5, (B, N))
+    x0 = rng.uniform(0.1, 1.0, (B, N))
+    res = {}
+    for precision in ("fp64", "mixed_dw"):
+        s = Solver("glv_shared", N, N, B, tableau=tableau, precision=precision, dt0=DT[tableau])
+        dA = torch.empty(N, N, dtype=torch.float64, device="cuda")
+        s.set_shared(dev(A), dA)
+        out = s.gradient("sum", dev(x0), dev(r), dev(np.zeros(B)), dev(np.full(B, T)))
+        torch.cuda.synchronize()
+        res[precision] = {k: v.cpu().numpy() for k, v in out.items()}
+        res[precision]["dA"] = dA.cpu().numpy()
+        s.close()
+    r64 = res["fp64"]
+    pb = oracle.problem("glv", tableau, N, N + N * N, 1e-6, 1e-6, dt0=DT[tableau])
+    dA = np.zeros((N, N))
+    for b in range(B):
+        g = oracle.gradient(pb, "sum", x0[b], np.concatenate([r[b], A.ravel()]), 0.0, T)
+        assert int(r64["n_acc"][b]) == g["n_acc"]
+        np.testing.assert_array_equal(r64["yT"][b], g["yT"])
+        np.testing.assert_array_equal(r64["dy0"][b], g["dy0"])
+        np.testing.assert_array_equal(r64["dp"][b], g["dp"][:N])
+        dA += g["dp"][N:].reshape(N, N)
+    assert np.abs(r64["dA"] - dA).max() <= 1e-12 * np.abs(dA).max()
+    rdw = res["mixed_dw"]
+    np.testing.assert_array_equal(rdw["n_acc"], r64["n_acc"])
+    for k in ("dy0", "dp", "dA"):
+        assert np.abs(rdw[k] - r64[k]).max() <= 1e-9 * np.abs(r64[k]).max()
+
+
+def test_rkf78_rejected_for_shared_matrix(cuda):
     with pytest.raises(Exception):
-        Solver("glv_shared", 64, 64, 4, tableau="rk4")
+        Solver("glv_shared", 64, 64, 4, tableau="rkf78")

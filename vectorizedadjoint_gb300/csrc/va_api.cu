@@ -240,7 +240,7 @@ va_status ensure_buffers(va_handle *h)
         VA_CUDA(h, cudaMalloc(&h->Aw, NN * sizeof(va::dword)));
         VA_CUDA(h, cudaMalloc(&h->Atw, NN * sizeof(va::dword)));
         VA_CUDA(h, cudaMalloc(&h->dA_part, grid * NN * sizeof(double)));
-        for (int t = 0; t < 2; t++)
+        for (int t = 0; t < va::kTableaux; t++)
             for (int p = 0; p < 3; p++) {
                 const void *fns[4] = {h->bks->fwd[t][p], h->bks->fwd1[t][p], h->bks->bwd[t][p], h->bks->bwd1[t][p]};
                 for (int f = 0; f < 4; f++)

@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
     const int i = threadIdx.x;
     const int CH = a.pool.chunk_len;
 
-    double y[NB], t[NB], t1[NB], dt[NB];
+    double y[NB], t[NB], t1[NB], dt[NB], t_start[NB];
     S ys[NB], r[NB], K[NS][NB], knew[NB];
     S z0[NB];           // ST: z_0 = A y of the current state
     double *rec_cur[NB]; // ST: the current step's record
@@ -184,6 +184,7 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
             ys[b] = from_d<S>(y[b]);
             t[b] = a.t0[inst[b]];
             t1[b] = a.t1[inst[b]];
+            t_start[b] = t[b];
         }
     }
     if (i == 0) {
@@ -233,7 +234,8 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
         for (int b = 0; b < NB; b++) {
             if (!active[b] || status[b] != ST_OK || !at_top[b])
                 continue;
-            if (!(t1[b] - t[b] > kDblEps)) {
+            // fixed steps: while ((t + dt) - t1 <= eps) (runge_kutta.hpp:54)
+            if (Tab::FIXED ? !((t[b] + dt[b]) - t1[b] <= kDblEps) : !(t1[b] - t[b] > kDblEps)) {
                 // finished: write the final record, like the single-thread sweep
                 if (slot[b] == CH)
                     need_chunk = true;
@@ -293,7 +295,8 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
                 }
                 slot[b]++;
             }
-            if (status[b] != ST_OK || !(t1[b] - t[b] > kDblEps)) {
+            if (status[b] != ST_OK ||
+                (Tab::FIXED ? !((t[b] + dt[b]) - t1[b] <= kDblEps) : !(t1[b] - t[b] > kDblEps))) {
                 // instance done: outputs
                 if (__syncthreads_or(isfinite(y[b]) ? 0 : 1) && status[b] == ST_OK)
                     status[b] = ST_NONFINITE;
@@ -313,7 +316,7 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
                 active[b] = false;
                 continue;
             }
-            if ((t[b] + dt[b]) - t1[b] > kDblEps)
+            if (!Tab::FIXED && (t[b] + dt[b]) - t1[b] > kDblEps)
                 dt[b] = t1[b] - t[b];
             fails[b] = 0;
             at_top[b] = false;
@@ -431,8 +434,8 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
                 e = dt[b] * to_d(acc);
                 ratio[b] = fabs(e) / (a.atol + a.rtol * (1.0 * fabs(y[b]) + fabs(dt[b]) * fabs(to_d(K[0][b]))));
             }
-            if (!active[b] || at_top[b])
-                ratio[b] = 0.0;
+            if (!active[b] || at_top[b] || Tab::FIXED)
+                ratio[b] = 0.0; // (fixed steps: no error estimate, every attempt accepted)
         }
         bundle_max<NT, NB>(ratio, red);
         // controller, per instance (uniform across the CTA)
@@ -452,7 +455,7 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
                 rej[b]++;
                 ok = false;
             } else {
-                t[b] += dt[b];
+                t[b] = Tab::FIXED ? fixed_time(t_start[b], count[b] + 1, dt[b]) : t[b] + dt[b];
                 dt[b] = increase_step<Tab, S>(dt[b], err);
                 y[b] = ynew[b];
                 ys[b] = ynew_s[b];

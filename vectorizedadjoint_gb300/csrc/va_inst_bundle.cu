@@ -10,6 +10,20 @@ namespace va {
 void fill_fp64_bundle64(BundleKernelSet &k);
 void fill_fp64_bundle256(BundleKernelSet &k);
 
+// the fixed-step tableaux (runge_kutta4, euler): tableau slot I
+template <int NT, int I, class Tab>
+static void fill_fixed(BundleKernelSet &k)
+{
+    constexpr int NB = kBundleNB;
+    k.fwd[I][1] = (const void *)forward_bundle_kernel<NT, NB, Tab, float>;
+    k.fwd[I][2] = (const void *)forward_bundle_kernel<NT, NB, Tab, dword, true>;
+    k.fwd1[I][2] = (const void *)forward_bundle_kernel<NT, NB, Tab, dword>;
+    k.bwd[I][1] = (const void *)backward_bundle_kernel<NT, NB, Tab, float>;
+    k.bwd[I][2] = (const void *)backward_bundle_kernel<NT, NB, Tab, dword, true>;
+    k.bwd1[I][2] = (const void *)backward_bundle_kernel<NT, NB, Tab, dword>;
+    k.rs_stage[I] = bundle_stage_record_doubles(NT, Tab::S);
+}
+
 template <int NT>
 static BundleKernelSet make_bundle(void (*fill_fp64)(BundleKernelSet &))
 {
@@ -32,6 +46,8 @@ static BundleKernelSet make_bundle(void (*fill_fp64)(BundleKernelSet &))
     k.bwd1[1][2] = (const void *)backward_bundle_kernel<NT, NB, TabCK54, dword>;
     k.rs_stage[0] = bundle_stage_record_doubles(NT, TabDopri5::S);
     k.rs_stage[1] = bundle_stage_record_doubles(NT, TabCK54::S);
+    fill_fixed<NT, 3, TabRK4>(k);
+    fill_fixed<NT, 4, TabEuler>(k);
     const size_t sz[3] = {sizeof(double), sizeof(float), sizeof(dword)};
     for (int p = 0; p < 3; p++) {
         k.smem_fwd[p] = sz[p] * NT * NB + sizeof(double) * (NT / 32) * NB + sizeof(int) * NB;

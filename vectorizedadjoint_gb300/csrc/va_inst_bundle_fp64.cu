@@ -13,6 +13,10 @@ static void fill(BundleKernelSet &k)
     k.fwd[1][0] = (const void *)forward_bundle_kernel<NT, NB, TabCK54, double>;
     k.bwd[0][0] = (const void *)backward_bundle_kernel<NT, NB, TabDopri5, double>;
     k.bwd[1][0] = (const void *)backward_bundle_kernel<NT, NB, TabCK54, double>;
+    k.fwd[3][0] = (const void *)forward_bundle_kernel<NT, NB, TabRK4, double>;
+    k.bwd[3][0] = (const void *)backward_bundle_kernel<NT, NB, TabRK4, double>;
+    k.fwd[4][0] = (const void *)forward_bundle_kernel<NT, NB, TabEuler, double>;
+    k.bwd[4][0] = (const void *)backward_bundle_kernel<NT, NB, TabEuler, double>;
 }
 
 void fill_fp64_bundle64(BundleKernelSet &k) { fill<64>(k); }
