@@ -29,6 +29,18 @@ typedef struct {
     int fixed;             /* no error estimate: fixed-step loop              */
 } tableau;
 
+/* Checkpoint traffic counter of orc_gradient_traffic: the bytes the
+ * reference's StateStorage (StateStorage.hpp:4-43) stores in the forward --
+ * one time and one state per accepted (t_n, y_n), n = 0 .. T -- and the
+ * bytes the adjoint reads back per step (t_n, t_{n+1} for h_n, and y_n). */
+static __thread orc_traffic *g_traffic = NULL;
+
+static void count_store(int n)
+{
+    if (g_traffic)
+        g_traffic->store_bytes += (long long)sizeof(double) * (1 + n);
+}
+
 /* Cash-Karp 5(4): Cash & Karp (1990), the coefficients the reference reads
  * through odeint's rk54_ck_coefficients_* (ButcherTable.hpp:259-308). */
 static void tab_ck54(tableau *T)
@@ -513,6 +525,7 @@ int orc_forward(const orc_problem *pb, const double *y0, const double *p, double
             }
             times[count] = t;
             memcpy(states + (size_t)count * n, y, sizeof(double) * n);
+            count_store(n);
             if (dt_trial)
                 dt_trial[count] = dt;
             orc_rhs(pb, y, p, t, K[0]);
@@ -524,6 +537,7 @@ int orc_forward(const orc_problem *pb, const double *y0, const double *p, double
         if (status == ORC_OK) {
             times[count] = t;
             memcpy(states + (size_t)count * n, y, sizeof(double) * n);
+            count_store(n);
             for (int i = 0; i < n; i++)
                 if (!isfinite(y[i]))
                     status = ORC_NONFINITE;
@@ -544,6 +558,7 @@ int orc_forward(const orc_problem *pb, const double *y0, const double *p, double
         }
         times[count] = t;
         memcpy(states + (size_t)count * n, y, sizeof(double) * n);
+        count_store(n);
         if (dt_trial)
             dt_trial[count] = dt;
         if (less_with_sign(t1, t + dt))
@@ -596,6 +611,7 @@ int orc_forward(const orc_problem *pb, const double *y0, const double *p, double
     if (status == ORC_OK) {
         times[count] = t;
         memcpy(states + (size_t)count * n, y, sizeof(double) * n);
+        count_store(n);
         for (int i = 0; i < n; i++)
             if (!isfinite(y[i]))
                 status = ORC_NONFINITE;
@@ -711,6 +727,8 @@ int orc_adjoint_history(const orc_problem *pb, const double *p, long T, const do
         for (long k = T - 1; k >= 0; k--) {
             double tn = times[k];
             double h = times[k + 1] - times[k];
+            if (g_traffic) /* times[k], times[k + 1], y_k (GetState / GetDt) */
+                g_traffic->load_bytes += (long long)sizeof(double) * (2 + n);
             back_prop_step(pb, &tab, p, tn, h, states + (size_t)k * n, lam, alphabar, K, X, Kbar,
                            ybar, gx, gp);
             if (hq)
@@ -819,4 +837,22 @@ int orc_gradient_batch(const orc_problem *pb, int cost, long B, const double *y0
         if (created[k])
             pthread_join(th[k], NULL);
     return ORC_OK;
+}
+
+int orc_gradient_traffic(const orc_problem *pb, int cost, const double *y0, const double *p, double t0,
+                         double t1, long *n_acc, orc_traffic *traffic)
+{
+    double yT[NMAX], dy0[NMAX];
+    double *dp = (double *)malloc(sizeof(double) * (size_t)(pb->npar > 0 ? pb->npar : 1));
+    if (!dp || pb->n < 1 || pb->n > NMAX) {
+        free(dp);
+        return ORC_BAD_ARGS;
+    }
+    traffic->store_bytes = traffic->load_bytes = 0;
+    g_traffic = traffic;
+    long n_rej = 0;
+    int st = orc_gradient(pb, cost, y0, p, t0, t1, yT, dy0, dp, n_acc, &n_rej);
+    g_traffic = NULL;
+    free(dp);
+    return st;
 }

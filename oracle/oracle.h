@@ -112,6 +112,16 @@ int orc_adjoint_history(const orc_problem *pb, const double *p, long T, const do
 int orc_gradient(const orc_problem *pb, int cost, const double *y0, const double *p, double t0,
                  double t1, double *yT, double *dy0, double *dp, long *n_acc, long *n_rej);
 
+/* Checkpoint bytes of one gradient: stored by the forward sweep (a time
+ * and a state per accepted point) and read back by the adjoint sweep. */
+typedef struct {
+    long long store_bytes, load_bytes;
+} orc_traffic;
+
+/* orc_gradient that counts its checkpoint traffic into *traffic. */
+int orc_gradient_traffic(const orc_problem *pb, int cost, const double *y0, const double *p, double t0,
+                         double t1, long *n_acc, orc_traffic *traffic);
+
 /* B independent gradients over nthreads POSIX threads (static partition). */
 int orc_gradient_batch(const orc_problem *pb, int cost, long B, const double *y0, const double *p,
                        const double *t0, const double *t1, int nthreads, double *yT, double *dy0,

@@ -42,6 +42,10 @@ def build():
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
 
 
+class Traffic(ctypes.Structure):
+    _fields_ = [("store_bytes", ctypes.c_longlong), ("load_bytes", ctypes.c_longlong)]
+
+
 _lib = None
 
 
@@ -70,6 +74,9 @@ def lib():
         L.orc_gradient_batch.argtypes = [P, ctypes.c_int, ctypes.c_long, dp, dp, dp, dp,
                                          ctypes.c_int, dp, dp, dp, lp, lp, ip]
         L.orc_gradient_batch.restype = ctypes.c_int
+        L.orc_gradient_traffic.argtypes = [P, ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double, lp,
+                                           ctypes.POINTER(Traffic)]
+        L.orc_gradient_traffic.restype = ctypes.c_int
         L.orc_rhs.argtypes = [P, dp, dp, ctypes.c_double, dp]
         L.orc_vjp.argtypes = [P, dp, dp, dp, ctypes.c_double, dp, dp]
         _lib = L
@@ -147,6 +154,16 @@ def gradient(pb, cost, y0, p, t0, t1):
     st = lib().orc_gradient(ctypes.byref(pb), COST[cost], _d(y0), _d(p), t0, t1, _d(yT), _d(dy0),
                             _d(dp), ctypes.byref(na), ctypes.byref(nr))
     return dict(status=st, yT=yT, dy0=dy0, dp=dp, n_acc=na.value, n_rej=nr.value)
+
+
+def gradient_traffic(pb, cost, y0, p, t0, t1):
+    """Checkpoint bytes one gradient stores (forward) and reads back (adjoint)."""
+    na, tr = ctypes.c_long(0), Traffic()
+    y0 = np.ascontiguousarray(y0, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    st = lib().orc_gradient_traffic(ctypes.byref(pb), COST[cost], _d(y0), _d(p), t0, t1, ctypes.byref(na),
+                                    ctypes.byref(tr))
+    return dict(status=st, n_acc=na.value, store_bytes=tr.store_bytes, load_bytes=tr.load_bytes)
 
 
 def gradient_batch(pb, cost, y0, p, t0, t1, nthreads=1):

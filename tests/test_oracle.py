@@ -100,3 +100,23 @@ def test_batch_threads_equal_serial(oracle):
     b = oracle.gradient_batch(pb, "sumsq", w["y0"], w["params"], w["t0"], w["t1"], nthreads=1)
     np.testing.assert_array_equal(a["dp"], b["dp"])
     np.testing.assert_array_equal(a["n_acc"], b["n_acc"])
+
+
+@pytest.mark.parametrize("name", ["vdp1", "dho", "vdpb", "glv10"])
+def test_checkpoint_traffic_counts(oracle, name):
+    """The instrumented oracle's checkpoint bytes: the forward stores one time
+    and one state per accepted point (StateStorage.hpp:22-43, T + 1 points);
+    the adjoint reads t_n, t_{n+1} and y_n once per step
+    (detail/backpropagation.hpp:256-278) -- (1 + N) 8 and (2 + N) 8 bytes per
+    accepted step, VdP 24 and 32."""
+    w = W.make(name, batch=2)
+    c = w["cfg"]
+    n = c["n"]
+    pb = oracle.problem(c["model"], c["tableau"], n, c["npar"], c["tol"], c["tol"])
+    for b in range(2):
+        tr = oracle.gradient_traffic(pb, c["cost"], w["y0"][b], w["params"][b], 0.0, w["t1"][b])
+        g = oracle.gradient(pb, c["cost"], w["y0"][b], w["params"][b], 0.0, w["t1"][b])
+        T = g["n_acc"]
+        assert tr["status"] == 0 and tr["n_acc"] == T > 0
+        assert tr["store_bytes"] == (T + 1) * (1 + n) * 8
+        assert tr["load_bytes"] == T * (2 + n) * 8
