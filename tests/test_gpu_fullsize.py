@@ -1,0 +1,119 @@
+"""The benchmark's full-size workloads (VdP batch 262,144; DHO 65,536;
+GLV-10 16,384; GLV-256 1,024 with the shared A) through properties that do
+not depend on the batch size:
+
+- every instance finishes (status OK);
+- an instance's result does not depend on the batch around it or on the
+  sweep's schedule: the batch reversed gives the same bits per instance (the
+  longest-first order, the chunk pool and the work counters all change);
+- a sample of instances, the longest among them, matches the oracle: FP64
+  bit for bit, double-word within the reduced-precision bound (1e-6 of the
+  instance's gradient scale; 1e-5 for the damped oscillators);
+- the shared-matrix dA of the whole batch equals the sum of the two halves'
+  dA to rounding, 1e-10 of its largest entry (dA is linear in the instances)."""
+import numpy as np
+import pytest
+import torch
+
+from vectorizedadjoint_gb300 import Solver
+from vectorizedadjoint_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+WORST = {"vdpb": 1e-6, "dho": 1e-5, "glv10": 1e-6}
+
+
+def dev(a):
+    return torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def gradient(c, precision, y0, params, t0, t1, shared=None):
+    B = y0.shape[0]
+    kw = {"ckpt_budget_bytes": c["budget"]} if "budget" in c else {}
+    s = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision=precision, atol=c["tol"],
+               rtol=c["tol"], **kw)
+    dA = None
+    if shared is not None:
+        dA = torch.empty(c["n"], c["n"], dtype=torch.float64, device="cuda")
+        s.set_shared(dev(shared), dA)
+    out = s.gradient(c["cost"], dev(y0), dev(params), dev(t0), dev(t1))
+    torch.cuda.synchronize()
+    res = {k: v.cpu().numpy() for k, v in out.items()}
+    if dA is not None:
+        res["dA"] = dA.cpu().numpy()
+    s.close()
+    return res
+
+
+def full(name, precision, reverse=False):
+    w = W.make(name)
+    sl = slice(None, None, -1) if reverse else slice(None)
+    r = gradient(w["cfg"], precision, w["y0"][sl], w["params"][sl], w["t0"][sl], w["t1"][sl], w["shared"])
+    if reverse:
+        r = {k: (v if k == "dA" else v[::-1]) for k, v in r.items()}
+    return w, r
+
+
+def sample(r, B, k=24):
+    idx = set(np.linspace(0, B - 1, k).astype(int).tolist())
+    idx.add(int(np.argmax(r["n_acc"])))
+    return sorted(idx)
+
+
+def rel(a, b, floor):
+    return float(np.max(np.abs(a - b)) / max(np.abs(b).max(), floor, 1e-300))
+
+
+@pytest.mark.parametrize("name", ["vdpb", "dho", "glv10"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed_dw"])
+def test_full_batch(oracle, cuda, name, precision):
+    w, r = full(name, precision)
+    c = w["cfg"]
+    assert (r["status"] == 0).all()
+    _, rr = full(name, precision, reverse=True)
+    for k in ("yT", "dy0", "dp", "n_acc"):
+        np.testing.assert_array_equal(rr[k], r[k], err_msg=k)
+    pb = oracle.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"])
+    errs = []
+    for b in sample(r, c["batch"]):
+        g = oracle.gradient(pb, c["cost"], w["y0"][b], w["params"][b], w["t0"][b], w["t1"][b])
+        assert g["status"] == 0
+        if precision == "fp64":
+            assert int(r["n_acc"][b]) == g["n_acc"]
+            np.testing.assert_array_equal(r["dy0"][b], g["dy0"])
+            np.testing.assert_array_equal(r["dp"][b], g["dp"])
+        else:
+            got = np.concatenate([r["dy0"][b], r["dp"][b]])
+            ref = np.concatenate([g["dy0"], g["dp"]])
+            errs.append(rel(got, ref, 1e-8 * np.abs(w["y0"][b]).max()))
+    if errs:
+        assert max(errs) <= WORST[name], (np.median(errs), max(errs))
+
+
+def test_glv256_full_batch(oracle, cuda):
+    """GLV N=256 with the shared A, 1,024 instances, double-word: per-instance
+    results independent of the batch order, the whole batch's dA the sum of
+    its halves' dA, and two instances (the longest among them) within 1e-6
+    of the oracle's FP64 gradient (dy0, dr)."""
+    w, r = full("glv256", "mixed_dw")
+    c = w["cfg"]
+    B, N = c["batch"], c["n"]
+    assert (r["status"] == 0).all()
+    _, rr = full("glv256", "mixed_dw", reverse=True)
+    for k in ("yT", "dy0", "dp", "n_acc"):
+        np.testing.assert_array_equal(rr[k], r[k], err_msg=k)
+    scale = np.abs(r["dA"]).max()
+    assert np.abs(rr["dA"] - r["dA"]).max() <= 1e-10 * scale
+    h = B // 2
+    parts = [gradient(c, "mixed_dw", w["y0"][sl], w["params"][sl], w["t0"][sl], w["t1"][sl], w["shared"])
+             for sl in (slice(0, h), slice(h, B))]
+    np.testing.assert_array_equal(np.concatenate([p["dy0"] for p in parts]), r["dy0"])
+    assert np.abs(parts[0]["dA"] + parts[1]["dA"] - r["dA"]).max() <= 1e-10 * scale
+    pb = oracle.problem("glv", "dopri5", N, N + N * N, c["tol"], c["tol"])
+    for b in (0, int(np.argmax(r["n_acc"]))):
+        p = np.concatenate([w["params"][b], w["shared"].ravel()])
+        g = oracle.gradient(pb, c["cost"], w["y0"][b], p, w["t0"][b], w["t1"][b])
+        assert g["status"] == 0
+        got = np.concatenate([r["dy0"][b], r["dp"][b]])
+        ref = np.concatenate([g["dy0"], g["dp"][:N]])
+        assert rel(got, ref, 0.0) <= 1e-6
