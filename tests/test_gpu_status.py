@@ -97,3 +97,22 @@ def test_backward_before_forward(cuda):
     with pytest.raises(VaError) as e:
         s.backward(p, lam)
     assert e.value.code == NOT_READY
+
+
+def test_pool_allocation_failure_is_clean(cuda):
+    """A checkpoint pool larger than the device (a 1 TiB budget against a
+    worst case of several TB) fails to allocate: va_gradient returns
+    VA_CUDA_ERROR with the allocation's message on every call (the half-built
+    handle is released, never run), and a handle of ordinary size then runs."""
+    from vectorizedadjoint_gb300 import _lib
+
+    B = 65536
+    w = W.make("vdpb", batch=B)
+    s = Solver("vdp", 2, 1, B, ckpt_budget_bytes=1 << 40)
+    for _ in range(2):
+        with pytest.raises(_lib.VaError) as e:
+            grads(s, w)
+        assert "cudaMalloc" in str(e.value)
+    s.close()
+    r = grads(Solver("vdp", 2, 1, 64), W.make("vdpb", batch=64))
+    assert (r["status"] == 0).all()

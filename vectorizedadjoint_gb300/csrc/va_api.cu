@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <string>
 #include <vector>
 
@@ -94,6 +95,9 @@ struct va_handle {
     double *shared_dA = nullptr;
     double *At = nullptr, *dA_part = nullptr;
     va::dword *Aw = nullptr, *Atw = nullptr;
+
+    bool buffers_ready = false; // ensure_buffers / ensure_staging completed
+    bool staging_ready = false;
 };
 
 namespace {
@@ -194,10 +198,21 @@ int scratch_record_doubles(const va_handle *h)
     return va::record_doubles_for(h->ks, h->opt.tableau, h->opt.precision, 1, h->N, true);
 }
 
-va_status ensure_buffers(va_handle *h)
+// Frees each buffer of a failed all-or-nothing allocation and clears its
+// pointer, so that the next call allocates again instead of running on a
+// half-built handle.
+void release(std::initializer_list<void **> ptrs)
 {
-    if (h->pool_rec)
-        return VA_OK;
+    for (void **p : ptrs) {
+        if (*p)
+            cudaFree(*p);
+        *p = nullptr;
+    }
+    (void)cudaGetLastError(); // the failed allocation's error is reported, not left for the next launch check
+}
+
+va_status alloc_buffers(va_handle *h)
+{
     const int B = h->prob.batch;
     // the pool is sized for the largest record layout of the handle; the
     // chunk links for the smallest (most chunks)
@@ -252,6 +267,23 @@ va_status ensure_buffers(va_handle *h)
     return VA_OK;
 }
 
+va_status ensure_buffers(va_handle *h)
+{
+    if (h->buffers_ready)
+        return VA_OK;
+    const va_status st = alloc_buffers(h);
+    if (st != VA_OK) {
+        release({(void **)&h->pool_rec, (void **)&h->chunk_prev, (void **)&h->inst_T, (void **)&h->inst_last,
+                 (void **)&h->inst_status, (void **)&h->ctl, (void **)&h->inst_t1, (void **)&h->inst_t0,
+                 (void **)&h->order_fwd, (void **)&h->order_bwd, (void **)&h->order_work, (void **)&h->inst_work,
+                 (void **)&h->At, (void **)&h->Aw, (void **)&h->Atw, (void **)&h->dA_part});
+        h->pool_bytes = 0;
+        return st;
+    }
+    h->buffers_ready = true;
+    return VA_OK;
+}
+
 va::BundleParams bundle_params(va_handle *h)
 {
     va::BundleParams bp{};
@@ -294,10 +326,8 @@ va_status ensure_scratch(va_handle *h)
     return VA_OK;
 }
 
-va_status ensure_staging(va_handle *h)
+va_status alloc_staging(va_handle *h)
 {
-    if (h->s_y0)
-        return VA_OK;
     const size_t B = h->prob.batch, N = h->N, P = h->P, Q = h->prob.nout;
     VA_CUDA(h, cudaMalloc(&h->s_y0, B * N * sizeof(double)));
     VA_CUDA(h, cudaMalloc(&h->s_par, B * P * sizeof(double)));
@@ -311,6 +341,21 @@ va_status ensure_staging(va_handle *h)
     VA_CUDA(h, cudaMalloc(&h->s_nrej, B * sizeof(int)));
     VA_CUDA(h, cudaMalloc(&h->s_lam, B * Q * N * sizeof(double)));
     VA_CUDA(h, cudaMalloc(&h->s_mu, B * Q * P * sizeof(double)));
+    return VA_OK;
+}
+
+va_status ensure_staging(va_handle *h)
+{
+    if (h->staging_ready)
+        return VA_OK;
+    const va_status st = alloc_staging(h);
+    if (st != VA_OK) {
+        release({(void **)&h->s_y0, (void **)&h->s_par, (void **)&h->s_t0, (void **)&h->s_t1, (void **)&h->s_yT,
+                 (void **)&h->s_dy0, (void **)&h->s_dpar, (void **)&h->s_nacc, (void **)&h->s_status,
+                 (void **)&h->s_nrej, (void **)&h->s_lam, (void **)&h->s_mu});
+        return st;
+    }
+    h->staging_ready = true;
     return VA_OK;
 }
 
