@@ -250,7 +250,8 @@ va_status alloc_buffers(va_handle *h)
     }
     if (h->bks) {
         const size_t NN = (size_t)h->N * h->N;
-        const size_t grid = ((size_t)B + h->bks->nb - 1) / h->bks->nb;
+        const int nb = std::min({h->bks->nb[0], h->bks->nb[1], h->bks->nb[2]}); // the most CTAs
+        const size_t grid = ((size_t)B + nb - 1) / nb;
         VA_CUDA(h, cudaMalloc(&h->At, NN * sizeof(double)));
         VA_CUDA(h, cudaMalloc(&h->Aw, NN * sizeof(va::dword)));
         VA_CUDA(h, cudaMalloc(&h->Atw, NN * sizeof(va::dword)));
@@ -292,11 +293,15 @@ va::BundleParams bundle_params(va_handle *h)
     bp.Aw = h->Aw;
     bp.Atw = h->Atw;
     bp.dA_part = h->dA_part;
-    bp.nb = h->bks->nb;
+    bp.nb = h->bks->nb[h->opt.precision];
     return bp;
 }
 
-int bundle_grid(va_handle *h) { return (h->prob.batch + h->bks->nb - 1) / h->bks->nb; }
+int bundle_grid(va_handle *h)
+{
+    const int nb = h->bks->nb[h->opt.precision];
+    return (h->prob.batch + nb - 1) / nb;
+}
 
 // Two-level backward launch: 64-thread blocks, at most 4 per SM, so the
 // re-integration scratch stays (stride + 1) records x 256 threads per SM.

@@ -140,8 +140,10 @@ __device__ __forceinline__ void bundle_matvec(const double *Mt, const dword *Mtw
 
 // ------------------------------------------------------------ forward sweep
 
+// bundles of two: two CTAs per SM (128 registers per thread); larger
+// bundles: no minimum (0), the compiler's own register choice
 template <int NT, int NB, class Tab, class S, bool STAGES = false>
-__global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
+__global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(BundleParams bp)
 {
     constexpr int NS = Tab::S;
     constexpr bool ST = STAGES && std::is_same<S, dword>::value; // stage records
@@ -499,8 +501,10 @@ __global__ void __launch_bounds__(NT) forward_bundle_kernel(BundleParams bp)
 
 // ----------------------------------------------------------- backward sweep
 
+// bundles of two: two CTAs per SM (128 registers per thread); larger
+// bundles: no minimum (0), the compiler's own register choice
 template <int NT, int NB, class Tab, class S, bool STAGES = false>
-__global__ void __launch_bounds__(NT) backward_bundle_kernel(BundleParams bp)
+__global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel(BundleParams bp)
 {
     constexpr int NS = Tab::S;
     constexpr bool ST = STAGES && std::is_same<S, dword>::value; // stage records

@@ -1,4 +1,5 @@
-// Shared-matrix GLV bundle kernels (N = 64, 256; 4 instances per CTA):
+// Shared-matrix GLV bundle kernels (N = 64, 256; 4 instances per CTA, 2 in
+// the double-word sweeps):
 // reduced-precision sweeps (double-word: with and without stage records) and
 // the helper kernels.  FP64 sweeps come from
 // va_inst_bundle_fp64.cu, built without FMA contraction.
@@ -14,44 +15,46 @@ void fill_fp64_bundle256(BundleKernelSet &k);
 template <int NT, int I, class Tab>
 static void fill_fixed(BundleKernelSet &k)
 {
-    constexpr int NB = kBundleNB;
+    constexpr int NB = kBundleNB, NW = kBundleNBdw;
     k.fwd[I][1] = (const void *)forward_bundle_kernel<NT, NB, Tab, float>;
-    k.fwd[I][2] = (const void *)forward_bundle_kernel<NT, NB, Tab, dword, true>;
-    k.fwd1[I][2] = (const void *)forward_bundle_kernel<NT, NB, Tab, dword>;
+    k.fwd[I][2] = (const void *)forward_bundle_kernel<NT, NW, Tab, dword, true>;
+    k.fwd1[I][2] = (const void *)forward_bundle_kernel<NT, NW, Tab, dword>;
     k.bwd[I][1] = (const void *)backward_bundle_kernel<NT, NB, Tab, float>;
-    k.bwd[I][2] = (const void *)backward_bundle_kernel<NT, NB, Tab, dword, true>;
-    k.bwd1[I][2] = (const void *)backward_bundle_kernel<NT, NB, Tab, dword>;
+    k.bwd[I][2] = (const void *)backward_bundle_kernel<NT, NW, Tab, dword, true>;
+    k.bwd1[I][2] = (const void *)backward_bundle_kernel<NT, NW, Tab, dword>;
     k.rs_stage[I] = bundle_stage_record_doubles(NT, Tab::S);
 }
 
 template <int NT>
 static BundleKernelSet make_bundle(void (*fill_fp64)(BundleKernelSet &))
 {
-    constexpr int NB = kBundleNB;
+    constexpr int NB = kBundleNB, NW = kBundleNBdw;
     BundleKernelSet k{};
     k.N = NT;
-    k.nb = NB;
+    k.nb[0] = k.nb[1] = NB;
+    k.nb[2] = NW;
     fill_fp64(k);
     k.fwd[0][1] = (const void *)forward_bundle_kernel<NT, NB, TabDopri5, float>;
-    k.fwd[0][2] = (const void *)forward_bundle_kernel<NT, NB, TabDopri5, dword, true>;
-    k.fwd1[0][2] = (const void *)forward_bundle_kernel<NT, NB, TabDopri5, dword>;
+    k.fwd[0][2] = (const void *)forward_bundle_kernel<NT, NW, TabDopri5, dword, true>;
+    k.fwd1[0][2] = (const void *)forward_bundle_kernel<NT, NW, TabDopri5, dword>;
     k.fwd[1][1] = (const void *)forward_bundle_kernel<NT, NB, TabCK54, float>;
-    k.fwd[1][2] = (const void *)forward_bundle_kernel<NT, NB, TabCK54, dword, true>;
-    k.fwd1[1][2] = (const void *)forward_bundle_kernel<NT, NB, TabCK54, dword>;
+    k.fwd[1][2] = (const void *)forward_bundle_kernel<NT, NW, TabCK54, dword, true>;
+    k.fwd1[1][2] = (const void *)forward_bundle_kernel<NT, NW, TabCK54, dword>;
     k.bwd[0][1] = (const void *)backward_bundle_kernel<NT, NB, TabDopri5, float>;
-    k.bwd[0][2] = (const void *)backward_bundle_kernel<NT, NB, TabDopri5, dword, true>;
-    k.bwd1[0][2] = (const void *)backward_bundle_kernel<NT, NB, TabDopri5, dword>;
+    k.bwd[0][2] = (const void *)backward_bundle_kernel<NT, NW, TabDopri5, dword, true>;
+    k.bwd1[0][2] = (const void *)backward_bundle_kernel<NT, NW, TabDopri5, dword>;
     k.bwd[1][1] = (const void *)backward_bundle_kernel<NT, NB, TabCK54, float>;
-    k.bwd[1][2] = (const void *)backward_bundle_kernel<NT, NB, TabCK54, dword, true>;
-    k.bwd1[1][2] = (const void *)backward_bundle_kernel<NT, NB, TabCK54, dword>;
+    k.bwd[1][2] = (const void *)backward_bundle_kernel<NT, NW, TabCK54, dword, true>;
+    k.bwd1[1][2] = (const void *)backward_bundle_kernel<NT, NW, TabCK54, dword>;
     k.rs_stage[0] = bundle_stage_record_doubles(NT, TabDopri5::S);
     k.rs_stage[1] = bundle_stage_record_doubles(NT, TabCK54::S);
     fill_fixed<NT, 3, TabRK4>(k);
     fill_fixed<NT, 4, TabEuler>(k);
     const size_t sz[3] = {sizeof(double), sizeof(float), sizeof(dword)};
     for (int p = 0; p < 3; p++) {
-        k.smem_fwd[p] = sz[p] * NT * NB + sizeof(double) * (NT / 32) * NB + sizeof(int) * NB;
-        k.smem_bwd[p] = 3 * sz[p] * (size_t)TabDopri5::S * NT * NB;
+        const size_t nb = k.nb[p];
+        k.smem_fwd[p] = sz[p] * NT * nb + sizeof(double) * (NT / 32) * nb + sizeof(int) * nb;
+        k.smem_bwd[p] = 3 * sz[p] * (size_t)TabDopri5::S * NT * nb;
     }
     k.prepare = (const void *)prepare_A_kernel<NT>;
     k.reduce = (const void *)reduce_dA_kernel<NT>;

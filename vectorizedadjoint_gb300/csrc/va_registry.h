@@ -58,10 +58,15 @@ void fill_fixed_decay(KernelSet &k);
 void fill_fixed_glv5(KernelSet &k);
 void fill_fixed_glv10(KernelSet &k);
 
-// Shared-matrix GLV: bundles of kBundleNB instances per CTA of N threads.
+// Shared-matrix GLV: bundles of kBundleNB instances per CTA of N threads
+// (FP64, FP32); the double-word sweeps take bundles of kBundleNBdw, whose
+// 128 registers per thread let two CTAs share an SM (GLV-256: 8% faster
+// than one CTA of 4; the FP32 sweeps measured 38% slower so).
 constexpr int kBundleNB = 4;
+constexpr int kBundleNBdw = 2;
 struct BundleKernelSet {
-    int N, nb;
+    int N;
+    int nb[3];                     // instances per CTA, per precision
     const void *fwd[kTableaux][3]; // __global__ void(BundleParams), blockDim = N (mixed_dw: stage records)
     const void *bwd[kTableaux][3];
     const void *fwd1[kTableaux][3]; // mixed_dw sweeps over [t, dt, y] records (stage records off); null: fwd
