@@ -704,11 +704,14 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel(Bu
 #pragma unroll
                 for (int b = 0; b < NB; b++)
                     vi[m][b] = vall[((size_t)m * NT + i) * NB + b];
-            for (int jj = 0; jj < NT; jj++) {
-                if constexpr (std::is_same<S, dword>::value) {
-                    // the partial stays a double-word (packed in the 8-byte
-                    // slot): accumulating it in FP64 cost four FP64-pipe
-                    // operations per element and step
+            if constexpr (std::is_same<S, dword>::value) {
+                // the partial stays a double-word (packed in the 8-byte
+                // slot): accumulating it in FP64 cost four FP64-pipe
+                // operations per element and step.  Eight rows per
+                // iteration keep eight partial loads in flight (the
+                // partials of all CTAs exceed L2: DRAM latency)
+#pragma unroll 8
+                for (int jj = 0; jj < NT; jj++) {
                     dacc acc{0.0f, 0.0f};
 #pragma unroll
                     for (int m = NS - 1; m >= 0; m--)
@@ -717,7 +720,9 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel(Bu
                             dacc_fma(acc, vi[m][b], xall[((size_t)m * NT + jj) * NB + b]);
                     double &pe = part[(size_t)jj * NT + i];
                     pe = dw_pack(dw_unpack(pe) + dacc_get(acc));
-                } else {
+                }
+            } else {
+                for (int jj = 0; jj < NT; jj++) {
                     S acc = S(0);
 #pragma unroll
                     for (int m = NS - 1; m >= 0; m--)
