@@ -95,8 +95,8 @@ __device__ __forceinline__ void bundle_max(double (&v)[NB], double *red /* [NT/3
 // consecutive addresses).  One pass over the matrix serves all NB vectors.
 // (Double-word path: the dot products run through the compensated
 // accumulator dacc, ~12 FP32 operations per term.)  UNR: matrix rows in
-// flight per thread (the loads come from L2; measured at N = 256: 16 rows
-// suit the forward, 8 the backward, which holds more registers).
+// flight per thread (the loads come from L2; measured at N = 256 with
+// bundles of 2: 16 rows suit both sweeps, 32 slowed the forward by 12%).
 template <int NT, int NB, class S, int UNR = 8>
 __device__ __forceinline__ void bundle_matvec_acc(const double *Mt, const dword *Mtw,
                                                   const S *xs /* [NT][NB] */, S (&z)[NB])
@@ -671,7 +671,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel(Bu
 #pragma unroll
             for (int b = 0; b < NB; b++)
                 g_all[b] = Kbar[m][b] * (r[b] + zall[((size_t)m * NT + i) * NB + b]);
-            bundle_matvec_acc<NT, NB, S>(bp.A, bp.Aw, vall + (size_t)m * NT * NB, g_all);
+            bundle_matvec_acc<NT, NB, S, 16>(bp.A, bp.Aw, vall + (size_t)m * NT * NB, g_all);
 #pragma unroll
             for (int b = 0; b < NB; b++) {
                 if (!step[b])
