@@ -162,9 +162,13 @@ def run_reference(args, rank, world):
     cb["value"] = v
     print(json.dumps({
         "impl": "reference", "metric": "adjoint gradients/s", "value": v, "unit": "gradients/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        # one step = one pass over the whole batch, at the bounded sample's rate
+        "ms_per_step": 1e3 * c["batch"] / v,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded PCG64)", "config": {"workload": args.config, "batch": c["batch"]},
+        "data": "synthetic (seeded PCG64)",
+        "config": {"workload": f"{args.config}: {c['model']} B={c['batch']} {c['tableau']} tol={c['tol']}",
+                   "batch": c["batch"], "cost": c["cost"]},
         "cpu_baseline": cb, "e2e": {"value": v, "unit": "gradients/s", "h2d_bytes_per_step": 0,
                                     "d2h_bytes_per_step": 0}}), flush=True)
 
