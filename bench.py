@@ -55,14 +55,17 @@ def flops(model, tableau, n, attempts, accepted):
 
 # FP32 FLOPs the double-word sweeps execute per forward attempt and per
 # backward step (FADD + FMUL + 2 FFMA, thread level), counted by ncu on the
-# one-thread-per-instance kernels at the named workload's acceptance ratio
+# double-word sweep kernels at the named workload's acceptance ratio
 # (profiles/forward_kernel_dw_vdpb.md, profiles/backward_kernel_dw_vdpb.md,
-# profiles/dw_kernels_dho.md), stage records on.
+# profiles/dw_kernels_dho.md, profiles/group_kernels_glv10.md,
+# profiles/bundle_kernels_glv256.md; per instance), stage records on.
 # Double-word arithmetic is FADD-heavy (2Sum chains), so its FLOP ceiling
 # sits near half the FFMA peak.
 DW_FP32_FLOPS = {
     ("vdp", "dopri5"): (1611.2, 1682.2),
     ("dho", "ck54"): (1414.5, 1566.0),
+    ("glv", "dopri5"): (16898.1, 25416.7),
+    ("glv_shared", "dopri5"): (6353397.4, 13211627.4),
 }
 
 
