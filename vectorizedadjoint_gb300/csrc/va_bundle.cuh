@@ -96,7 +96,8 @@ __device__ __forceinline__ void bundle_max(double (&v)[NB], double *red /* [NT/3
 // (Double-word path: the dot products run through the compensated
 // accumulator dacc, ~12 FP32 operations per term.)  UNR: matrix rows in
 // flight per thread (the loads come from L2; measured at N = 256 with
-// bundles of 2: 16 rows suit both sweeps, 32 slowed the forward by 12%).
+// bundles of 2: 16 rows suit both sweeps; 8 slowed the forward by 3%, 32
+// by 12%).
 template <int NT, int NB, class S, int UNR = 8>
 __device__ __forceinline__ void bundle_matvec_acc(const double *Mt, const dword *Mtw,
                                                   const S *xs /* [NT][NB] */, S (&z)[NB])
