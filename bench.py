@@ -54,11 +54,10 @@ def flops(model, tableau, n, attempts, accepted):
 
 
 # FP32 FLOPs the double-word sweeps execute per forward attempt and per
-# backward step (FADD + FMUL + 2 FFMA, thread level), counted by ncu on the
-# double-word sweep kernels at the named workload's acceptance ratio
-# (profiles/forward_kernel_dw_vdpb.md, profiles/backward_kernel_dw_vdpb.md,
-# profiles/dw_kernels_dho.md, profiles/group_kernels_glv10.md,
-# profiles/bundle_kernels_glv256.md; per instance), stage records on.
+# backward step (FADD + FMUL + 2 FFMA, thread level), counted by ncu
+# (smsp__sass_thread_inst_executed_op_f{add,mul,fma}_pred_on) on the
+# double-word sweep kernels at the named workload's acceptance ratio, per
+# instance, stage records on.
 # Double-word arithmetic is FADD-heavy (2Sum chains), so its FLOP ceiling
 # sits near half the FFMA peak.
 DW_FP32_FLOPS = {
@@ -119,7 +118,8 @@ class Clocks:
 
 
 def cpu_baseline(cfg_name, w, seconds=10.0, threads=None):
-    """The oracle's multi-threaded batch gradient on a bounded sample."""
+    """The oracle's multi-threaded batch gradient on a bounded sample, with the
+    C library's pow in the step-size controller, as the reference calls it."""
     from oracle import oracle_py as O
     c = w["cfg"]
     threads = threads or os.cpu_count() or 1
@@ -128,10 +128,10 @@ def cpu_baseline(cfg_name, w, seconds=10.0, threads=None):
     if w["shared"] is not None:
         # per instance the reference's GLV layout: r, then the (common) A
         A = np.asarray(w["shared"]).ravel()
-        pb = O.problem("glv", c["tableau"], c["n"], c["n"] + c["n"] ** 2, c["tol"], c["tol"])
+        pb = O.problem("glv", c["tableau"], c["n"], c["n"] + c["n"] ** 2, c["tol"], c["tol"], pow_mode=1)
         params = lambda k: np.concatenate([w["params"][:k], np.broadcast_to(A, (k, A.size))], axis=1)
     else:
-        pb = O.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"])
+        pb = O.problem(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], c["tol"], pow_mode=1)
         params = (lambda k, P=params: P[:k])
     pilot = min(B, (64 if c["n"] <= 16 else 1) * threads)
     t0 = time.perf_counter()
@@ -229,6 +229,22 @@ def gemm_tflops(torch, dtype, n):
 DW_TRAFFIC = {("vdpb", "forward"): 100.6e6 + 5552.3e6, ("vdpb", "backward"): 5655.6e6 + 22.5e6}
 
 
+def pipe_rates():
+    """This GPU's arithmetic pipe rates from the library's probes
+    (va_probe_rate): FP64 FMA, FP32 FMA and FP64 tensor-core MMA, TFLOP/s."""
+    import ctypes
+
+    from vectorizedadjoint_gb300 import _lib
+    L = _lib.load()
+    out = {}
+    for kind, name, iters in [(0, "fp64_fma", 4096), (1, "fp32_fma", 65536), (2, "fp64_mma_m8n8k4", 2048),
+                              (3, "fp64_mma_m16n8k16", 512)]:
+        tf, ms = ctypes.c_double(), ctypes.c_double()
+        st = L.va_probe_rate(kind, iters, ctypes.byref(tf), ctypes.byref(ms))
+        out[name] = tf.value if st == 0 else None
+    return out
+
+
 def roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted):
     """Roofline of the dominant sweep kernel.  fp64: algorithmic FP64 FLOPs
     against cuBLAS DGEMM.  mixed_dw: the FP32 FLOPs the double-word
@@ -283,6 +299,10 @@ def main():
                     help="with --quick: pick the launch shape by the autotune sweep first, as the full run does")
     ap.add_argument("--batch", type=int, default=0, help="override the workload's batch size")
     ap.add_argument("--budget-gb", type=float, default=0.0, help="checkpoint pool budget (GiB)")
+    ap.add_argument("--step-pow", type=int, default=1, choices=[0, 1],
+                    help="FP64 controller: 1 correctly rounded step factor (default), 0 Newton root")
+    ap.add_argument("--probe", action="store_true",
+                    help="print this GPU's FP64 / FP32 / FP64-MMA pipe rates as one JSON line and exit")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", 0))
@@ -295,6 +315,10 @@ def main():
     import torch.distributed as dist
 
     torch.cuda.set_device(local)
+    if args.probe:
+        if rank == 0:
+            print(json.dumps({"pipe_rates_tflops": pipe_rates(), "gpu": torch.cuda.get_device_name(local)}))
+        return
     if world > 1:
         dist.init_process_group("nccl")
     # a non-default stream, so va_gradient captures both sweeps in one CUDA graph
@@ -318,9 +342,9 @@ def _bench(args, rank, world, local, torch, dist):
     y0, par, t0, t1 = dev(w["y0"]), dev(w["params"]), dev(w["t0"]), dev(w["t1"])
     shared = dev(w["shared"]) if w["shared"] is not None else None
 
-    def make_solver(batch, precision, budget=c.get("budget", 0)):
+    def make_solver(batch, precision, budget=c.get("budget", 0), step_pow=args.step_pow):
         sv = Solver(c["model"], c["n"], c["npar"], batch, tableau=c["tableau"], precision=precision,
-                    atol=c["tol"], rtol=c["tol"], ckpt_budget_bytes=budget)
+                    atol=c["tol"], rtol=c["tol"], ckpt_budget_bytes=budget, step_pow=step_pow)
         if shared is not None:
             sv.set_shared(shared, torch.empty_like(shared))
         return sv
@@ -359,6 +383,7 @@ def _bench(args, rank, world, local, torch, dist):
         if rank == 0:
             print(json.dumps({"metric": "adjoint gradients/s", "value": value, "unit": "gradients/s",
                               "ms_per_step": ms, "quick": True, "precision": args.precision,
+                              "step_pow": args.step_pow,
                               "config": {"workload": args.config, "batch": B, "launch": s.launch()},
                               "status_ok": int((status == 0).sum()), "clocks": clk.summary()}), flush=True)
         s.close()
@@ -392,8 +417,8 @@ def _bench(args, rank, world, local, torch, dist):
     roofline = roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted)
 
     # the other precision modes on the same batch: throughput and gradient error vs FP64
-    def run_mode(precision):
-        sm = make_solver(B, precision)
+    def run_mode(precision, step_pow=args.step_pow):
+        sm = make_solver(B, precision, step_pow=step_pow)
         sm.autotune(c["cost"], y0, par, t0, t1)
         o = sm.gradient(c["cost"], y0, par, t0, t1)
         tt = []
@@ -432,6 +457,9 @@ def _bench(args, rank, world, local, torch, dist):
         if other not in modes:
             v, o = run_mode(other)
             modes[other] = {"gradients_per_s": v, "grad_err_vs_fp64": grad_err(o, o64)}
+    # FP64 with the other step-factor power (Newton root <-> correctly rounded)
+    v, o = run_mode("fp64", step_pow=1 - args.step_pow)
+    modes["fp64_step_pow%d" % (1 - args.step_pow)] = {"gradients_per_s": v, "grad_err_vs_fp64": grad_err(o, o64)}
     err = modes[args.precision].get("grad_err_vs_fp64")
 
     # plain drop-in: the FP64 path called once per instance through the host entry point

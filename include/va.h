@@ -51,9 +51,16 @@ typedef enum {
                                per instance (examples/GeneralizedLotkaVolterra/main.cpp:105-119);
                                npar = n + n*n                                            */
     VA_MODEL_DECAY = 4,     /* y'=-k y;                              n=1, npar=1        */
-    VA_MODEL_GLV_SHARED = 5 /* GLV with one A shared by the batch; per-instance
+    VA_MODEL_GLV_SHARED = 5, /* GLV with one A shared by the batch; per-instance
                                params = r[n]; shared params = A[n][n]                   */
+    VA_MODEL_USER = 6       /* a device model compiled by the caller (include/va_model.cuh,
+                               VA_DEFINE_MODEL), passed to va_create_model               */
 } va_model;
+
+/* Kernel table of a device model compiled outside the library: the struct
+ * that VA_DEFINE_MODEL (include/va_model.cuh) builds in the caller's nvcc
+ * translation unit and returns from the function it defines.  Opaque here. */
+typedef struct va_model_kernels va_model_kernels;
 
 /* Embedded pairs (ButcherTable.hpp:259-308 for Cash-Karp, :191-246 for
  * Fehlberg 7(8); Dormand-Prince is added from the published tableau) and
@@ -139,11 +146,20 @@ typedef struct {
                             records and stage recompute, the reference's scheme.
                             With ckpt_stride = -1 a pool overflow first drops the
                             stage values, then thins the checkpoints              */
-    int32_t reserved[4];
+    int32_t step_pow;    /* FP64 step-size controller (odeint default_step_adjuster,
+                            called from detail/runge_kutta.hpp:103-107): 1 (default)
+                            -- the factors pow(err, -1.0/(q-1)) and pow(err, -1.0/p)
+                            correctly rounded, i.e. what odeint's std::pow gives
+                            wherever the host libm rounds correctly, so the sweep
+                            takes the reference's accepted steps; 0 -- Newton's
+                            inverse root (a few ulps off, ~25% cheaper per attempt).
+                            The reduced precisions keep their own controllers     */
+    int32_t reserved[3];
 } va_options;
 
 /* Fills the reference's defaults: DOPRI5, FP64, atol=rtol=1e-6, dt0=1e-3,
- * max_rejects=500 (odeint failed_step_checker), max_steps=1000000. */
+ * max_rejects=500 (odeint failed_step_checker), max_steps=1000000, and the
+ * correctly rounded step factor (step_pow = 1). */
 VA_API va_status va_default_options(va_options *opt);
 
 /* Replaces Driver(Nin, Nout, Npar) (Driver.hpp:39-42) together with
@@ -151,6 +167,17 @@ VA_API va_status va_default_options(va_options *opt);
  * recordDriverRHSFunction (Driver.hpp:95-100): the model id stands for the
  * recorded RHS, opt->tableau for the tableau. */
 VA_API va_status va_create(const va_problem *prob, const va_options *opt, va_handle **out);
+
+/* va_create for a model the caller compiled (prob->model = VA_MODEL_USER):
+ * replaces recordDriverRHSFunction (Driver.hpp:95-100, which tapes any
+ * templated functor through AadData::Record, AadData.hpp:124-171) for device
+ * code.  `model` is what the function defined by VA_DEFINE_MODEL returns;
+ * prob->n and prob->npar must equal the model's N and P.  The tableaux and
+ * precisions are those the model was instantiated for; the handle keeps the
+ * pointer, which must outlive it.  VA_BAD_ARGS for a table built from
+ * another version of the sweep templates. */
+VA_API va_status va_create_model(const va_problem *prob, const va_options *opt, const va_model_kernels *model,
+                                 va_handle **out);
 
 /* Replaces delete_driver_handle (Driver.hpp:81-85). */
 VA_API va_status va_destroy(va_handle *h);
@@ -229,6 +256,22 @@ VA_API va_status va_gradient_noalloc(int32_t model, int32_t tableau, int32_t pre
                                      const double *t1, double *yT, double *dy0, double *dparams,
                                      int32_t *n_acc, int32_t *status, void *stream);
 
+/* Frozen-step replay of the handle's model and tableau in FP64: for each of
+ * `count` lanes, integrates from y0[lane] with params[lane] over the given
+ * accepted-step sequence, h_n = t_{n+1} - t_n with t_n =
+ * times[lane][n], n = 0..n_steps[lane], no step-size control, and writes
+ * y(T) to yT[lane].  This is the map whose exact derivative the backward
+ * sweep computes (the reference's back_prop_step,
+ * detail/backpropagation.hpp:83-158, differentiates it with step sizes
+ * frozen): central differences of it check va_backward on the GPU.  All
+ * arrays are DEVICE arrays: times[count][times_stride], n_steps[count],
+ * y0[count][n], params[count][npar], yT[count][n].  `shared` (may be NULL):
+ * the matrix A of VA_MODEL_GLV_SHARED for this call (NULL: the one of
+ * va_set_shared).  Times come from va_trajectory of a forward sweep. */
+VA_API va_status va_forward_frozen(va_handle *h, int32_t count, int32_t times_stride, const double *times,
+                                   const int32_t *n_steps, const double *y0, const double *params,
+                                   const double *shared, double *yT, void *stream);
+
 /* Picks the block size and resident blocks per SM of both sweeps by timing
  * candidate launches on the given inputs (device pointers); the choice is
  * kept in the handle.  Runs forward+backward several times. */
@@ -281,6 +324,12 @@ VA_API va_status va_adjoint_history_buffer(const va_handle *h, double **buf, int
  * has no shared-parameter batch; per instance this is its GLV parameter
  * layout (examples/GeneralizedLotkaVolterra/main.cpp:105-119) with A common. */
 VA_API va_status va_set_shared(va_handle *h, const double *A, double *dA);
+
+/* Step factors of the last forward sweep whose correctly rounded value could
+ * not be decided at double-double precision (Ziv's rounding test failed;
+ * expected ~2^-42 per factor, so 0 in practice); such a factor is the
+ * nearest rounding of a value within 2^-98 of the power.  Synchronous. */
+VA_API va_status va_step_pow_undecided(va_handle *h, int64_t *count);
 
 /* Message of the last failing call on this handle ("" if none). */
 VA_API const char *va_last_error(const va_handle *h);

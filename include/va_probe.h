@@ -1,0 +1,31 @@
+/*
+ * va_probe.h -- arithmetic-rate probes of libva_gb300.so.
+ *
+ * No counterpart in the reference, which has no GPU path: these measure the
+ * pipes the sweep kernels run on (FP64 vector FMA, FP32 FMA, FP64
+ * tensor-core MMA) on the current device, so that the roofline fractions the
+ * benchmark reports rest on this part's own rates.
+ */
+#ifndef VA_GB300_PROBE_H
+#define VA_GB300_PROBE_H
+
+#include <stdint.h>
+
+#include "va.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* kind 0: FP64 FMA, 1: FP32 FMA, 2: FP64 MMA m8n8k4 (mma.sync), 3: FP64 MMA
+ * m16n8k16 (mma.sync).  Runs `iters` iterations of eight independent chains
+ * per thread (or warp) on 8 blocks of 256 threads per SM of the current
+ * device, best of three timed launches; writes TFLOP/s (FMA = 2 FLOPs) and
+ * the launch time in ms (ms_out may be NULL).  Allocates a small output
+ * buffer.  Returns a va_status. */
+VA_API int32_t va_probe_rate(int32_t kind, int32_t iters, double *tflops, double *ms_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

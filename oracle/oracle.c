@@ -5,6 +5,9 @@
  * the operation order of the reference / Boost.odeint expressions.
  */
 #include "oracle.h"
+#if !(defined(__aarch64__) || (defined(__LDBL_MANT_DIG__) && __LDBL_MANT_DIG__ == 113))
+#include <quadmath.h>
+#endif
 
 #include <float.h>
 #include <stdint.h>
@@ -434,17 +437,63 @@ static double error_norm(const orc_problem *pb, const double *x, const double *d
     return m;
 }
 
+/* pow(a, -1.0/k) correctly rounded: the power evaluated in binary128
+ * (113-bit significand; the C library's powl where long double is binary128,
+ * as on aarch64 Linux, else GCC's libquadmath powq, both accurate to about an
+ * ulp of binary128) and rounded once to double.  The rounding to double can
+ * only differ from the correctly rounded result when the exact power lies
+ * within ~2^-110 of a midpoint between doubles (probability ~2^-57 per
+ * call).  Independent of the CUDA library's double-double evaluation, which
+ * it checks. */
+static double cr_pow_q(double a, double y)
+{
+#if defined(__aarch64__) || (defined(__LDBL_MANT_DIG__) && __LDBL_MANT_DIG__ == 113)
+    return (double)powl((long double)a, (long double)y);
+#else
+    return (double)powq((__float128)a, (__float128)y);
+#endif
+}
+
 /* err^(-1/k).  pow_mode 1: the C library's pow, as odeint calls std::pow.
- * pow_mode 0: a fixed IEEE-only scheme -- Newton's iteration for the inverse
- * k-th root x <- x + x (1 - a x^k) / k from a seed read off the float bit
- * pattern (exponent field scaled by -1/k), four FP32 steps then two FP64
- * steps -- whose result is the same bits on every IEEE machine, so step
- * sequences can be compared bit for bit with the CUDA library, which uses
- * the same scheme.  The two modes differ in the last bit of some factors. */
+ * pow_mode 2: the correctly rounded pow (cr_pow_q), what a correctly rounded
+ * libm returns; the CUDA library's reference-parity controller computes the
+ * same values.  pow_mode 0: a fixed IEEE-only scheme -- Newton's iteration
+ * for the inverse k-th root x <- x + x (1 - a x^k) / k from a seed read off
+ * the float bit pattern (exponent field scaled by -1/k), four FP32 steps then
+ * two FP64 steps -- whose result is the same bits on every IEEE machine, so
+ * step sequences can be compared bit for bit with the CUDA library's fast
+ * controller, which uses the same scheme.  The modes differ in the last bit
+ * of some factors (libm against correctly rounded: ~0.1% of calls with
+ * glibc 2.39). */
+/* pow trace of the calling thread (orc_set_powtrace): libm pow calls, and
+ * those whose result is not the correctly rounded one */
+static __thread orc_powtrace *g_pow = NULL;
+
+void orc_set_powtrace(orc_powtrace *tr)
+{
+    g_pow = tr;
+    if (tr) {
+        tr->calls = tr->noncr = tr->step = 0;
+        tr->first_noncr_step = -1;
+        tr->first_noncr_arg = 0.0;
+    }
+}
+
 static double inv_root(double a, int k, int pow_mode)
 {
-    if (pow_mode == 1)
-        return pow(a, -1.0 / k);
+    if (pow_mode == 1) {
+        const double r = pow(a, -1.0 / k);
+        if (g_pow) {
+            g_pow->calls++;
+            if (a < 1e30 && r != cr_pow_q(a, -1.0 / k) && g_pow->noncr++ == 0) {
+                g_pow->first_noncr_step = g_pow->step;
+                g_pow->first_noncr_arg = a;
+            }
+        }
+        return r;
+    }
+    if (pow_mode == 2)
+        return a < 1e30 ? cr_pow_q(a, -1.0 / k) : 0.0;
     if (!(a < 1e30))
         return 0.0;
     float af = (float)a;
@@ -472,6 +521,8 @@ static double inv_root(double a, int k, int pow_mode)
     }
     return xd;
 }
+
+double orc_step_pow(double a, int k, int pow_mode) { return inv_root(a, k, pow_mode); }
 
 /* default_step_adjuster::decrease_step / increase_step */
 static double decrease_step(double dt, double err, int error_order, int pow_mode)
@@ -561,6 +612,8 @@ int orc_forward(const orc_problem *pb, const double *y0, const double *p, double
         count_store(n);
         if (dt_trial)
             dt_trial[count] = dt;
+        if (g_pow)
+            g_pow->step = count;
         if (less_with_sign(t1, t + dt))
             dt = t1 - t;
         int fails = 0;

@@ -76,10 +76,27 @@ typedef struct {
     double dt0;    /* initial step                            */
     long max_steps;/* accepted-step capacity                  */
     int max_fail;  /* consecutive failed attempts (odeint 500) */
-    int pow_mode;  /* step-size factor err^(-1/k): 0 = fixed IEEE-only Newton
-                      scheme shared with the CUDA library (bit-comparable),
-                      1 = the C library's pow (as odeint's std::pow) */
+    int pow_mode;  /* step-size factor err^(-1.0/k): 0 = fixed IEEE-only Newton
+                      scheme shared with the CUDA library's fast controller
+                      (bit-comparable), 1 = the C library's pow (as odeint's
+                      std::pow), 2 = the correctly rounded pow (binary128
+                      evaluation rounded once; the CUDA library's
+                      reference-parity controller gives the same values) */
 } orc_problem;
+
+/* Trace of the C library's pow in pow_mode 1: calls, calls whose result is
+ * not the correctly rounded power (checked against the binary128 value), and
+ * the accepted-step index and argument of the first such call (-1, 0: none).
+ * orc_set_powtrace(tr) zeroes *tr and traces the calling thread's later
+ * forward sweeps into it; NULL stops tracing. */
+typedef struct {
+    long calls, noncr, first_noncr_step, step;
+    double first_noncr_arg;
+} orc_powtrace;
+void orc_set_powtrace(orc_powtrace *tr);
+
+/* The step-size factor pow(a, -1.0/k) in the given pow_mode (a >= 1e30: 0). */
+double orc_step_pow(double a, int k, int pow_mode);
 
 /* Right-hand side and vector-Jacobian product of the built-in models. */
 void orc_rhs(const orc_problem *pb, const double *x, const double *p, double t, double *f);

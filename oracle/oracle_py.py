@@ -42,6 +42,11 @@ def build():
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
 
 
+class PowTrace(ctypes.Structure):
+    _fields_ = [("calls", ctypes.c_long), ("noncr", ctypes.c_long), ("first_noncr_step", ctypes.c_long),
+                ("step", ctypes.c_long), ("first_noncr_arg", ctypes.c_double)]
+
+
 class Traffic(ctypes.Structure):
     _fields_ = [("store_bytes", ctypes.c_longlong), ("load_bytes", ctypes.c_longlong)]
 
@@ -77,6 +82,10 @@ def lib():
         L.orc_gradient_traffic.argtypes = [P, ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double, lp,
                                            ctypes.POINTER(Traffic)]
         L.orc_gradient_traffic.restype = ctypes.c_int
+        L.orc_set_powtrace.argtypes = [ctypes.POINTER(PowTrace)]
+        L.orc_set_powtrace.restype = None
+        L.orc_step_pow.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.orc_step_pow.restype = ctypes.c_double
         L.orc_rhs.argtypes = [P, dp, dp, ctypes.c_double, dp]
         L.orc_vjp.argtypes = [P, dp, dp, dp, ctypes.c_double, dp, dp]
         _lib = L
@@ -87,14 +96,24 @@ def _d(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-def problem(model, tableau, n, npar, atol, rtol, dt0=1e-3, max_steps=200000, max_fail=500, pow_mode=0):
-    """pow_mode 0: the IEEE-only step-factor power shared with the CUDA library
-    (bit-comparable step sequences); 1: the C library's pow, as odeint calls it."""
+def problem(model, tableau, n, npar, atol, rtol, dt0=1e-3, max_steps=200000, max_fail=500, pow_mode=2):
+    """Step-factor power pow(err, -1.0/k): pow_mode 2 (default) the correctly
+    rounded value, what the CUDA library's FP64 controller computes by
+    default (step_pow = 1); 1: the C library's pow, as odeint calls it; 0: the
+    Newton root of the library's fast controller (step_pow = 0)."""
     return Problem(MODEL[model], TABLEAU[tableau], n, npar, atol, rtol, dt0, max_steps, max_fail, pow_mode)
 
 
-def forward(pb, y0, p, t0, t1, cap=None):
-    """Returns dict(status, times[T+1], states[T+1,n], dt_trial[T], yT, n_acc, n_rej)."""
+def step_pow(a, k, pow_mode):
+    """The oracle's step factor pow(a, -1.0/k) in the given mode."""
+    return lib().orc_step_pow(float(a), int(k), int(pow_mode))
+
+
+def forward(pb, y0, p, t0, t1, cap=None, powtrace=False):
+    """Returns dict(status, times[T+1], states[T+1,n], dt_trial[T], yT, n_acc, n_rej).
+    powtrace (pow_mode 1): also pow_calls, pow_noncr (libm results that are not
+    correctly rounded) and first_noncr_step (accepted-step index of the first
+    such call, -1 if none)."""
     cap = cap or pb.max_steps
     n = pb.n
     times = np.zeros(cap + 1)
@@ -104,11 +123,22 @@ def forward(pb, y0, p, t0, t1, cap=None):
     na, nr = ctypes.c_long(0), ctypes.c_long(0)
     y0 = np.ascontiguousarray(y0, dtype=np.float64)
     p = np.ascontiguousarray(p, dtype=np.float64)
-    st = lib().orc_forward(ctypes.byref(pb), _d(y0), _d(p), t0, t1, cap, _d(times), _d(states),
-                           _d(dtt), _d(yT), ctypes.byref(na), ctypes.byref(nr))
+    tr = PowTrace()
+    if powtrace:
+        lib().orc_set_powtrace(ctypes.byref(tr))
+    try:
+        st = lib().orc_forward(ctypes.byref(pb), _d(y0), _d(p), t0, t1, cap, _d(times), _d(states),
+                               _d(dtt), _d(yT), ctypes.byref(na), ctypes.byref(nr))
+    finally:
+        if powtrace:
+            lib().orc_set_powtrace(None)
     T = na.value
-    return dict(status=st, times=times[:T + 1].copy(), states=states[:T + 1].copy(),
-                dt_trial=dtt[:T].copy(), yT=yT, n_acc=T, n_rej=nr.value)
+    out = dict(status=st, times=times[:T + 1].copy(), states=states[:T + 1].copy(),
+               dt_trial=dtt[:T].copy(), yT=yT, n_acc=T, n_rej=nr.value)
+    if powtrace:
+        out.update(pow_calls=tr.calls, pow_noncr=tr.noncr, first_noncr_step=tr.first_noncr_step,
+                   first_noncr_arg=tr.first_noncr_arg)
+    return out
 
 
 def forward_frozen(pb, y0, p, times):

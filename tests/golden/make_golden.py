@@ -2,8 +2,16 @@
 its unchanged lib/include headers compiled against the project's Boost
 stand-in and linked with the AADC runtime it ships (oracle/ref/, built into
 oracle/_ref/libvaref.so by `make -C oracle/ref`).  Needs the reference
-sources at /root/reference and an x86-64 host (AADC is x86-only); the
-fixtures it writes are committed so the tests run anywhere.
+sources (directory from $VA_REFERENCE_DIR, default /root/reference) and an
+x86-64 host (AADC is x86-only); the fixtures it writes are committed so the
+tests run anywhere.
+
+Every case stores the reference's accepted-step record (times, states) when
+it has at most 5000 steps, and the trace of the C library's pow over the
+same forward sweep, taken with the oracle in its libm mode (which lands on
+the reference's steps bit for bit, so it makes the same pow calls): the
+number of calls and of calls whose result was not the correctly rounded
+power on the machine that generated the fixtures.
 
 Cases: seeded instances of every benchmark configuration (same draws as
 vectorizedadjoint_gb300.workloads), and the reference's own GLV example
@@ -25,9 +33,30 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
-REF = "/root/reference"
+REF = os.environ.get("VA_REFERENCE_DIR", "/root/reference")
 
+from oracle import oracle_py as O  # noqa: E402
 from vectorizedadjoint_gb300 import workloads as W  # noqa: E402
+
+MAX_STORED_STEPS = 5000
+
+
+def pow_trace(model, tableau, n, npar, tol, y0, p, t1, dt, first=False):
+    """libm pow calls of the forward sweep and how many were not correctly
+    rounded (with first=True also the accepted-step index of the first)."""
+    pb = O.problem(model, tableau, n, npar, tol, tol, dt0=dt, pow_mode=1)
+    fw = O.forward(pb, y0, p, 0.0, t1, powtrace=True)
+    if first:
+        return fw["pow_calls"], fw["pow_noncr"], fw["first_noncr_step"]
+    return fw["pow_calls"], fw["pow_noncr"]
+
+
+def differs_with_cr_pow(model, tableau, n, npar, tol, y0, p, t1, dt):
+    """Whether the correctly rounded step factor changes the accepted steps."""
+    f1 = O.forward(O.problem(model, tableau, n, npar, tol, tol, dt0=dt, pow_mode=1), y0, p, 0.0, t1)
+    f2 = O.forward(O.problem(model, tableau, n, npar, tol, tol, dt0=dt, pow_mode=2), y0, p, 0.0, t1)
+    return not (f1["n_acc"] == f2["n_acc"] and np.array_equal(f1["states"], f2["states"])
+                and np.array_equal(f1["times"], f2["times"]))
 
 MODEL_ID = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3}
 TABLEAU_ID = {"dopri5": 0, "ck54": 1, "rkf78": 2, "rk4": 3, "euler": 4}
@@ -131,10 +160,38 @@ def main():
             lam = (2.0 * yT if c["cost"] == "sumsq" else np.ones(c["n"]))[None, :]
             T, times, states, yT, lo, mo = solve(L, c["model"], c["tableau"], c["n"], c["npar"], c["tol"], y0, p,
                                                  t1, lam, mu, dt=dt)
+            keep = T <= MAX_STORED_STEPS
+            calls, noncr = pow_trace(c["model"], c["tableau"], c["n"], c["npar"], c["tol"], y0, p, t1, dt)
             cases.append(dict(name=f"{name}[{b}]", model=c["model"], tableau=c["tableau"], n=c["n"],
                               npar=c["npar"], tol=c["tol"], dt=dt, y0=y0, p=p, t1=t1, lam=lam, mu=mu, T=T, yT=yT,
-                              dy0=lo, dp=mo, times=times if name == "vdp1" else None,
-                              states=states if name == "vdp1" else None))
+                              dy0=lo, dp=mo, times=times if keep else None, states=states if keep else None,
+                              pow_calls=calls, pow_noncr=noncr))
+    # instances of the Van der Pol and damped-oscillator batches on which the
+    # C library's pow returns a value that is not the correctly rounded power
+    # and the accepted steps change because of it: the first two of each
+    for name in ("vdpb", "dho"):
+        w = W.make(name, batch=600)
+        c = w["cfg"]
+        found = 0
+        for b in range(600):
+            y0, p, t1 = w["y0"][b], w["params"][b], float(w["t1"][b])
+            args = (c["model"], c["tableau"], c["n"], c["npar"], c["tol"], y0, p, t1, 1e-3)
+            calls, noncr, first = pow_trace(*args, first=True)
+            if noncr == 0 or not differs_with_cr_pow(*args):
+                continue
+            mu = np.zeros((1, c["npar"]))
+            T, times, states, yT, _, _ = solve(L, c["model"], c["tableau"], c["n"], c["npar"], c["tol"], y0, p, t1,
+                                               np.zeros((1, c["n"])), mu)
+            lam = (2.0 * yT if c["cost"] == "sumsq" else np.ones(c["n"]))[None, :]
+            T, times, states, yT, lo, mo = solve(L, c["model"], c["tableau"], c["n"], c["npar"], c["tol"], y0, p,
+                                                 t1, lam, mu)
+            cases.append(dict(name=f"{name}_libm_noncr[{b}]", model=c["model"], tableau=c["tableau"], n=c["n"],
+                              npar=c["npar"], tol=c["tol"], dt=1e-3, y0=y0, p=p, t1=t1, lam=lam, mu=mu, T=T,
+                              yT=yT, dy0=lo, dp=mo, times=times, states=states, pow_calls=calls, pow_noncr=noncr,
+                              first_noncr_step=first))
+            found += 1
+            if found == 2:
+                break
     # the reference's GLV example on its own data, identity seeds (Nout = N)
     for N in (5, 10):
         vals = np.array([float(v) for v in open(f"{REF}/examples/GeneralizedLotkaVolterra/data/N{N}/alphasfile_cpp.csv")
@@ -144,9 +201,10 @@ def main():
         lam, mu = np.eye(N), np.zeros((N, N + N * N))
         for tol in (1e-6, 1e-9):
             T, times, states, yT, lo, mo = solve(L, "glv", "ck54", N, N + N * N, tol, y0, vals, 10.0, lam, mu)
+            calls, noncr = pow_trace("glv", "ck54", N, N + N * N, tol, y0, vals, 10.0, 1e-3)
             cases.append(dict(name=f"glv_example_N{N}_tol{tol:g}", model="glv", tableau="ck54", n=N,
                               npar=N + N * N, tol=tol, dt=1e-3, y0=y0, p=vals, t1=10.0, lam=lam, mu=mu, T=T, yT=yT,
-                              dy0=lo, dp=mo, times=None, states=None))
+                              dy0=lo, dp=mo, times=times, states=states, pow_calls=calls, pow_noncr=noncr))
     out = {}
     for k, cs in enumerate(cases):
         for key, v in cs.items():

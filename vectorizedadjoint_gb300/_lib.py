@@ -14,7 +14,7 @@ STATUS_NAMES = {0: "VA_OK", 1: "VA_MAX_REJECTS", 2: "VA_MAX_STEPS", 3: "VA_NONFI
                 4: "VA_CKPT_BUDGET", 5: "VA_BAD_ARGS", 6: "VA_CUDA_ERROR", 7: "VA_NOT_READY",
                 8: "VA_RECOMPUTE_MISMATCH", 9: "VA_NOT_RUN"}
 
-MODELS = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3, "decay": 4, "glv_shared": 5}
+MODELS = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3, "decay": 4, "glv_shared": 5, "user": 6}
 TABLEAUX = {"dopri5": 0, "ck54": 1, "rkf78": 2, "rk4": 3, "euler": 4}
 PRECISIONS = {"fp64": 0, "mixed": 1, "mixed_dw": 2}
 COSTS = {"seeds": -1, "sumsq": 0, "sum": 1}
@@ -25,7 +25,8 @@ EXPORTS = ["va_default_options", "va_create", "va_destroy", "va_forward", "va_ba
            "va_autotune",
            "va_get_launch", "va_checkpoint_info",
            "va_trajectory", "va_set_adjoint_history", "va_adjoint_history", "va_adjoint_history_buffer",
-           "va_set_shared", "va_last_error", "va_status_string"]
+           "va_set_shared", "va_last_error", "va_status_string", "va_probe_rate",
+           "va_step_pow_undecided", "va_create_model", "va_forward_frozen"]
 
 
 class VaProblem(ctypes.Structure):
@@ -40,7 +41,8 @@ class VaOptions(ctypes.Structure):
                 ("ckpt_budget_bytes", ctypes.c_int64), ("ckpt_stride", ctypes.c_int32),
                 ("block_size", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("chunk_len", ctypes.c_int32), ("schedule", ctypes.c_int32),
-                ("stage_records", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
+                ("stage_records", ctypes.c_int32), ("step_pow", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 3)]
 
 
 class VaError(RuntimeError):
@@ -89,6 +91,12 @@ def load():
     L.va_last_error.restype = ctypes.c_char_p
     L.va_status_string.argtypes = [ctypes.c_int32]
     L.va_status_string.restype = ctypes.c_char_p
+    L.va_create_model.argtypes = [ctypes.POINTER(VaProblem), ctypes.POINTER(VaOptions), ctypes.c_void_p,
+                                  ctypes.POINTER(H)]
+    L.va_forward_frozen.argtypes = [H, ctypes.c_int32, ctypes.c_int32, dp, ip, dp, dp, dp, dp, vp]
+    L.va_step_pow_undecided.argtypes = [H, ctypes.POINTER(ctypes.c_int64)]
+    L.va_probe_rate.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
+                                ctypes.POINTER(ctypes.c_double)]
     for name in EXPORTS:
         f = getattr(L, name)
         if f.restype is ctypes.c_int:  # default restype

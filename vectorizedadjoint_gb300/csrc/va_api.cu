@@ -17,6 +17,7 @@
 #include "va_kernels.cuh"
 #include "va_order.h"
 #include "va_registry.h"
+#include "va_replay.cuh"
 
 namespace {
 
@@ -47,6 +48,7 @@ struct va_handle {
     int device = 0;
     int sm_count = 0;
     const va::KernelSet *ks = nullptr;
+    const va::ModelKernels *user = nullptr; // a device model compiled outside the library
     int N = 0, P = 0;
     int RS = 0; // doubles per checkpoint record at the current stride (record_layout)
     bool stages_on = true; // opt.stage_records, cleared by the automatic checkpoint ladder
@@ -145,10 +147,20 @@ const va::KernelSet *kernel_set(const va_problem &p)
     }
 }
 
-int grid_for(va_handle *h, const void *fn, int block, int instances)
+// Resident blocks per SM of a sweep kernel: a model compiled outside the
+// library answers through its own runtime (its kernels are registered there).
+int occupancy_of(const va_handle *h, const void *fn, int block)
 {
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, block, 0) != cudaSuccess || occ < 1)
+    const cudaError_t e = h->user ? h->user->occupancy(&occ, fn, block, 0)
+                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, block, 0);
+    return e == cudaSuccess ? occ : 0;
+}
+
+int grid_for(va_handle *h, const void *fn, int block, int instances)
+{
+    int occ = occupancy_of(h, fn, block);
+    if (occ < 1)
         occ = 1;
     int bps = h->opt.blocks_per_sm > 0 ? std::min(h->opt.blocks_per_sm, occ) : occ;
     long need = ((long)instances * h->ks->tpi + block - 1) / block;
@@ -374,10 +386,15 @@ va::Pool pool_of(va_handle *h)
     return p;
 }
 
-cudaError_t launch(const void *fn, int grid, int block, void *params, cudaStream_t s)
+// Launches a sweep kernel of the handle's model with one parameter block;
+// kernels of a model compiled outside the library go through its launcher.
+cudaError_t launch(const va_handle *h, const void *fn, int grid, int block, void *params, cudaStream_t s,
+                   size_t smem = 0)
 {
+    if (h->user)
+        return h->user->launch(fn, (unsigned)grid, (unsigned)block, params, smem, s);
     void *args[] = {params};
-    return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, 0, s);
+    return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, s);
 }
 
 va_status enqueue_forward(va_handle *h, const double *y0, const double *params, const double *t0,
@@ -395,6 +412,7 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
     a.dt0 = h->opt.dt0;
     a.max_steps = h->opt.max_steps;
     a.max_fail = h->opt.max_rejects;
+    a.step_pow = h->opt.step_pow;
     a.yT = yT;
     a.n_acc_out = n_acc;
     a.n_rej_out = n_rej;
@@ -438,7 +456,7 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
         a.work_valid = h->inst_work + a.B;
     }
     VA_CUDA(h, cudaMemsetAsync(h->ctl, 0, sizeof(va::Control), s));
-    VA_CUDA(h, launch(fn, h->fwd_grid, h->fwd_block, &a, s));
+    VA_CUDA(h, launch(h, fn, h->fwd_grid, h->fwd_block, &a, s));
     return VA_OK;
 }
 
@@ -505,8 +523,9 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
         a.rtol = h->opt.rtol;
         a.dt0 = h->opt.dt0;
         a.max_fail = h->opt.max_rejects;
+        a.step_pow = h->opt.step_pow;
         VA_CUDA(h, cudaMemsetAsync(&h->ctl->adj_next, 0, sizeof(unsigned int), s));
-        VA_CUDA(h, launch(h->ks->bwd2[h->opt.tableau][h->opt.precision], two_level_grid(h), kTwoLevelBlock, &a, s));
+        VA_CUDA(h, launch(h, h->ks->bwd2[h->opt.tableau][h->opt.precision], two_level_grid(h), kTwoLevelBlock, &a, s));
         return VA_OK;
     }
     const void *fn = h->ks->bwd[h->opt.tableau][h->opt.precision];
@@ -515,7 +534,82 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
     if (h->bwd_grid <= 0)
         h->bwd_grid = grid_for(h, fn, h->bwd_block, a.B);
     VA_CUDA(h, cudaMemsetAsync(&h->ctl->adj_next, 0, sizeof(unsigned int), s));
-    VA_CUDA(h, launch(fn, h->bwd_grid, h->bwd_block, &a, s));
+    VA_CUDA(h, launch(h, fn, h->bwd_grid, h->bwd_block, &a, s));
+    return VA_OK;
+}
+
+// CUDA events of one autotune sweep, destroyed on every return path
+struct AutotuneEvents {
+    cudaEvent_t e[3] = {nullptr, nullptr, nullptr};
+    ~AutotuneEvents()
+    {
+        for (cudaEvent_t x : e)
+            if (x)
+                cudaEventDestroy(x);
+    }
+};
+
+// Times every (block size, resident blocks per SM) candidate of both sweeps
+// and leaves the best of each in the handle.
+va_status autotune_sweep(va_handle *h, int32_t cost, const double *y0, const double *params,
+                         const double *t0, const double *t1, cudaStream_t s, AutotuneEvents &ev)
+{
+    const void *ffn = h->ks->fwd[h->opt.tableau][h->opt.precision];
+    const void *bfn = h->ks->bwd[h->opt.tableau][h->opt.precision];
+    for (cudaEvent_t &x : ev.e)
+        VA_CUDA(h, cudaEventCreate(&x));
+    cudaEvent_t e0 = ev.e[0], e1 = ev.e[1], e2 = ev.e[2];
+    float best_f = 1e30f, best_b = 1e30f;
+    int bf_block = h->fwd_block, bf_grid = h->fwd_grid, bb_block = h->bwd_block, bb_grid = h->bwd_grid;
+    const int blocks[] = {64, 128, 256};
+    for (int blk : blocks) {
+        const int occf = occupancy_of(h, ffn, blk), occb = occupancy_of(h, bfn, blk);
+        // every resident-block count: the best differs between the sweeps and
+        // between workloads (stage-record traffic favours fewer warps in the
+        // backward, issue rate more in the forward)
+        const int maxocc = std::max(1, std::max(occf, occb));
+        for (int bps = 1; bps <= maxocc; bps++) {
+            h->fwd_block = h->bwd_block = blk;
+            long need = ((long)h->prob.batch * h->ks->tpi + blk - 1) / blk;
+            h->fwd_grid = (int)std::max(1L, std::min((long)h->sm_count * std::min(bps, std::max(occf, 1)), need));
+            h->bwd_grid = (int)std::max(1L, std::min((long)h->sm_count * std::min(bps, std::max(occb, 1)), need));
+            // a warm-up run, then the best of two timed runs
+            float cand_f = 1e30f, cand_b = 1e30f;
+            for (int rep = 0; rep < 3; rep++) {
+                VA_CUDA(h, cudaEventRecord(e0, s));
+                va_status st = enqueue_forward(h, y0, params, t0, t1, h->s_yT, nullptr, nullptr, h->s_status, s);
+                if (st != VA_OK)
+                    return st;
+                VA_CUDA(h, cudaEventRecord(e1, s));
+                st = enqueue_backward(h, params, nullptr, nullptr, cost, h->s_dy0, h->s_dpar, h->s_status, s);
+                if (st != VA_OK)
+                    return st;
+                VA_CUDA(h, cudaEventRecord(e2, s));
+                VA_CUDA(h, cudaEventSynchronize(e2));
+                float tf = 0, tb = 0;
+                VA_CUDA(h, cudaEventElapsedTime(&tf, e0, e1));
+                VA_CUDA(h, cudaEventElapsedTime(&tb, e1, e2));
+                if (rep > 0) {
+                    cand_f = std::min(cand_f, tf);
+                    cand_b = std::min(cand_b, tb);
+                }
+            }
+            if (cand_f < best_f) {
+                best_f = cand_f;
+                bf_block = blk;
+                bf_grid = h->fwd_grid;
+            }
+            if (cand_b < best_b) {
+                best_b = cand_b;
+                bb_block = blk;
+                bb_grid = h->bwd_grid;
+            }
+        }
+    }
+    h->fwd_block = bf_block;
+    h->fwd_grid = bf_grid;
+    h->bwd_block = bb_block;
+    h->bwd_grid = bb_grid;
     return VA_OK;
 }
 
@@ -562,6 +656,19 @@ const char *va_status_string(int32_t s)
 
 const char *va_last_error(const va_handle *h) { return h ? h->err.c_str() : "null handle"; }
 
+va_status va_step_pow_undecided(va_handle *h, int64_t *count)
+{
+    if (!h || !count)
+        return fail(h, VA_BAD_ARGS, "va_step_pow_undecided: null argument%s");
+    *count = 0;
+    if (!h->ctl)
+        return VA_OK; // no sweep has run
+    unsigned int c = 0;
+    VA_CUDA(h, cudaMemcpy(&c, &h->ctl->pow_undecided, sizeof(c), cudaMemcpyDeviceToHost));
+    *count = c;
+    return VA_OK;
+}
+
 va_status va_default_options(va_options *o)
 {
     if (!o)
@@ -580,10 +687,17 @@ va_status va_default_options(va_options *o)
     o->blocks_per_sm = 0;
     o->chunk_len = 0;
     o->stage_records = 1;
+    o->step_pow = 1;
     return VA_OK;
 }
 
-va_status va_create(const va_problem *prob, const va_options *opt, va_handle **out)
+} // extern "C"
+
+namespace {
+
+// va_create / va_create_model: `user` is null for the built-in models
+va_status create_handle(const va_problem *prob, const va_options *opt, const va::ModelKernels *user,
+                        va_handle **out)
 {
     if (!prob || !out)
         return VA_BAD_ARGS;
@@ -606,7 +720,16 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
     const va::KernelSet *ks = nullptr;
     const va::BundleKernelSet *bks = nullptr;
     int N = 0, P = 0;
-    if (prob->model == VA_MODEL_GLV_SHARED) {
+    if (user) {
+        if (prob->model != VA_MODEL_USER || user->magic != va::kModelMagic || user->abi != va::kModelAbi ||
+            !user->launch || !user->occupancy)
+            return VA_BAD_ARGS;
+        ks = &user->set;
+        if (!ks->fwd[o.tableau][o.precision])
+            return VA_BAD_ARGS;
+        N = ks->N;
+        P = ks->P;
+    } else if (prob->model == VA_MODEL_GLV_SHARED) {
         bks = va::kernels_glv_shared(prob->n);
         // a (tableau, precision) pair without compiled kernels is rejected
         if (!bks || prob->nout != 1 || !bks->fwd[o.tableau][o.precision])
@@ -634,6 +757,7 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
     h->prob = *prob;
     h->opt = o;
     h->ks = ks;
+    h->user = user;
     h->bks = bks;
     h->N = N;
     h->P = P;
@@ -650,6 +774,67 @@ va_status va_create(const va_problem *prob, const va_options *opt, va_handle **o
         return VA_CUDA_ERROR;
     }
     *out = h;
+    return VA_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+va_status va_create(const va_problem *prob, const va_options *opt, va_handle **out)
+{
+    return create_handle(prob, opt, nullptr, out);
+}
+
+va_status va_create_model(const va_problem *prob, const va_options *opt, const va_model_kernels *model,
+                          va_handle **out)
+{
+    if (!model) {
+        if (out)
+            *out = nullptr;
+        return VA_BAD_ARGS;
+    }
+    return create_handle(prob, opt, reinterpret_cast<const va::ModelKernels *>(model), out);
+}
+
+va_status va_forward_frozen(va_handle *h, int32_t count, int32_t times_stride, const double *times,
+                            const int32_t *n_steps, const double *y0, const double *params,
+                            const double *shared, double *yT, void *stream)
+{
+    if (!h)
+        return VA_BAD_ARGS;
+    if (count < 1 || times_stride < 2 || !times || !n_steps || !y0 || !params || !yT)
+        return fail(h, VA_BAD_ARGS, "va_forward_frozen: bad count, stride or null pointer%s");
+    va::ReplayParams r{};
+    r.count = count;
+    r.stride = times_stride;
+    r.n = h->N;
+    r.np = h->P;
+    r.times = times;
+    r.n_steps = n_steps;
+    r.y0 = y0;
+    r.par = params;
+    r.yT = yT;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int tab = h->opt.tableau;
+    if (h->ks && h->ks->tpi == 1) {
+        const void *fn = h->ks->replay[tab];
+        if (!fn)
+            return fail(h, VA_BAD_ARGS, "va_forward_frozen: no replay kernel for this model and tableau%s");
+        VA_CUDA(h, launch(h, fn, (count + 127) / 128, 128, &r, s));
+        return VA_OK;
+    }
+    // Lotka-Volterra (per-instance matrix, or the shared one): a CTA per lane
+    if (h->bks) {
+        r.shared = shared ? shared : h->shared_A;
+        if (!r.shared)
+            return fail(h, VA_BAD_ARGS, "va_forward_frozen: shared-matrix model without a matrix%s");
+    }
+    const void *fn = va::replay_glv(tab);
+    if (!fn || h->N > 1024)
+        return fail(h, VA_BAD_ARGS, "va_forward_frozen: no replay kernel for this model and tableau%s");
+    void *args[] = {&r};
+    VA_CUDA(h, cudaLaunchKernel(fn, dim3(count), dim3(h->N), args, sizeof(double) * h->N, s));
     return VA_OK;
 }
 
@@ -1081,73 +1266,20 @@ va_status va_autotune(va_handle *h, int32_t cost, const double *y0, const double
     if (h->bks)
         return VA_OK; // bundle kernels: one CTA of N threads per bundle, nothing to tune
     cudaStream_t s = (cudaStream_t)stream;
-    const void *ffn = h->ks->fwd[h->opt.tableau][h->opt.precision];
-    const void *bfn = h->ks->bwd[h->opt.tableau][h->opt.precision];
-    cudaEvent_t e0, e1, e2;
-    VA_CUDA(h, cudaEventCreate(&e0));
-    VA_CUDA(h, cudaEventCreate(&e1));
-    VA_CUDA(h, cudaEventCreate(&e2));
-    float best_f = 1e30f, best_b = 1e30f;
-    int bf_block = h->fwd_block, bf_grid = h->fwd_grid, bb_block = h->bwd_block, bb_grid = h->bwd_grid;
-    const int blocks[] = {64, 128, 256};
-    for (int blk : blocks) {
-        int occf = 0, occb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occf, ffn, blk, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occb, bfn, blk, 0);
-        // every resident-block count: the best differs between the sweeps and
-        // between workloads (stage-record traffic favours fewer warps in the
-        // backward, issue rate more in the forward)
-        int maxocc = std::max(1, std::max(occf, occb));
-        std::vector<int> cands;
-        for (int c = 1; c <= maxocc; c++)
-            cands.push_back(c);
-        for (int bps : cands) {
-            h->fwd_block = h->bwd_block = blk;
-            long need = ((long)h->prob.batch * h->ks->tpi + blk - 1) / blk;
-            h->fwd_grid = (int)std::max(1L, std::min((long)h->sm_count * std::min(bps, std::max(occf, 1)), need));
-            h->bwd_grid = (int)std::max(1L, std::min((long)h->sm_count * std::min(bps, std::max(occb, 1)), need));
-            // a warm-up run, then the best of two timed runs
-            float cand_f = 1e30f, cand_b = 1e30f;
-            for (int rep = 0; rep < 3; rep++) {
-                VA_CUDA(h, cudaEventRecord(e0, s));
-                st = enqueue_forward(h, y0, params, t0, t1, h->s_yT, nullptr, nullptr, h->s_status, s);
-                if (st != VA_OK)
-                    return st;
-                VA_CUDA(h, cudaEventRecord(e1, s));
-                st = enqueue_backward(h, params, nullptr, nullptr, cost, h->s_dy0, h->s_dpar, h->s_status, s);
-                if (st != VA_OK)
-                    return st;
-                VA_CUDA(h, cudaEventRecord(e2, s));
-                VA_CUDA(h, cudaEventSynchronize(e2));
-                float tf = 0, tb = 0;
-                cudaEventElapsedTime(&tf, e0, e1);
-                cudaEventElapsedTime(&tb, e1, e2);
-                if (rep > 0) {
-                    cand_f = std::min(cand_f, tf);
-                    cand_b = std::min(cand_b, tb);
-                }
-            }
-            if (cand_f < best_f) {
-                best_f = cand_f;
-                bf_block = blk;
-                bf_grid = h->fwd_grid;
-            }
-            if (cand_b < best_b) {
-                best_b = cand_b;
-                bb_block = blk;
-                bb_grid = h->bwd_grid;
-            }
-        }
+    // the launch shape before tuning, restored if a candidate run fails
+    const int prev[4] = {h->fwd_block, h->fwd_grid, h->bwd_block, h->bwd_grid};
+    AutotuneEvents ev;
+    st = autotune_sweep(h, cost, y0, params, t0, t1, s, ev);
+    if (st != VA_OK) {
+        h->fwd_block = prev[0];
+        h->fwd_grid = prev[1];
+        h->bwd_block = prev[2];
+        h->bwd_grid = prev[3];
+        drop_graph(h);
+        return st;
     }
-    h->fwd_block = bf_block;
-    h->fwd_grid = bf_grid;
-    h->bwd_block = bb_block;
-    h->bwd_grid = bb_grid;
     drop_graph(h);
     h->forward_done = true;
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaEventDestroy(e2);
     return VA_OK;
 }
 

@@ -454,12 +454,12 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
                 continue;
             }
             if (err > 1.0) {
-                dt[b] = decrease_step<Tab, S>(dt[b], err);
+                dt[b] = decrease_step<Tab, S>(dt[b], err, a.step_pow, threadIdx.x == 0 ? &a.ctl->pow_undecided : nullptr);
                 rej[b]++;
                 ok = false;
             } else {
                 t[b] = Tab::FIXED ? fixed_time(t_start[b], count[b] + 1, dt[b]) : t[b] + dt[b];
-                dt[b] = increase_step<Tab, S>(dt[b], err);
+                dt[b] = increase_step<Tab, S>(dt[b], err, a.step_pow, threadIdx.x == 0 ? &a.ctl->pow_undecided : nullptr);
                 y[b] = ynew[b];
                 ys[b] = ynew_s[b];
                 if constexpr (Tab::FSAL) {

@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
             continue;
         }
         if (err > 1.0) {
-            dt = decrease_step<Tab, S>(dt, err);
+            dt = decrease_step<Tab, S>(dt, err, a.step_pow, li == 0 ? &a.ctl->pow_undecided : nullptr);
             rej++;
             ok = false;
         } else {
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
                 t = fixed_time(t_start, count + 1, dt);
             } else {
                 t += dt;
-                dt = increase_step<Tab, S>(dt, err);
+                dt = increase_step<Tab, S>(dt, err, a.step_pow, li == 0 ? &a.ctl->pow_undecided : nullptr);
             }
             ys[0] = ynew_s[0];
             if constexpr (std::is_same<S, dword>::value)

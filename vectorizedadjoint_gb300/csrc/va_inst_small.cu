@@ -16,7 +16,7 @@ void fill_fp64_decay(KernelSet &k);
 
 template <class M>
 static KernelSet make_set(void (*fill_fp64)(KernelSet &), void (*fill_rkf78)(KernelSet &),
-                          void (*fill_fixed)(KernelSet &))
+                          void (*fill_fixed)(KernelSet &), void (*fill_replay)(KernelSet &))
 {
     KernelSet k{};
     k.N = M::N;
@@ -44,28 +44,30 @@ static KernelSet make_set(void (*fill_fp64)(KernelSet &), void (*fill_rkf78)(Ker
     k.dw_records = true;
     fill_rkf78(k);
     fill_fixed(k);
+    fill_replay(k);
     return k;
 }
 
 const KernelSet *kernels_vdp()
 {
-    static const KernelSet k = make_set<ModelVdP>(fill_fp64_vdp, fill_rkf78_vdp, fill_fixed_vdp);
+    static const KernelSet k = make_set<ModelVdP>(fill_fp64_vdp, fill_rkf78_vdp, fill_fixed_vdp, fill_replay_vdp);
     return &k;
 }
 const KernelSet *kernels_vdp_petsc()
 {
     static const KernelSet k = make_set<ModelVdPPetsc>(fill_fp64_vdp_petsc, fill_rkf78_vdp_petsc,
-                                                          fill_fixed_vdp_petsc);
+                                                          fill_fixed_vdp_petsc, fill_replay_vdp_petsc);
     return &k;
 }
 const KernelSet *kernels_dho()
 {
-    static const KernelSet k = make_set<ModelDHO>(fill_fp64_dho, fill_rkf78_dho, fill_fixed_dho);
+    static const KernelSet k = make_set<ModelDHO>(fill_fp64_dho, fill_rkf78_dho, fill_fixed_dho, fill_replay_dho);
     return &k;
 }
 const KernelSet *kernels_decay()
 {
-    static const KernelSet k = make_set<ModelDecay>(fill_fp64_decay, fill_rkf78_decay, fill_fixed_decay);
+    static const KernelSet k = make_set<ModelDecay>(fill_fp64_decay, fill_rkf78_decay, fill_fixed_decay,
+                                                       fill_replay_decay);
     return &k;
 }
 

@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "va_dword.cuh"
+#include "va_stepfactor.cuh"
 #include "va_tableau.cuh"
 
 namespace va {
@@ -47,6 +48,7 @@ struct Control {
     unsigned int adj_next;  // next position in the backward work order
     unsigned int pool_next; // next free checkpoint chunk
     unsigned int pool_fail; // set when the pool ran out
+    unsigned int pow_undecided; // step factors whose rounding test failed (cr_step_pow)
 };
 
 // Checkpoint pool: chunks of `chunk_len` records of `rs` doubles.
@@ -66,6 +68,8 @@ struct FwdParams {
     const double *t1;  // [B]
     double atol, rtol, dt0;
     int max_steps, max_fail;
+    int step_pow;    // FP64 controller: 1 = correctly rounded pow (odeint's
+                     // std::pow), 0 = Newton root (cr_step_pow / inv_root)
     double *yT;      // [B][N] (may be null)
     int *n_acc_out;  // [B] (may be null)
     int *n_rej_out;  // [B] (may be null)
@@ -118,6 +122,7 @@ struct AdjParams {
     double atol, rtol;
     double dt0;              // the step of the fixed-step tableaux
     int max_fail;
+    int step_pow;            // the forward's step-factor power (FwdParams::step_pow)
     // adjoint history (may be null): lambda_n of seed q at
     // hist[((b * nout + q) * hist_cap + n) * N + i] for record n < hist_cap
     double *hist;
@@ -176,74 +181,6 @@ __host__ __device__ __forceinline__ float fromf<float>(float v)
 
 // ---------------------------------------------------------------- controller
 
-__host__ __device__ __forceinline__ int32_t f32_bits(float f)
-{
-#ifdef __CUDA_ARCH__
-    return __float_as_int(f);
-#else
-    int32_t i;
-    memcpy(&i, &f, 4);
-    return i;
-#endif
-}
-__host__ __device__ __forceinline__ float f32_from_bits(int32_t i)
-{
-#ifdef __CUDA_ARCH__
-    return __int_as_float(i);
-#else
-    float f;
-    memcpy(&f, &i, 4);
-    return f;
-#endif
-}
-
-// a^(-1/K) for the step-size controller, without a double-precision pow
-// (FP64 issues at 1/61 of the FP32 rate on this part).  Newton's iteration
-// for the inverse K-th root, x <- x + x (1 - a x^K) / K, from a seed built on
-// the float bit pattern (log2 read off the exponent field and scaled by
-// -1/K, the idea of the classic fast inverse square root): four FP32 steps
-// (seed error ~6% -> ~1e-7), two FP64 steps (-> ~1e-14 -> rounding).  Only
-// IEEE adds, multiplies and fused multiply-adds, in a fixed order: the
-// result has the same bits on any IEEE machine, which the oracle relies on
-// for a bit-exact comparison of step sequences.  a >= 1e30 (decrease only)
-// returns 0, which the 0.2 limiter turns into the same factor pow would.
-template <int K>
-__host__ __device__ __forceinline__ float inv_root_f32(float af)
-{
-    constexpr int32_t c = (int32_t)(((int64_t)(K + 1) * 0x3F800000LL) / K);
-    float x = f32_from_bits(c - f32_bits(af) / K);
-    const float rk = 1.0f / (float)K;
-#pragma unroll
-    for (int it = 0; it < 4; it++) {
-        float xk = x;
-#pragma unroll
-        for (int k = 1; k < K; k++)
-            xk = xk * x;
-        const float r = fmaf(-af, xk, 1.0f);
-        x = fmaf(x * r, rk, x);
-    }
-    return x;
-}
-
-template <int K, int FP64_STEPS = 2>
-__host__ __device__ __forceinline__ double inv_root(double a)
-{
-    if (!(a < 1e30))
-        return 0.0;
-    const float x = inv_root_f32<K>((float)a);
-    double xd = (double)x;
-#pragma unroll
-    for (int it = 0; it < FP64_STEPS; it++) {
-        double xk = xd;
-#pragma unroll
-        for (int k = 1; k < K; k++)
-            xk = xk * xd;
-        const double r = fma(-a, xk, 1.0);
-        xd = fma(xd * r, 1.0 / K, xd);
-    }
-    return xd;
-}
-
 // FP64 Newton steps of the step-factor root: two on the FP64 path (the
 // scheme the oracle shares), one on the reduced paths (~3e-14 relative,
 // far below the error estimate's own accuracy there).
@@ -254,15 +191,26 @@ struct RootSteps {
 
 // odeint default_step_adjuster::decrease_step:
 //   dt *= max(0.9 err^(-1/(q-1)), 0.2)
-// (fixed-step tableaux: dt unchanged; their sweeps never call it)
+// (fixed-step tableaux: dt unchanged; their sweeps never call it).
+// step_pow != 0 on the FP64 path: err^(-1/(q-1)) is odeint's
+// pow(err, -1.0/(q-1)) correctly rounded (cr_step_pow; undecided roundings
+// are counted in *undecided); else the Newton root.
 template <class Tab, class S = double>
-__host__ __device__ __forceinline__ double decrease_step(double dt, double err)
+__host__ __device__ __forceinline__ double decrease_step(double dt, double err, int step_pow = 0,
+                                                         unsigned int *undecided = nullptr)
 {
     if constexpr (Tab::FIXED) {
         (void)err;
+        (void)step_pow;
+        (void)undecided;
         return dt;
     } else {
-        double f = 9.0 / 10.0 * inv_root<Tab::ERROR_ORDER - 1, RootSteps<S>::value>(err);
+        double r;
+        if (std::is_same<S, double>::value && step_pow)
+            r = cr_step_pow<Tab::ERROR_ORDER - 1>(err, undecided);
+        else
+            r = inv_root<Tab::ERROR_ORDER - 1, RootSteps<S>::value>(err);
+        double f = 9.0 / 10.0 * r;
         return dt * fmax(f, 1.0 / 5.0);
     }
 }
@@ -270,17 +218,28 @@ __host__ __device__ __forceinline__ double decrease_step(double dt, double err)
 // odeint default_step_adjuster::increase_step:
 //   if err < 0.5: dt *= 0.9 max(err, 5^-p)^(-1/p)
 template <class Tab, class S = double>
-__host__ __device__ __forceinline__ double increase_step(double dt, double err)
+__host__ __device__ __forceinline__ double increase_step(double dt, double err, int step_pow = 0,
+                                                         unsigned int *undecided = nullptr)
 {
-    if constexpr (Tab::FIXED)
+    if constexpr (Tab::FIXED) {
+        (void)err;
+        (void)step_pow;
+        (void)undecided;
         return dt;
-    if (err < 0.5) {
-        // 5^-p as the correctly rounded quotient (1/3125, 1/390625), what
-        // pow(5.0, -p) returns
-        err = fmax(Tab::ERR_FLOOR, err);
-        dt *= 9.0 / 10.0 * inv_root<Tab::STEPPER_ORDER, RootSteps<S>::value>(err);
+    } else {
+        if (err < 0.5) {
+            // 5^-p as the correctly rounded quotient (1/3125, 1/390625), what
+            // pow(5.0, -p) returns
+            err = fmax(Tab::ERR_FLOOR, err);
+            double r;
+            if (std::is_same<S, double>::value && step_pow)
+                r = cr_step_pow<Tab::STEPPER_ORDER>(err, undecided);
+            else
+                r = inv_root<Tab::STEPPER_ORDER, RootSteps<S>::value>(err);
+            dt *= 9.0 / 10.0 * r;
+        }
+        return dt;
     }
-    return dt;
 }
 
 // ------------------------------------------------------------- stage algebra
@@ -771,7 +730,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
             continue;
         }
         if (err > 1.0) {
-            dt = decrease_step<Tab, S>(dt, err);
+            dt = decrease_step<Tab, S>(dt, err, a.step_pow, &a.ctl->pow_undecided);
             rej++;
             ok = false;
         } else {
@@ -779,7 +738,7 @@ __global__ void __launch_bounds__(256) forward_kernel(FwdParams a)
                 t = fixed_time(t_start, count + 1, dt); // t_0 + n dt (:61-62)
             } else {
                 t += dt;
-                dt = increase_step<Tab, S>(dt, err);
+                dt = increase_step<Tab, S>(dt, err, a.step_pow, &a.ctl->pow_undecided);
             }
             accept_state<M, Tab, S>(y, ys, k0, ynew, ynew_s, knew, p, t);
             ok = true;
@@ -1177,14 +1136,14 @@ __global__ void __launch_bounds__(256) backward_kernel_2level(AdjParams a)
             }
             fails++;
             if (err > 1.0) {
-                dt = decrease_step<Tab, S>(dt, err);
+                dt = decrease_step<Tab, S>(dt, err, a.step_pow, &a.ctl->pow_undecided);
                 continue;
             }
             if constexpr (Tab::FIXED) {
                 t = fixed_time(t_start, first + done + 1, dt);
             } else {
                 t += dt;
-                dt = increase_step<Tab, S>(dt, err);
+                dt = increase_step<Tab, S>(dt, err, a.step_pow, &a.ctl->pow_undecided);
             }
             accept_state<M, Tab, S>(y, ys, k0, ynew, ynew_s, knew, p, t);
             at_top = true;

@@ -163,6 +163,7 @@ extern "C" va_status va_gradient_noalloc(int32_t model, int32_t tableau, int32_t
     fa.dt0 = dt0;
     fa.max_steps = max_steps;
     fa.max_fail = max_rejects;
+    fa.step_pow = 1; // the correctly rounded step factor, as va_default_options
     fa.yT = yT;
     fa.n_acc_out = n_acc;
     fa.n_rej_out = nullptr;

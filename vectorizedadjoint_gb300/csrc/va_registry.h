@@ -4,6 +4,10 @@
 // that is not compiled (va_create rejects it).
 #pragma once
 
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
 namespace va {
 
 // tableaux: 0 Dormand-Prince 5(4), 1 Cash-Karp 5(4), 2 Fehlberg 7(8),
@@ -23,6 +27,8 @@ struct KernelSet {
     bool dw_records;                // mixed_dw [t, dt, y] records hold double-words (t stays
                                     // FP64); stage records always do
     int rs_stage[kTableaux];        // mixed_dw: doubles per stage record (0: no stage records)
+    const void *replay[kTableaux];  // FP64 frozen-step replay, one thread per lane
+                                    // (one-thread models); __global__ void(ReplayParams)
 };
 
 // whether the sweeps keep stage records: mixed_dw kernels that have them,
@@ -38,6 +44,23 @@ inline int record_doubles_for(const KernelSet *ks, int tableau, int precision, i
     return stage_records_on(ks, tableau, precision, stride, enabled) ? ks->rs_stage[tableau] : (2 + n + 1) & ~1;
 }
 
+// A device model compiled outside the library (include/va_model.cuh,
+// VA_DEFINE_MODEL): its kernel table plus a launcher and an occupancy query
+// compiled in the same translation unit, so its kernels are launched through
+// the CUDA runtime they were registered with (the model's shared object may
+// link its own copy of the runtime).  magic and abi guard against a table
+// built from another version of the sweep templates.
+constexpr uint32_t kModelMagic = 0x4B4D4156u; // "VAMK"
+constexpr uint32_t kModelAbi = 1;
+struct ModelKernels {
+    uint32_t magic, abi;
+    KernelSet set;
+    cudaError_t (*launch)(const void *fn, unsigned grid, unsigned block, void *params, size_t smem,
+                          cudaStream_t s);
+    cudaError_t (*occupancy)(int *blocks, const void *fn, int block, size_t smem);
+    const char *name;
+};
+
 const KernelSet *kernels_vdp();
 const KernelSet *kernels_vdp_petsc();
 const KernelSet *kernels_dho();
@@ -49,6 +72,13 @@ void fill_rkf78_vdp(KernelSet &k);
 void fill_rkf78_vdp_petsc(KernelSet &k);
 void fill_rkf78_dho(KernelSet &k);
 void fill_rkf78_decay(KernelSet &k);
+
+// FP64 frozen-step replay kernels of the one-thread models, every tableau
+// (va_inst_replay_fp64.cu)
+void fill_replay_vdp(KernelSet &k);
+void fill_replay_vdp_petsc(KernelSet &k);
+void fill_replay_dho(KernelSet &k);
+void fill_replay_decay(KernelSet &k);
 
 // fixed-step runge_kutta4 and euler entries (their own translation units)
 void fill_fixed_vdp(KernelSet &k);

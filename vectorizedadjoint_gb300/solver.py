@@ -32,12 +32,14 @@ class Solver:
     precision : 'fp64' | 'mixed' (FP32 stages) | 'mixed_dw' (double-word FP32-pair stages)
     stage_records : mixed_dw, every step checkpointed: 1 stores each step's stage
                 values for the backward sweep, 0 recomputes them (va_options)
+    step_pow  : FP64 controller: 1 (default) the correctly rounded step factor
+                (odeint's std::pow), 0 the Newton root (va_options)
     """
 
     def __init__(self, model, n, npar, batch, nout=1, tableau="dopri5", precision="fp64",
                  atol=1e-6, rtol=1e-6, dt0=1e-3, max_steps=1000000, max_rejects=500,
                  ckpt_budget_bytes=0, ckpt_stride=0, block_size=0, blocks_per_sm=0, chunk_len=0,
-                 stage_records=1):
+                 stage_records=1, step_pow=1):
         self.L = _lib.load()
         if not torch.cuda.is_available():
             raise RuntimeError("vectorizedadjoint_gb300 needs a CUDA device (no CPU fallback)")
@@ -53,11 +55,19 @@ class Solver:
         opt.ckpt_budget_bytes, opt.ckpt_stride = ckpt_budget_bytes, ckpt_stride
         opt.block_size, opt.blocks_per_sm, opt.chunk_len = block_size, blocks_per_sm, chunk_len
         opt.stage_records = stage_records
+        opt.step_pow = step_pow
         torch.cuda.init()
         self.h = ctypes.c_void_p()
         st = self.L.va_create(ctypes.byref(prob), ctypes.byref(opt), ctypes.byref(self.h))
         if st != _lib.VA_OK:
             raise _lib.VaError(st, f"va_create({model}, n={n}, npar={npar}, B={batch})")
+
+    def pow_undecided(self):
+        """Step factors of the last forward sweep whose correctly rounded value
+        was not decided (va_step_pow_undecided; 0 expected)."""
+        c = ctypes.c_int64()
+        self._check(self.L.va_step_pow_undecided(self.h, ctypes.byref(c)), "va_step_pow_undecided")
+        return c.value
 
     def _check(self, st, what):
         if st != _lib.VA_OK:
