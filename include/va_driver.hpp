@@ -14,10 +14,13 @@
 //   computeSensitivityMatrix(driver, alphas)       backpropagation.hpp:69-87
 //   computeSensitivityMatrixNoSIMD(driver, alphas) backpropagation.hpp:46-66
 //
-// Differences, by design: the right-hand side must be one of the built-in
-// device models (VanDerPol, VanDerPolPETSc, DampedOscillator,
-// LotkaVolterra, Decay) instead of an arbitrary host functor, and the
-// steppers are tags carrying the tableau and tolerances.  Step sizes are
+// Differences, by design: the right-hand side is device code -- one of the
+// built-in models (VanDerPol, VanDerPolPETSc, DampedOscillator,
+// LotkaVolterra, Decay) or a model of your own compiled with
+// include/va_model.cuh, passed as a tag struct with
+//   static const va_model_kernels *va_kernels();
+// returning its VA_DEFINE_MODEL table -- instead of an arbitrary host
+// functor, and the steppers are tags carrying the tableau and tolerances.  Step sizes are
 // frozen in the adjoint, as in the reference.  runge_kutta throws
 // std::runtime_error where odeint throws (failed step checker); adjointSolve
 // prints errors and returns, like the reference.
@@ -30,6 +33,7 @@
 #include <iostream>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "va.h"
@@ -74,6 +78,11 @@ struct DampedOscillator { static constexpr int32_t model = VA_MODEL_DHO; };
 struct LotkaVolterra { static constexpr int32_t model = VA_MODEL_GLV; };
 struct Decay { static constexpr int32_t model = VA_MODEL_DECAY; };
 
+// a model compiled outside the library: System::va_kernels() gives its table
+template <class System, class = void> struct is_device_model : std::false_type {};
+template <class System>
+struct is_device_model<System, std::void_t<decltype(System::va_kernels())>> : std::true_type {};
+
 // ------------------------------------------------------------------ driver
 class Driver {
   public:
@@ -91,15 +100,19 @@ class Driver {
     std::vector<std::vector<double>> *p_lambda = nullptr;
     std::vector<std::vector<double>> *p_mu = nullptr;
     int32_t m_model = -1;
+    const va_model_kernels *m_user = nullptr;
     int32_t m_tableau = -1;
     double m_atol = 1e-6, m_rtol = 1e-6, m_dt0 = 1e-3;
     int32_t m_T = -1;
 
-    // (Re)creates the handle when the problem or the stepper changed.
-    va_handle *handle(int32_t model, int32_t tableau, double atol, double rtol, double dt0)
+    // (Re)creates the handle when the problem or the stepper changed; `user`
+    // is the table of a model compiled outside the library (model
+    // VA_MODEL_USER), null for the built-in models.
+    va_handle *handle(int32_t model, int32_t tableau, double atol, double rtol, double dt0,
+                      const va_model_kernels *user = nullptr)
     {
         if (m_h && model == m_model && tableau == m_tableau && atol == m_atol && rtol == m_rtol &&
-            dt0 == m_dt0)
+            dt0 == m_dt0 && user == m_user)
             return m_h;
         release();
         va_problem p{model, m_Nin, m_Npar, 1, m_Nout};
@@ -109,12 +122,13 @@ class Driver {
         o.atol = atol;
         o.rtol = rtol;
         o.dt0 = dt0;
-        va_status st = va_create(&p, &o, &m_h);
+        va_status st = user ? va_create_model(&p, &o, user, &m_h) : va_create(&p, &o, &m_h);
         if (st != VA_OK) {
             m_h = nullptr;
             throw std::runtime_error(std::string("va_create failed: ") + va_status_string(st));
         }
         m_model = model;
+        m_user = user;
         m_tableau = tableau;
         m_atol = atol;
         m_rtol = rtol;
@@ -143,7 +157,12 @@ size_t runge_kutta(Stepper stepper, System system, State &start_state, const Sta
                    Time start_time, const Time end_time, Time dt, Driver &driver)
 {
     (void)system;
-    va_handle *h = driver.handle(System::model, Stepper::tableau, stepper.atol, stepper.rtol, (double)dt);
+    va_handle *h;
+    if constexpr (is_device_model<System>::value)
+        h = driver.handle(VA_MODEL_USER, Stepper::tableau, stepper.atol, stepper.rtol, (double)dt,
+                          System::va_kernels());
+    else
+        h = driver.handle(System::model, Stepper::tableau, stepper.atol, stepper.rtol, (double)dt);
     const double t0 = (double)start_time, t1 = (double)end_time;
     std::vector<double> y0(start_state.begin(), start_state.end()), p(alphas.begin(), alphas.end()),
         yT(y0.size());

@@ -313,6 +313,9 @@ void orc_rhs(const orc_problem *pb, const double *x, const double *p, double t, 
         for (int i = 0; i < n; i++)
             f[i] = -p[i] * x[i];
         break;
+    case ORC_MODEL_USER:
+        pb->user_rhs(x, p, t, f);
+        break;
     }
 }
 
@@ -369,6 +372,9 @@ void orc_vjp(const orc_problem *pb, const double *w, const double *x, const doub
             gx[i] = -p[i] * w[i];
             gp[i] = -x[i] * w[i];
         }
+        break;
+    case ORC_MODEL_USER:
+        pb->user_vjp(w, x, p, t, gx, gp);
         break;
     }
 }

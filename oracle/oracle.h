@@ -52,7 +52,8 @@ enum {
     ORC_MODEL_VDP_PETSC = 1, /* x0' = x1, x1' = mu ((1 - x0^2) x1 - x0)         */
     ORC_MODEL_DHO = 2,       /* x' = v, v' = -w^2 x - 2 z w v, p = (w, z)       */
     ORC_MODEL_GLV = 3,       /* x_i' = x_i (r_i + sum_j A_ij x_j), p = (r, A)  */
-    ORC_MODEL_DECAY = 4      /* y_i' = -p_i y_i (analytic test model)          */
+    ORC_MODEL_DECAY = 4,     /* y_i' = -p_i y_i (analytic test model)          */
+    ORC_MODEL_USER = 6       /* the callbacks user_rhs / user_vjp of orc_problem */
 };
 
 enum { ORC_TAB_DOPRI5 = 0, ORC_TAB_CK54 = 1, ORC_TAB_RKF78 = 2, ORC_TAB_RK4 = 3, ORC_TAB_EULER = 4 };
@@ -82,6 +83,9 @@ typedef struct {
                       std::pow), 2 = the correctly rounded pow (binary128
                       evaluation rounded once; the CUDA library's
                       reference-parity controller gives the same values) */
+    /* ORC_MODEL_USER: f = rhs(x, p, t) and (gx, gp) = (J_x^T w, J_p^T w) */
+    void (*user_rhs)(const double *x, const double *p, double t, double *f);
+    void (*user_vjp)(const double *w, const double *x, const double *p, double t, double *gx, double *gp);
 } orc_problem;
 
 /* Trace of the C library's pow in pow_mode 1: calls, calls whose result is

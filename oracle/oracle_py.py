@@ -16,7 +16,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _SO = os.path.join(_HERE, "_build", "liboracle.so")
 
-MODEL = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3, "decay": 4}
+MODEL = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3, "decay": 4, "user": 6}
 TABLEAU = {"dopri5": 0, "ck54": 1, "rkf78": 2, "rk4": 3, "euler": 4}
 COST = {"sumsq": 0, "sum": 1}
 STATUS = {0: "OK", 1: "MAX_REJECTS", 2: "MAX_STEPS", 3: "NONFINITE", 5: "BAD_ARGS"}
@@ -34,6 +34,8 @@ class Problem(ctypes.Structure):
         ("max_steps", ctypes.c_long),
         ("max_fail", ctypes.c_int),
         ("pow_mode", ctypes.c_int),
+        ("user_rhs", ctypes.c_void_p),
+        ("user_vjp", ctypes.c_void_p),
     ]
 
 
@@ -102,6 +104,14 @@ def problem(model, tableau, n, npar, atol, rtol, dt0=1e-3, max_steps=200000, max
     default (step_pow = 1); 1: the C library's pow, as odeint calls it; 0: the
     Newton root of the library's fast controller (step_pow = 0)."""
     return Problem(MODEL[model], TABLEAU[tableau], n, npar, atol, rtol, dt0, max_steps, max_fail, pow_mode)
+
+
+def user_problem(rhs, vjp, tableau, n, npar, atol, rtol, dt0=1e-3, max_steps=200000, max_fail=500, pow_mode=2):
+    """A problem whose right-hand side and VJP are C callbacks (function
+    pointers, e.g. ctypes.cast(lib.f, ctypes.c_void_p).value) with the
+    signatures of orc_problem.user_rhs / user_vjp."""
+    return Problem(MODEL["user"], TABLEAU[tableau], n, npar, atol, rtol, dt0, max_steps, max_fail, pow_mode,
+                   rhs, vjp)
 
 
 def step_pow(a, k, pow_mode):

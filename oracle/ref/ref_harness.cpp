@@ -83,6 +83,19 @@ struct LotkaVolterra { // examples/GeneralizedLotkaVolterra/main.cpp:105-119
     }
 };
 
+// The test suite's device models (tests/cpp/user_models.cuh), wrapped in the
+// reference's functor signature: the reference tapes them with AADC like any
+// user functor, so they pin the bring-your-own-model path.
+#include "../../tests/cpp/user_models.cuh"
+template <class Model> struct UserFunctor {
+    template <typename T> void operator()(const std::vector<T> &x, std::vector<T> &dxdt, const std::vector<T> &p, T t) const
+    {
+        Model::template rhs<T>(x.data(), p.data(), t, dxdt.data());
+    }
+};
+using DuffingFunctor = UserFunctor<ForcedDuffing>;
+using BrusselatorFunctor = UserFunctor<Brusselator>;
+
 template <class Stepper, class System>
 static int run(System sys, int n, int nout, int npar, double atol, double rtol, double dt0, const double *y0,
                const double *p, double t0, double t1, const double *lam_in, const double *mu_in, long cap,
@@ -181,7 +194,8 @@ static int run_history(System sys, int n, int nout, int npar, double atol, doubl
 }
 
 // model: 0 VdP (Lienard), 1 VdP (reference example form), 2 damped
-// oscillator, 3 GLV; tableau: 0 DOPRI5, 1 Cash-Karp, 2 Fehlberg 7(8) (the
+// oscillator, 3 GLV, 10 forced Duffing and 11 Brusselator (the test suite's
+// own models); tableau: 0 DOPRI5, 1 Cash-Karp, 2 Fehlberg 7(8) (the
 // reference's own ButcherTable branch), 3 fixed-step RK4, 4 fixed-step Euler
 // (step dt0).  Returns 0 on success.
 extern "C" int ref_solve(int model, int tableau, int n, int nout, int npar, double atol, double rtol, double dt0,
@@ -205,6 +219,10 @@ extern "C" int ref_solve(int model, int tableau, int n, int nout, int npar, doub
         return VA_RUN(DampedOscillator);
     case 3:
         return VA_RUN(LotkaVolterra);
+    case 10:
+        return VA_RUN(DuffingFunctor);
+    case 11:
+        return VA_RUN(BrusselatorFunctor);
     default:
         return 2;
     }
@@ -234,6 +252,10 @@ extern "C" int ref_history(int model, int tableau, int n, int nout, int npar, do
         return VA_RUN(DampedOscillator);
     case 3:
         return VA_RUN(LotkaVolterra);
+    case 10:
+        return VA_RUN(DuffingFunctor);
+    case 11:
+        return VA_RUN(BrusselatorFunctor);
     default:
         return 2;
     }

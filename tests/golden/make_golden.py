@@ -58,7 +58,7 @@ def differs_with_cr_pow(model, tableau, n, npar, tol, y0, p, t1, dt):
     return not (f1["n_acc"] == f2["n_acc"] and np.array_equal(f1["states"], f2["states"])
                 and np.array_equal(f1["times"], f2["times"]))
 
-MODEL_ID = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3}
+MODEL_ID = {"vdp": 0, "vdp_petsc": 1, "dho": 2, "glv": 3, "duffing": 10, "brusselator": 11}
 TABLEAU_ID = {"dopri5": 0, "ck54": 1, "rkf78": 2, "rk4": 3, "euler": 4}
 
 
@@ -133,6 +133,70 @@ def main_history(L):
     path = os.path.join(ROOT, "tests", "golden", "history_cases.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {len(specs)} history cases to {path} ({os.path.getsize(path)} bytes)")
+
+
+def user_model_draws(name, count, seed):
+    """Seeded instances of the test suite's own device models
+    (tests/cpp/user_models.cuh): (y0[count, 2], p[count, P], T)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    if name == "duffing":
+        p = np.stack([rng.uniform(0.1, 0.5, count), rng.uniform(0.5, 2.0, count), rng.uniform(0.0, 1.0, count),
+                      rng.uniform(0.5, 2.0, count), rng.uniform(0.5, 2.0, count)], axis=1)
+        return rng.uniform(-1.0, 1.0, (count, 2)), p, 10.0
+    p = np.stack([rng.uniform(0.8, 1.5, count), rng.uniform(1.5, 3.5, count)], axis=1)
+    return rng.uniform(0.5, 2.0, (count, 2)), p, 20.0
+
+
+def user_model_callbacks():
+    """Host build of tests/cpp/user_models.cuh for the oracle (g++, no contraction)."""
+    import subprocess
+    import tempfile
+    so = os.path.join(tempfile.mkdtemp(), "libuser_models_host.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-shared", "-fPIC",
+                    os.path.join(ROOT, "tests", "cpp", "user_models_host.cpp"), "-o", so], check=True)
+    H = ctypes.CDLL(so)
+    fp = lambda name: ctypes.cast(getattr(H, name), ctypes.c_void_p).value
+    return H, {"duffing": (fp("duffing_rhs"), fp("duffing_vjp")),
+               "brusselator": (fp("brusselator_rhs"), fp("brusselator_vjp"))}
+
+
+def main_user_models(L):
+    """The test models through the reference (its functor path, AADC tape):
+    forward records, pow traces and gradients -> tests/golden/user_model_cases.npz.
+    The forced Duffing model is non-autonomous: the reference's back-propagation
+    evaluates every recomputed stage at t_n and reads its stage times one
+    entry off (detail/backpropagation.hpp:48,197), so its gradients for that
+    model are kept only to measure that difference."""
+    keep_alive, cbs = user_model_callbacks()
+    out = {}
+    k = 0
+    for name, seed, tabs in [("duffing", 21, ("dopri5", "ck54", "rkf78")),
+                             ("brusselator", 22, ("dopri5", "ck54", "rkf78", "rk4"))]:
+        y0s, ps, T = user_model_draws(name, 3, seed)
+        npar = ps.shape[1]
+        for tab in tabs:
+            dt = 1e-2 if tab == "rk4" else 1e-3
+            for b in range(3):
+                y0, p = y0s[b], ps[b]
+                mu = np.zeros((1, npar))
+                _, _, _, yT, _, _ = solve(L, name, tab, 2, npar, 1e-8, y0, p, T, np.zeros((1, 2)), mu, dt=dt)
+                lam = 2.0 * yT[None, :]
+                Tn, times, states, yT, lo, mo = solve(L, name, tab, 2, npar, 1e-8, y0, p, T, lam, mu, dt=dt)
+                pb = O.user_problem(*cbs[name], tab, 2, npar, 1e-8, 1e-8, dt0=dt, pow_mode=1)
+                fw = O.forward(pb, y0, p, 0.0, T, powtrace=True)
+                assert fw["n_acc"] == Tn and np.array_equal(fw["states"], states), name
+                case = dict(name=f"{name}_{tab}[{b}]", model=name, tableau=tab, n=2, npar=npar, tol=1e-8, dt=dt,
+                            y0=y0, p=p, t1=T, lam=lam, mu=mu, T=Tn, yT=yT, dy0=lo, dp=mo, times=times,
+                            states=states, pow_calls=fw["pow_calls"], pow_noncr=fw["pow_noncr"],
+                            first_noncr_step=fw["first_noncr_step"])
+                for key, v in case.items():
+                    out[f"c{k}_{key}"] = np.asarray(v)
+                k += 1
+    out["count"] = np.array(k)
+    path = os.path.join(ROOT, "tests", "golden", "user_model_cases.npz")
+    np.savez_compressed(path, **out)
+    del keep_alive
+    print(f"wrote {k} user-model cases to {path} ({os.path.getsize(path)} bytes)")
 
 
 def main():
@@ -215,6 +279,7 @@ def main():
     np.savez_compressed(path, **out)
     print(f"wrote {len(cases)} cases to {path} ({os.path.getsize(path)} bytes)")
     main_history(L)
+    main_user_models(L)
 
 
 if __name__ == "__main__":

@@ -24,7 +24,9 @@ def _stream():
 class Solver:
     """One batch of B independent instances of a built-in model.
 
-    model     : 'vdp' | 'vdp_petsc' | 'dho' | 'glv' | 'decay'
+    model     : 'vdp' | 'vdp_petsc' | 'dho' | 'glv' | 'decay' | 'glv_shared', or 'user'
+                with model_kernels = the address returned by a VA_DEFINE_MODEL
+                accessor (a device model compiled outside the library)
     n, npar   : state and per-instance parameter counts
     batch     : B
     nout      : cost functions (seed rows) per instance
@@ -39,7 +41,7 @@ class Solver:
     def __init__(self, model, n, npar, batch, nout=1, tableau="dopri5", precision="fp64",
                  atol=1e-6, rtol=1e-6, dt0=1e-3, max_steps=1000000, max_rejects=500,
                  ckpt_budget_bytes=0, ckpt_stride=0, block_size=0, blocks_per_sm=0, chunk_len=0,
-                 stage_records=1, step_pow=1):
+                 stage_records=1, step_pow=1, model_kernels=None):
         self.L = _lib.load()
         if not torch.cuda.is_available():
             raise RuntimeError("vectorizedadjoint_gb300 needs a CUDA device (no CPU fallback)")
@@ -58,7 +60,11 @@ class Solver:
         opt.step_pow = step_pow
         torch.cuda.init()
         self.h = ctypes.c_void_p()
-        st = self.L.va_create(ctypes.byref(prob), ctypes.byref(opt), ctypes.byref(self.h))
+        if model_kernels is not None:
+            st = self.L.va_create_model(ctypes.byref(prob), ctypes.byref(opt), ctypes.c_void_p(model_kernels),
+                                        ctypes.byref(self.h))
+        else:
+            st = self.L.va_create(ctypes.byref(prob), ctypes.byref(opt), ctypes.byref(self.h))
         if st != _lib.VA_OK:
             raise _lib.VaError(st, f"va_create({model}, n={n}, npar={npar}, B={batch})")
 
@@ -163,6 +169,24 @@ class Solver:
                                          ctypes.c_void_p(dt.ctypes.data), ctypes.c_void_p(y.ctypes.data),
                                          ctypes.byref(nrec)), "va_trajectory")
         return t[:nrec.value], dt[:nrec.value], y[:nrec.value]
+
+    def forward_frozen(self, times, y0, params, shared=None):
+        """va_forward_frozen: FP64 replay of recorded accepted-step sequences.
+        times: list of 1-D arrays (t_0 .. t_T per lane); y0 [L, n], params
+        [L, npar] CUDA tensors; shared: an [n, n] CUDA tensor (shared-matrix
+        GLV) or None.  Returns y(T) [L, n]."""
+        import numpy as np
+        L = len(times)
+        stride = max(len(t) for t in times)
+        tt = np.zeros((L, stride))
+        for k, t in enumerate(times):
+            tt[k, :len(t)] = t
+        dtimes = torch.tensor(tt, dtype=torch.float64, device="cuda")
+        steps = torch.tensor([len(t) - 1 for t in times], dtype=torch.int32, device="cuda")
+        yT = self._alloc(L, self.n)
+        self._check(self.L.va_forward_frozen(self.h, L, stride, _ptr(dtimes), _ptr(steps), _ptr(y0), _ptr(params),
+                                             _ptr(shared), _ptr(yT), _stream()), "va_forward_frozen")
+        return yT
 
     def set_adjoint_history(self, capacity):
         """Keep lambda_n (every seed, record indices n < capacity) in later
