@@ -186,7 +186,8 @@ def max_over_ranks(ms, world, dist, torch, device="cpu"):
 
 
 def replica_throughput(batch_per_rank, ms, world):
-    """Whole-job gradients/s: every rank differentiates its own batch (weak scaling)."""
+    """Whole-job gradients/s: every rank differentiates its own contiguous
+    share of the instances (weak scaling: the share is fixed as ranks grow)."""
     return world * batch_per_rank / (ms * 1e-3)
 
 
@@ -305,9 +306,20 @@ def main():
                     help="print this GPU's FP64 / FP32 / FP64-MMA pipe rates as one JSON line and exit")
     args = ap.parse_args()
 
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: relaunch this command under torch.distributed.run
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + sys.argv[1:]
+        return subprocess.call(cmd)
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local = int(os.environ.get("LOCAL_RANK", 0))
+    if world != args.gpus and rank == 0:
+        sys.stderr.write(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}; using {world} ranks\n")
     if args.impl == "reference":
         return run_reference(args, rank, world)
 
@@ -333,7 +345,9 @@ def _bench(args, rank, world, local, torch, dist):
     from vectorizedadjoint_gb300 import Solver
     from vectorizedadjoint_gb300 import workloads as W
 
-    w = W.make(args.config, batch=args.batch or None)
+    # rank r solves its contiguous share of a job of world x batch instances
+    w = W.make_shard(args.config, rank, world, batch=args.batch or None) if world > 1 else \
+        W.make(args.config, batch=args.batch or None)
     c = w["cfg"]
     B = c["batch"]
     if args.budget_gb > 0:
@@ -348,6 +362,18 @@ def _bench(args, rank, world, local, torch, dist):
         if shared is not None:
             sv.set_shared(shared, torch.empty_like(shared))
         return sv
+
+    def exchange_dA(sv):
+        """The shared matrix's gradient is the sum over every rank's instances:
+        gathered and added in rank order (deterministic for a world size)."""
+        if world > 1 and shared is not None:
+            dA = sv._shared[1]
+            bufs = [torch.empty_like(dA) for _ in range(world)]
+            dist.all_gather(bufs, dA)
+            acc = bufs[0].clone()
+            for b in bufs[1:]:
+                acc += b
+            dA.copy_(acc)
 
     s = make_solver(B, args.precision)
     if not args.quick or args.tune:
@@ -370,6 +396,7 @@ def _bench(args, rank, world, local, torch, dist):
             torch.cuda.nvtx.range_push("timed_step")
             e0.record(stream)
             s.gradient(c["cost"], y0, par, t0, t1, out=out)
+            exchange_dA(s)
             e1.record(stream)
             torch.cuda.nvtx.range_pop()
             e1.synchronize()
@@ -505,7 +532,11 @@ def _bench(args, rank, world, local, torch, dist):
                       "mixed": "f32 stages / f64 controller+accumulators", "fp64": "f64"}[args.precision],
             "data": "synthetic (seeded PCG64)",
             "config": {"workload": f"{args.config}: {c['model']} B={B} {c['tableau']} tol={c['tol']}",
-                       "batch": B, "precision": args.precision, "cost": c["cost"],
+                       "batch": B, "global_batch": B * world,
+                       "parallelism": f"{world} rank(s), contiguous instance shards" + (
+                           ", shared dA summed across ranks in rank order" if shared is not None and world > 1
+                           else ""),
+                       "precision": args.precision, "cost": c["cost"],
                        "l2": "flushed between timed steps (256 MB write)",
                        "launch": s.launch(), "status_ok": int((status == 0).sum())},
             "e2e": {"value": e2e, "unit": "gradients/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -528,4 +559,4 @@ def _bench(args, rank, world, local, torch, dist):
 
 
 if __name__ == "__main__":
-    main()
+    sys.exit(main() or 0)

@@ -93,3 +93,22 @@ def test_one_pending_backward_per_solver(cuda):
     yT2, _ = odeint_adjoint(s, *args)  # free again after the backward
     yT2.sum().backward()
     s.close()
+
+
+def test_dropped_graph_releases_solver(cuda):
+    """A forward whose graph is discarded without a backward (here: the
+    outputs deleted) does not block the solver's next forward."""
+    import gc
+    B = 8
+    w = W.make("vdpb", batch=B)
+    s = solver_for(w, B)
+    args = (dev(w["y0"], True), dev(w["params"], True), dev(w["t0"]), dev(w["t1"]))
+    yT, st = odeint_adjoint(s, *args)
+    del yT, st
+    gc.collect()
+    yT2, _ = odeint_adjoint(s, *args)
+    yT2.sum().backward()
+    with torch.no_grad():
+        odeint_adjoint(s, *args)  # no graph: nothing stays pending
+    odeint_adjoint(s, *args)[0].sum().backward()
+    s.close()

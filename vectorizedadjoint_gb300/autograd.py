@@ -11,9 +11,14 @@ on the inputs is not differentiated, as in the reference.
 
 The solver's checkpoints belong to its last forward sweep, so one solver
 serves one pending backward at a time: a second forward on the same solver
-before the first backward has run raises.  The library does all arithmetic;
-torch only carries the device buffers and the graph bookkeeping.
+while the first one's graph is alive and its backward has not run raises.
+A graph that is dropped without a backward (an exception, evaluation under
+grad, a discarded output) releases the solver: the pending forward is
+tracked through a weak reference to its autograd node.  The library does all
+arithmetic; torch only carries the device buffers and the graph bookkeeping.
 """
+import weakref
+
 import torch
 
 from .solver import Solver
@@ -22,13 +27,14 @@ from .solver import Solver
 class _OdeAdjoint(torch.autograd.Function):
     @staticmethod
     def forward(ctx, solver, y0, params, t0, t1):
-        if getattr(solver, "_pending_backward", False):
+        pending = getattr(solver, "_pending_node", None)
+        if pending is not None and pending() is not None:
             raise RuntimeError("odeint_adjoint: this solver's checkpoints still wait for a backward pass; "
                                "use one solver per pending graph")
         y0c, pc = y0.detach().contiguous(), params.detach().contiguous()
         out = solver.forward(y0c, pc, t0.detach().contiguous(), t1.detach().contiguous())
         status = out["status"]
-        solver._pending_backward = True
+        solver._pending_node = weakref.ref(ctx)
         ctx.solver = solver
         ctx.save_for_backward(pc)
         ctx.mark_non_differentiable(status)
@@ -45,7 +51,7 @@ class _OdeAdjoint(torch.autograd.Function):
         try:
             bw = solver.backward(params, lam)
         finally:
-            solver._pending_backward = False
+            solver._pending_node = None
         return None, bw["dy0"][:, 0], bw["dp"][:, 0], None, None
 
 

@@ -32,6 +32,7 @@ namespace {
 constexpr size_t kScratchBytes = VA_NOALLOC_SCRATCH_BYTES;
 constexpr int kMaxDevices = 64;
 constexpr int kChunkLen = 64;
+constexpr size_t kStageChunks = 4; // chunks per instance below which stage records are dropped
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -103,17 +104,31 @@ extern "C" va_status va_gradient_noalloc(int32_t model, int32_t tableau, int32_t
     // chunk_prev | checkpoint chunks.  Every instance needs at least one
     // chunk; a batch whose metadata and first chunks do not fit is rejected.
     const size_t B = (size_t)batch;
-    // every step is checkpointed: the double-word sweeps use stage records
-    const size_t rec_bytes = (size_t)va::record_doubles_for(ks, tableau, precision, 1, ks->N, true) * sizeof(double);
-    const size_t chunk_bytes = rec_bytes * kChunkLen;
     const size_t off_T = 256, off_last = off_T + align256(B * 4), off_st = off_last + align256(B * 4);
     const size_t off_prev = off_st + align256(B * 4);
     if (off_prev >= kScratchBytes)
         return VA_BAD_ARGS;
     const size_t room = kScratchBytes - off_prev;
-    size_t n_chunks = room / (chunk_bytes + sizeof(int));
-    while (n_chunks > 0 && align256(n_chunks * sizeof(int)) + n_chunks * chunk_bytes > room)
-        n_chunks--;
+    auto chunks_for = [&](size_t rec_doubles) {
+        const size_t chunk_bytes = rec_doubles * sizeof(double) * kChunkLen;
+        size_t n = room / (chunk_bytes + sizeof(int));
+        while (n > 0 && align256(n * sizeof(int)) + n * chunk_bytes > room)
+            n--;
+        return n;
+    };
+    // Every step is checkpointed.  The double-word sweeps keep stage records
+    // (the step's stage values too) while the array holds kStageChunks
+    // chunks per instance; below that they switch to [t, dt, y] records and
+    // recompute the stages in the backward sweep (the kernels va_create uses
+    // with stage_records = 0), which fits ~4x more steps.
+    const void *ffn = ks->fwd[tableau][precision];
+    const void *bfn = ks->bwd[tableau][precision];
+    size_t n_chunks = chunks_for((size_t)va::record_doubles_for(ks, tableau, precision, 1, ks->N, true));
+    if (n_chunks < kStageChunks * B && ks->fwd2[tableau][precision] && ks->bwd1[tableau][precision]) {
+        n_chunks = chunks_for((size_t)va::record_doubles_for(ks, tableau, precision, 1, ks->N, false));
+        ffn = ks->fwd2[tableau][precision];
+        bfn = ks->bwd1[tableau][precision];
+    }
     if (n_chunks < B || n_chunks > 0x7fffffff)
         return VA_BAD_ARGS;
     const size_t off_pool = off_prev + align256(n_chunks * sizeof(int));
@@ -174,7 +189,6 @@ extern "C" va_status va_gradient_noalloc(int32_t model, int32_t tableau, int32_t
     fa.stride = 1; // every accepted step is checkpointed
     fa.pool = pool;
     fa.ctl = ctl;
-    const void *ffn = ks->fwd[tableau][precision];
     void *fargs[] = {&fa};
     if (cudaLaunchKernel(ffn, dim3(grid(ffn)), dim3(block), fargs, 0, s) != cudaSuccess)
         return VA_CUDA_ERROR;
@@ -195,7 +209,6 @@ extern "C" va_status va_gradient_noalloc(int32_t model, int32_t tableau, int32_t
     ba.inst_status = inst_status;
     ba.pool = pool;
     ba.ctl = ctl;
-    const void *bfn = ks->bwd[tableau][precision];
     void *bargs[] = {&ba};
     if (cudaLaunchKernel(bfn, dim3(grid(bfn)), dim3(block), bargs, 0, s) != cudaSuccess)
         return VA_CUDA_ERROR;

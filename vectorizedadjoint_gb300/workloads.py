@@ -72,3 +72,19 @@ def make(name, batch=None):
         raise KeyError(name)
     return dict(cfg=cfg, y0=np.ascontiguousarray(x0), params=np.ascontiguousarray(params),
                 t0=np.zeros(B), t1=np.ascontiguousarray(T), shared=shared)
+
+
+def make_shard(name, rank, world, batch=None):
+    """Rank `rank`'s contiguous share of a job of `world` x batch instances:
+    the job's workload is drawn once with the global batch (the same draws on
+    every rank) and each rank keeps its own range, so ranks solve different
+    instances and the shared matrix, where there is one, is common."""
+    from .shard import shard_range
+    per = batch or CONFIGS[name]["batch"]
+    w = make(name, batch=per * world)
+    lo, hi = shard_range(per * world, rank, world)
+    out = dict(w)
+    for k in ("y0", "params", "t0", "t1"):
+        out[k] = np.ascontiguousarray(w[k][lo:hi])
+    out["cfg"] = dict(w["cfg"], batch=hi - lo, global_batch=per * world, shard=(lo, hi))
+    return out
