@@ -25,6 +25,17 @@ extern "C" {
  * buffer.  Returns a va_status. */
 VA_API int32_t va_probe_rate(int32_t kind, int32_t iters, double *tflops, double *ms_out);
 
+/* The tensor-core contraction the shared-matrix GLV backward sweep uses for
+ * its matrix gradient, on caller data: dA[256][256] = sum_k v_k x_k^T for
+ * DEVICE arrays v[K][256], x[K][256] of double-words packed in 8-byte slots
+ * (float hi in the low word, lo in the high word).  Exact integer digit
+ * products on tcgen05 (bf16 inputs, FP32 tensor-memory accumulators) of
+ * factors split into four 8-bit digits per 64-row chunk; the truncation of
+ * the digits leaves ~2^-32 of the chunk's column maxima per term.
+ * Allocates scratch, synchronises `stream`.  Returns a va_status
+ * (VA_CUDA_ERROR also when a bounded wait in the kernel gave up). */
+VA_API int32_t va_contract_dA(int32_t K, const double *v, const double *x, double *dA, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,7 +26,7 @@ EXPORTS = ["va_default_options", "va_create", "va_destroy", "va_forward", "va_ba
            "va_get_launch", "va_checkpoint_info",
            "va_trajectory", "va_set_adjoint_history", "va_adjoint_history", "va_adjoint_history_buffer",
            "va_set_shared", "va_last_error", "va_status_string", "va_probe_rate",
-           "va_step_pow_undecided", "va_create_model", "va_forward_frozen"]
+           "va_step_pow_undecided", "va_create_model", "va_forward_frozen", "va_contract_dA"]
 
 
 class VaProblem(ctypes.Structure):
@@ -94,6 +94,7 @@ def load():
     L.va_create_model.argtypes = [ctypes.POINTER(VaProblem), ctypes.POINTER(VaOptions), ctypes.c_void_p,
                                   ctypes.POINTER(H)]
     L.va_forward_frozen.argtypes = [H, ctypes.c_int32, ctypes.c_int32, dp, ip, dp, dp, dp, dp, vp]
+    L.va_contract_dA.argtypes = [ctypes.c_int32, dp, dp, dp, vp]
     L.va_step_pow_undecided.argtypes = [H, ctypes.POINTER(ctypes.c_int64)]
     L.va_probe_rate.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                                 ctypes.POINTER(ctypes.c_double)]

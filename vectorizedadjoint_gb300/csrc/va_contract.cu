@@ -1,0 +1,506 @@
+// Kernels of the tensor-core dA contraction (va_contract.cuh): the factor-row
+// offsets of each instance, the contraction on tcgen05 with tensor-memory
+// accumulators, and the fixed-order sum of the CTA partials.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "../../include/va.h"
+#include "../../include/va_probe.h"
+#include "va_contract.cuh"
+#include "va_kernels.cuh"
+
+namespace va {
+
+// -------------------------------------------------------------- PTX wrappers
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase with the given parity to complete; gives up after 2^22
+// polls (each try_wait suspends for a while: about a second in all), sets
+// *error and returns false.  Every wait of these kernels ends.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, unsigned *error)
+{
+    for (int it = 0; it < (1 << 22); it++)
+        if (mbar_try_wait(bar, parity))
+            return true;
+    atomicExch(error, 1u);
+    return false;
+}
+
+// shared-memory matrix descriptor of a tcgen05 operand: no swizzle, K-major;
+// lbo = bytes between the two core matrices of a K step, sbo = bytes between
+// 8-row groups; bits 46-47 hold the descriptor version (1).
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// instruction descriptor of tcgen05.mma kind::f16: FP32 accumulator (bits 4-5
+// = 1), bf16 A and B (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17,
+// M >> 4 at bit 24
+constexpr uint32_t umma_idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                 "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+                 : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive FP32 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                 "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+                 "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+                   "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+                   "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int c = 0; c < 32; c++)
+        v[c] = __uint_as_float(r[c]);
+}
+
+// ------------------------------------------------------------ row offsets
+
+// k_base[b] = nsv * sum_{b' < b, OK} T_b' (the first factor row of instance
+// b), k_base[B] = K.  One block; each thread a contiguous range of instances.
+__global__ void __launch_bounds__(1024) factor_offsets_kernel(const int *inst_T, const int *inst_status, int B,
+                                                              int nsv, int *k_base)
+{
+    __shared__ long long part[1024];
+    const int t = threadIdx.x, per = (B + 1023) / 1024;
+    const int lo = min(B, t * per), hi = min(B, lo + per);
+    long long s = 0;
+    for (int b = lo; b < hi; b++)
+        s += inst_status[b] == ST_OK ? (long long)inst_T[b] * nsv : 0;
+    part[t] = s;
+    __syncthreads();
+    // inclusive scan of the 1024 partial sums (Hillis-Steele)
+    for (int o = 1; o < 1024; o <<= 1) {
+        const long long v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    long long run = t > 0 ? part[t - 1] : 0;
+    for (int b = lo; b < hi; b++) {
+        k_base[b] = (int)run;
+        run += inst_status[b] == ST_OK ? (long long)inst_T[b] * nsv : 0;
+    }
+    if (t == 1023)
+        k_base[B] = (int)part[1023];
+}
+
+// ------------------------------------------------------------ contraction
+
+// |hi| of a packed double-word (for the exponent bound)
+__device__ __forceinline__ float dw_abs_hi(double packed) { return fabsf(dw_unpack(packed).hi); }
+
+// exponent e with |x| < 2^e for every entry whose leading word is at most m
+__device__ __forceinline__ int bound_exponent(float m) { return m > 0.0f ? ilogbf(m) + 1 : -120; }
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+// One column's 8 consecutive rows (a core-matrix row of 16 bytes) as Q digit
+// planes: vals are packed double-words, e the column's exponent.
+__device__ __forceinline__ void slice_row8(const double (&vals)[8], int e, uint8_t *plane0, size_t plane_stride)
+{
+    float d[8][kContractQ];
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        const dword w = dw_unpack(vals[r]);
+        split_digits(w.hi, w.lo, e, d[r]);
+    }
+#pragma unroll
+    for (int s = 0; s < kContractQ; s++) {
+        uint4 q;
+        q.x = pack_bf16x2(d[0][s], d[1][s]);
+        q.y = pack_bf16x2(d[2][s], d[3][s]);
+        q.z = pack_bf16x2(d[4][s], d[5][s]);
+        q.w = pack_bf16x2(d[6][s], d[7][s]);
+        *reinterpret_cast<uint4 *>(plane0 + s * plane_stride) = q;
+    }
+}
+
+// Slices chunk c of the CTA's tile into one shared-memory stage and stores
+// the column exponents (e_v[128], e_x[64]).
+__device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int K, int ti, int tj, uint8_t *stage,
+                                            int *ev, int *ex, float *red)
+{
+    const int t = threadIdx.x;
+    const int k0 = c * kContractKC;
+    // v: column i = t & 127, rows 32 h .. 32 h + 31 (h = t >> 7)
+    {
+        const int i = t & 127, h = t >> 7;
+        const double *col = p.v + (size_t)ti * kContractTileM + i;
+        float m = 0.0f;
+        for (int r = 0; r < 32; r++) {
+            const int k = k0 + 32 * h + r;
+            if (k < K)
+                m = fmaxf(m, dw_abs_hi(__ldg(col + (size_t)k * kContractN)));
+        }
+        red[t] = m;
+    }
+    // x: column j = t & 63, rows 16 q .. 16 q + 15 (q = t >> 6)
+    {
+        const int j = t & 63, q = t >> 6;
+        float m = 0.0f;
+        for (int r = 0; r < 16; r++) {
+            const int k = k0 + 16 * q + r;
+            if (k < K)
+                m = fmaxf(m, dw_abs_hi(__ldg(p.xp[k] + tj * kContractTileN + j)));
+        }
+        red[256 + t] = m;
+    }
+    __syncthreads();
+    if (t < 128)
+        ev[t] = bound_exponent(fmaxf(red[t], red[t + 128]));
+    else if (t < 192) {
+        const int j = t - 128;
+        ex[j] = bound_exponent(fmaxf(fmaxf(red[256 + j], red[256 + j + 64]),
+                                     fmaxf(red[256 + j + 128], red[256 + j + 192])));
+    }
+    __syncthreads();
+    // digits: v planes [slice][kgroup 8][row 128][8] (plane = 16 KB, kgroup = 2 KB)
+    {
+        const int i = t & 127, h = t >> 7;
+        const double *col = p.v + (size_t)ti * kContractTileM + i;
+        const int e = ev[i];
+#pragma unroll 1
+        for (int g = 0; g < 4; g++) {
+            const int kg = 4 * h + g;
+            double vals[8];
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                const int k = k0 + 8 * kg + r;
+                vals[r] = k < K ? __ldg(col + (size_t)k * kContractN) : 0.0;
+            }
+            slice_row8(vals, e, stage + (size_t)kg * 2048 + i * 16, (size_t)kContractKC * kContractTileM * 2);
+        }
+    }
+    // digits: x planes [slice][kgroup 8][row 64][8] (plane = 8 KB, kgroup = 1 KB)
+    {
+        const int j = t & 63, q = t >> 6;
+        const int e = ex[j];
+        uint8_t *xs = stage + kTileVBytes;
+#pragma unroll 1
+        for (int g = 0; g < 2; g++) {
+            const int kg = 2 * q + g;
+            double vals[8];
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                const int k = k0 + 8 * kg + r;
+                vals[r] = k < K ? __ldg(p.xp[k] + tj * kContractTileN + j) : 0.0;
+            }
+            slice_row8(vals, e, xs + (size_t)kg * 1024 + j * 16, (size_t)kContractKC * kContractTileN * 2);
+        }
+    }
+}
+
+// The 40 MMAs of one chunk: for every group g = s + t the digit pairs
+// (s, t), each over the chunk's four K steps of 16, into accumulator g.
+__device__ __forceinline__ void issue_chunk(uint32_t tmem_acc, const uint8_t *stage)
+{
+    constexpr uint32_t idesc = umma_idesc_bf16(kContractTileM, kContractTileN);
+    const uint32_t vbase = smem_u32(stage), xbase = smem_u32(stage + kTileVBytes);
+    constexpr uint32_t vplane = kContractKC * kContractTileM * 2, xplane = kContractKC * kContractTileN * 2;
+#pragma unroll
+    for (int g = 0; g < kContractQ; g++) {
+        bool first = true;
+#pragma unroll
+        for (int s = 0; s <= g; s++) {
+            const int tq = g - s;
+#pragma unroll
+            for (int kk = 0; kk < kContractKC / 16; kk++) {
+                // K step kk covers kgroups 2kk and 2kk + 1
+                const uint64_t ad = umma_desc(vbase + s * vplane + kk * 2 * 2048, 2048, 128);
+                const uint64_t bd = umma_desc(xbase + tq * xplane + kk * 2 * 1024, 1024, 128);
+                umma_bf16(tmem_acc + g * kContractTileN, ad, bd, idesc, first ? 0u : 1u);
+                first = false;
+            }
+        }
+    }
+}
+
+// Folds one chunk's group sums into the double-word accumulators of this
+// thread's row and 32 columns: acc += R_g 2^(e_v + e_x - 8(g + 2)).
+__device__ __forceinline__ void fold_chunk(uint32_t tmem_row, const int *ev, const int *ex, int row, int col0,
+                                           float (&ah)[32], float (&al)[32])
+{
+    int esum[32];
+#pragma unroll
+    for (int c = 0; c < 32; c++)
+        esum[c] = ev[row] + ex[col0 + c] - 16;
+#pragma unroll 1
+    for (int g = 0; g < kContractQ; g++) {
+        float R[32];
+        tmem_ld32(tmem_row + g * kContractTileN, R);
+#pragma unroll
+        for (int c = 0; c < 32; c++) {
+            const float v = ldexpf(R[c], esum[c] - 8 * g); // exact (power-of-two scaling)
+            // double-word accumulation: (ah, al) += v
+            const float s = ah[c] + v;
+            const float bb = s - ah[c];
+            const float e = (ah[c] - (s - bb)) + (v - bb);
+            const float lo = al[c] + e;
+            ah[c] = s + lo;
+            al[c] = lo - (ah[c] - s);
+        }
+    }
+}
+
+// grid = tiles x splits, 256 threads, kContractSmem dynamic shared memory
+__global__ void __launch_bounds__(256, 1) contract_kernel(ContractParams p)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *stages[2] = {smem, smem + kStageBytes};
+    uint64_t *done = reinterpret_cast<uint64_t *>(smem + 2 * kStageBytes); // [2]
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 2);
+    __shared__ int ev_s[2][kContractTileM], ex_s[2][kContractTileN];
+    __shared__ float red[512];
+
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int tile = blockIdx.x % kContractTiles, split = blockIdx.x / kContractTiles;
+    const int ti = tile / (kContractN / kContractTileN), tj = tile % (kContractN / kContractTileN);
+    const int K = *p.k_total;
+    const int nc = (K + kContractKC - 1) / kContractKC;
+    const int c0 = (int)((long long)split * nc / p.splits), c1 = (int)((long long)(split + 1) * nc / p.splits);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (t == 0) {
+        mbar_init(&done[0], 1);
+        mbar_init(&done[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    // this thread's accumulator row and columns: warp w reads tensor-memory
+    // lanes 32 (w % 4) .. +31, columns 32 (w / 4) .. +31 of each group
+    const int row = 32 * (warp & 3) + lane, col0 = 32 * (warp >> 2);
+    const uint32_t lane_addr = (uint32_t)(32 * (warp & 3)) << 16;
+    float ah[32], al[32];
+#pragma unroll
+    for (int c = 0; c < 32; c++)
+        ah[c] = al[c] = 0.0f;
+
+    // ok stays uniform across the block (a bounded wait that gave up on any
+    // thread stops the work of all of them at the next barrier)
+    bool ok = true;
+    int issued = 0, waited = 0; // chunks committed / chunks whose commit was awaited
+    const int n = c1 - c0;
+    for (int idx = 0; idx < n; idx++) {
+        const int st = idx & 1;
+        if (ok)
+            slice_chunk(p, c0 + idx, K, ti, tj, stages[st], ev_s[st], ex_s[st], red);
+        // the digit planes, written by this CTA's threads, feed the tensor core
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();
+        __syncthreads();
+        if (ok) {
+            if (t == 0) {
+                tc_fence_after();
+                issue_chunk(tmem + st * kContractQ * kContractTileN, stages[st]);
+                umma_commit(&done[st]);
+            }
+            issued = idx + 1;
+        }
+        if (idx > 0 && ok) {
+            // the previous chunk's group sums
+            const int pst = st ^ 1;
+            const bool w = mbar_wait_bounded(&done[pst], ((idx - 1) >> 1) & 1, p.error);
+            ok = __syncthreads_and(w) != 0;
+            if (ok) {
+                waited = idx;
+                tc_fence_after();
+                fold_chunk(tmem + lane_addr + pst * kContractQ * kContractTileN + col0, ev_s[pst], ex_s[pst], row,
+                           col0, ah, al);
+            }
+            tc_fence_before();
+        }
+        __syncthreads();
+    }
+    if (ok && issued == n && n > 0) {
+        const int idx = n - 1, st = idx & 1;
+        const bool w = mbar_wait_bounded(&done[st], (idx >> 1) & 1, p.error);
+        ok = __syncthreads_and(w) != 0;
+        if (ok) {
+            waited = n;
+            tc_fence_after();
+            fold_chunk(tmem + lane_addr + st * kContractQ * kContractTileN + col0, ev_s[st], ex_s[st], row, col0,
+                       ah, al);
+        }
+    }
+    // after an error: wait (bounded) for the MMAs still in flight before the
+    // tensor memory is released
+    for (int c = waited; c < issued; c++)
+        (void)mbar_wait_bounded(&done[c & 1], (c >> 1) & 1, p.error);
+    // partial[split][j][i] (transposed, as the fixed-order reduction reads it)
+    const int i = ti * kContractTileM + row;
+#pragma unroll
+    for (int c = 0; c < 32; c++) {
+        const int j = tj * kContractTileN + col0 + c;
+        p.partials[((size_t)split * kContractN + j) * kContractN + i] = (double)ah[c] + (double)al[c];
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+}
+
+// x_k pointers of a dense [K][256] factor matrix (the diagnostic entry point)
+__global__ void dense_rows_kernel(const double *x, int K, const double **xp)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < K)
+        xp[k] = x + (size_t)k * kContractN;
+}
+
+// dA[i][j] = sum over splits, in split order, of partial[split][j][i]
+__global__ void reduce_partials_kernel(const double *part, int nparts, double *dA)
+{
+    constexpr int NT = kContractN;
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; // k = j * NT + i
+    if (k >= (size_t)NT * NT)
+        return;
+    double s = 0.0;
+    for (int c = 0; c < nparts; c++)
+        s += part[(size_t)c * NT * NT + k];
+    const size_t j = k / NT, i = k % NT;
+    dA[i * NT + j] = s;
+}
+
+int contract_splits(int sm_count) { return std::max(1, sm_count / kContractTiles); }
+
+cudaError_t enqueue_factor_offsets(const int *inst_T, const int *inst_status, int B, int nsv, int *k_base,
+                                   cudaStream_t s)
+{
+    factor_offsets_kernel<<<1, 1024, 0, s>>>(inst_T, inst_status, B, nsv, k_base);
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_contract(const ContractParams &p, double *dA, cudaStream_t s)
+{
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)kContractSmem);
+        if (e != cudaSuccess)
+            return e;
+        attr = true;
+    }
+    contract_kernel<<<kContractTiles * p.splits, 256, kContractSmem, s>>>(p);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    constexpr int NN = kContractN * kContractN;
+    reduce_partials_kernel<<<(NN + 255) / 256, 256, 0, s>>>(p.partials, p.splits, dA);
+    return cudaGetLastError();
+}
+
+} // namespace va
+
+extern "C" VA_API int32_t va_contract_dA(int32_t K, const double *v, const double *x, double *dA, void *stream)
+{
+    if (K < 0 || !v || !x || !dA)
+        return VA_BAD_ARGS;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return VA_CUDA_ERROR;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int splits = va::contract_splits(sms);
+    const double **xp = nullptr;
+    int *k_total = nullptr;
+    unsigned *err = nullptr;
+    double *part = nullptr;
+    const size_t nn = (size_t)va::kContractN * va::kContractN;
+    int32_t st = VA_OK;
+    if (cudaMalloc(&xp, sizeof(double *) * (size_t)std::max(K, 1)) != cudaSuccess ||
+        cudaMalloc(&k_total, sizeof(int)) != cudaSuccess || cudaMalloc(&err, sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&part, sizeof(double) * nn * splits) != cudaSuccess)
+        st = VA_CUDA_ERROR;
+    if (st == VA_OK) {
+        va::dense_rows_kernel<<<(K + 255) / 256 + 1, 256, 0, s>>>(x, K, xp);
+        cudaMemcpyAsync(k_total, &K, sizeof(int), cudaMemcpyHostToDevice, s);
+        cudaMemsetAsync(err, 0, sizeof(unsigned), s);
+        va::ContractParams p{};
+        p.v = v;
+        p.xp = xp;
+        p.k_total = k_total;
+        p.partials = part;
+        p.splits = splits;
+        p.error = err;
+        if (va::enqueue_contract(p, dA, s) != cudaSuccess)
+            st = VA_CUDA_ERROR;
+        unsigned e = 0;
+        if (cudaMemcpyAsync(&e, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            st = VA_CUDA_ERROR;
+        else if (e)
+            st = VA_CUDA_ERROR;
+    }
+    cudaFree(xp);
+    cudaFree(k_total);
+    cudaFree(err);
+    cudaFree(part);
+    return st;
+}
