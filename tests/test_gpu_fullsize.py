@@ -10,7 +10,9 @@ not depend on the batch size:
   bit for bit, double-word within the reduced-precision bound (1e-6 of the
   instance's gradient scale; 1e-5 for the damped oscillators);
 - the shared-matrix dA of the whole batch equals the sum of the two halves'
-  dA to rounding, 1e-10 of its largest entry (dA is linear in the instances)."""
+  dA within 2e-8 of its largest entry (dA is linear in the instances; the
+  tensor-core contraction's digit truncation depends on which factor rows
+  share a 64-row chunk)."""
 import numpy as np
 import pytest
 import torch
@@ -102,13 +104,16 @@ def test_glv256_full_batch(oracle, cuda):
     _, rr = full("glv256", "mixed_dw", reverse=True)
     for k in ("yT", "dy0", "dp", "n_acc"):
         np.testing.assert_array_equal(rr[k], r[k], err_msg=k)
+    # dA comes from the tensor-core contraction, whose digits are relative to
+    # each 64-row chunk of factor rows: another batch order or split puts other
+    # rows in a chunk, so dA moves by its truncation (~1e-9), not by rounding
     scale = np.abs(r["dA"]).max()
-    assert np.abs(rr["dA"] - r["dA"]).max() <= 1e-10 * scale
+    assert np.abs(rr["dA"] - r["dA"]).max() <= 2e-8 * scale
     h = B // 2
     parts = [gradient(c, "mixed_dw", w["y0"][sl], w["params"][sl], w["t0"][sl], w["t1"][sl], w["shared"])
              for sl in (slice(0, h), slice(h, B))]
     np.testing.assert_array_equal(np.concatenate([p["dy0"] for p in parts]), r["dy0"])
-    assert np.abs(parts[0]["dA"] + parts[1]["dA"] - r["dA"]).max() <= 1e-10 * scale
+    assert np.abs(parts[0]["dA"] + parts[1]["dA"] - r["dA"]).max() <= 2e-8 * scale
     pb = oracle.problem("glv", "dopri5", N, N + N * N, c["tol"], c["tol"])
     for b in (0, int(np.argmax(r["n_acc"]))):
         p = np.concatenate([w["params"][b], w["shared"].ravel()])

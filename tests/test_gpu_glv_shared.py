@@ -98,3 +98,21 @@ def test_shared_glv_workload_smoke(cuda):
     res = run(256, 8, w["shared"], w["params"], w["y0"], 10.0, "mixed_dw")
     assert (res["status"] == 0).all()
     assert np.isfinite(res["dA"]).all()
+
+
+def test_shared_glv256_tensor_core_dA_vs_fp64(cuda):
+    """N = 256, double-word sweeps with stage records: the backward writes
+    factor rows and dA comes from the tcgen05 contraction
+    (csrc/va_contract.cu); against the FP64 path's dA (FP64 CTA partials)
+    within 1e-8 of its largest entry, and against the double-word sweeps
+    without stage records (which keep the fused double-word partials) to the
+    same bound."""
+    N, B, T = 256, 12, 10.0
+    A, r, x0 = make_small(N, B, seed=21)
+    r64 = run(N, B, A, r, x0, T, "fp64")
+    rtc = run(N, B, A, r, x0, T, "mixed_dw", stage_records=1)
+    rfu = run(N, B, A, r, x0, T, "mixed_dw", stage_records=0)
+    scale = np.abs(r64["dA"]).max()
+    assert np.isfinite(rtc["dA"]).all()
+    assert np.abs(rtc["dA"] - r64["dA"]).max() <= 1e-8 * scale, np.abs(rtc["dA"] - r64["dA"]).max() / scale
+    assert np.abs(rtc["dA"] - rfu["dA"]).max() <= 1e-8 * scale

@@ -14,6 +14,7 @@
 
 #include "../../include/va.h"
 #include "va_bundle.cuh"
+#include "va_contract.cuh"
 #include "va_kernels.cuh"
 #include "va_order.h"
 #include "va_registry.h"
@@ -97,6 +98,15 @@ struct va_handle {
     double *shared_dA = nullptr;
     double *At = nullptr, *dA_part = nullptr;
     va::dword *Aw = nullptr, *Atw = nullptr;
+    // deferred dA on the tensor pipe (N = 256, double-word sweeps with stage
+    // records): factor rows, their x pointers, per-instance row offsets,
+    // contraction partials and its error flag
+    double *fac_v = nullptr;
+    const double **fac_xp = nullptr;
+    int *k_base = nullptr;
+    double *c_part = nullptr;
+    unsigned *c_err = nullptr;
+    int64_t fac_rows = 0;
 
     bool buffers_ready = false; // ensure_buffers / ensure_staging completed
     bool staging_ready = false;
@@ -179,6 +189,16 @@ bool stages_now(const va_handle *h)
     return va::stage_records_on(h->ks, h->opt.tableau, h->opt.precision, h->stride, h->stages_on);
 }
 
+// Whether the handle's shared-matrix gradient can be contracted on the
+// tensor pipe (va_contract.cu): N = 256, double-word sweeps, stage records
+// (the backward points at the stage points X_m they hold).
+bool deferred_possible(const va_handle *h)
+{
+    return h->bks && h->N == va::kContractN && h->opt.precision == VA_PREC_MIXED_DW &&
+           h->bks->rs_stage[h->opt.tableau] > 0 && h->opt.stage_records != 0;
+}
+bool deferred_now(const va_handle *h) { return deferred_possible(h) && stages_now(h) && h->fac_v && h->shared_dA; }
+
 // the bundle sweep for the current record layout
 const void *bundle_fwd(const va_handle *h)
 {
@@ -236,7 +256,14 @@ va_status alloc_buffers(va_handle *h)
     h->worst_chunks = per_inst_chunks * B;
     const int64_t big_chunk = (int64_t)rs_big * sizeof(double) * h->chunk_len;
     const int64_t small_chunk = (int64_t)rs_small * sizeof(double) * h->chunk_len;
-    int64_t bytes = std::min<int64_t>(budget, h->worst_chunks * big_chunk);
+    // with the deferred dA, every stored step also needs nsv factor rows (a v
+    // row and an x pointer): the budget is shared in proportion
+    const int64_t rec_bytes = (int64_t)rs_big * sizeof(double);
+    const int64_t fac_per_rec = deferred_possible(h)
+                                    ? (int64_t)h->bks->nsv[h->opt.tableau] * (h->N * (int64_t)sizeof(double) + 8)
+                                    : 0;
+    const int64_t pool_budget = fac_per_rec ? (int64_t)((double)budget * rec_bytes / (rec_bytes + fac_per_rec)) : budget;
+    int64_t bytes = std::min<int64_t>(pool_budget, h->worst_chunks * big_chunk);
     bytes = std::max<int64_t>(bytes, big_chunk);
     h->pool_bytes = (size_t)bytes;
     int64_t links = std::min<int64_t>(h->worst_chunks, bytes / small_chunk);
@@ -268,6 +295,17 @@ va_status alloc_buffers(va_handle *h)
         VA_CUDA(h, cudaMalloc(&h->Aw, NN * sizeof(va::dword)));
         VA_CUDA(h, cudaMalloc(&h->Atw, NN * sizeof(va::dword)));
         VA_CUDA(h, cudaMalloc(&h->dA_part, grid * NN * sizeof(double)));
+        if (fac_per_rec) {
+            // one row set per record the pool can hold
+            const int64_t recs = (int64_t)(h->pool_bytes / (size_t)big_chunk) * h->chunk_len;
+            h->fac_rows = recs * h->bks->nsv[h->opt.tableau];
+            VA_CUDA(h, cudaMalloc(&h->fac_v, (size_t)h->fac_rows * h->N * sizeof(double)));
+            VA_CUDA(h, cudaMalloc(&h->fac_xp, (size_t)h->fac_rows * sizeof(double *)));
+            VA_CUDA(h, cudaMalloc(&h->k_base, ((size_t)B + 1) * sizeof(int)));
+            VA_CUDA(h, cudaMalloc(&h->c_part, (size_t)va::contract_splits(h->sm_count) * NN * sizeof(double)));
+            VA_CUDA(h, cudaMalloc(&h->c_err, sizeof(unsigned)));
+            VA_CUDA(h, va::contract_prepare());
+        }
         for (int t = 0; t < va::kTableaux; t++)
             for (int p = 0; p < 3; p++) {
                 const void *fns[4] = {h->bks->fwd[t][p], h->bks->fwd1[t][p], h->bks->bwd[t][p], h->bks->bwd1[t][p]};
@@ -289,8 +327,10 @@ va_status ensure_buffers(va_handle *h)
         release({(void **)&h->pool_rec, (void **)&h->chunk_prev, (void **)&h->inst_T, (void **)&h->inst_last,
                  (void **)&h->inst_status, (void **)&h->ctl, (void **)&h->inst_t1, (void **)&h->inst_t0,
                  (void **)&h->order_fwd, (void **)&h->order_bwd, (void **)&h->order_work, (void **)&h->inst_work,
-                 (void **)&h->At, (void **)&h->Aw, (void **)&h->Atw, (void **)&h->dA_part});
+                 (void **)&h->At, (void **)&h->Aw, (void **)&h->Atw, (void **)&h->dA_part, (void **)&h->fac_v,
+                 (void **)&h->fac_xp, (void **)&h->k_base, (void **)&h->c_part, (void **)&h->c_err});
         h->pool_bytes = 0;
+        h->fac_rows = 0;
         return st;
     }
     h->buffers_ready = true;
@@ -495,9 +535,27 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
         void *args[] = {&bp};
         const int p = h->opt.precision;
         const int grid = bundle_grid(h);
+        const bool defer = deferred_now(h);
+        if (defer) {
+            VA_CUDA(h, va::enqueue_factor_offsets(h->inst_T, h->inst_status, a.B, h->bks->nsv[h->opt.tableau],
+                                                  h->k_base, s));
+            bp.fac_v = h->fac_v;
+            bp.fac_xp = h->fac_xp;
+            bp.k_base = h->k_base;
+        }
         VA_CUDA(h, cudaLaunchKernel(bundle_bwd(h), dim3(grid), dim3(h->N), args,
                                     h->bks->smem_bwd[p], s));
-        if (h->shared_dA) {
+        if (defer) {
+            va::ContractParams cp{};
+            cp.v = h->fac_v;
+            cp.xp = h->fac_xp;
+            cp.k_total = h->k_base + a.B;
+            cp.partials = h->c_part;
+            cp.splits = va::contract_splits(h->sm_count);
+            cp.error = h->c_err;
+            VA_CUDA(h, cudaMemsetAsync(h->c_err, 0, sizeof(unsigned), s));
+            VA_CUDA(h, va::enqueue_contract(cp, h->shared_dA, s));
+        } else if (h->shared_dA) {
             const int NN = h->N * h->N;
             int dw = p == VA_PREC_MIXED_DW;
             void *rargs[] = {(void *)&h->dA_part, (void *)&grid, (void *)&dw, (void *)&h->shared_dA};
@@ -848,7 +906,8 @@ va_status va_destroy(va_handle *h)
                     h->s_yT,     h->s_dy0,      h->s_dpar,  h->s_nacc,    h->s_status,
                     h->s_nrej,   h->s_lam,      h->s_mu,    h->At,        h->Aw,
                     h->Atw,      h->dA_part,    h->inst_t1, h->scratch, h->order_fwd,
-                    h->order_bwd, h->order_work, h->inst_work, h->inst_t0, h->hist};
+                    h->order_bwd, h->order_work, h->inst_work, h->inst_t0, h->hist, h->fac_v,
+                    h->fac_xp,    h->k_base,    h->c_part,  h->c_err};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);

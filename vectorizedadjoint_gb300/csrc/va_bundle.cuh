@@ -47,7 +47,24 @@ struct BundleParams {
     const dword *Atw;
     double *dA_part;      // [gridDim.x][N][N], transposed per CTA: [j][i] += dA_ij
     int nb;               // instances per CTA (<= NB)
+    // deferred dA (double-word sweeps with stage records; null: the CTA
+    // partials above): factor row k = k_base[b] + n nsv + m of step n, stage m
+    // of instance b holds v = Kbar_m . X_m (packed double-words) and a pointer
+    // to X_m in the step's stage record; the tensor-core contraction
+    // (va_contract.cu) forms dA = sum_k v_k X_k^T from them
+    double *fac_v;        // [K][N]
+    const double **fac_xp;// [K]
+    const int *k_base;    // [B + 1]
 };
+
+// stages whose factor row can be non-zero: all but a last stage of weight 0
+// (the FSAL stage of Dormand-Prince, whose adjoint seed b_s h lambda is 0
+// and which feeds no other stage)
+template <class Tab>
+__host__ __device__ constexpr int factor_stages()
+{
+    return Tab::S - (Tab::b(Tab::S - 1) == 0.0 ? 1 : 0);
+}
 
 template <class S>
 __device__ __forceinline__ S load_A(const double *A, const dword *Aw, size_t k)
@@ -557,8 +574,9 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel(Bu
     }
     // this CTA's partial of dA, transposed: part[jj][i] += dA_i,jj
     double *part = bp.dA_part + (size_t)blockIdx.x * NT * NT;
-    for (int jj = 0; jj < NT; jj++)
-        part[(size_t)jj * NT + i] = 0.0;
+    if (!(ST && bp.fac_v))
+        for (int jj = 0; jj < NT; jj++)
+            part[(size_t)jj * NT + i] = 0.0;
 
     for (;;) {
         bool any = false;
@@ -697,8 +715,26 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel(Bu
             }
             __syncthreads();
         }
+        if constexpr (ST) {
+            if (bp.fac_v) {
+                // deferred dA: this step's factor rows v_m (and pointers to X_m)
+                constexpr int NSV = factor_stages<Tab>();
+#pragma unroll
+                for (int b = 0; b < NB; b++) {
+                    if (!step[b])
+                        continue;
+                    const size_t k0 = (size_t)bp.k_base[inst[b]] + (size_t)j[b] * NSV;
+#pragma unroll
+                    for (int m = 0; m < NSV; m++) {
+                        bp.fac_v[(k0 + m) * NT + i] = dw_pack(vall[((size_t)m * NT + i) * NB + b]);
+                        if (i == 0)
+                            bp.fac_xp[k0 + m] = srec[b] + 2 + (size_t)m * NT;
+                    }
+                }
+            }
+        }
         // dA partial: part[jj][i] += sum_{m,b} v_{m,b,i} x_{m,b,jj}
-        {
+        if (!(ST && bp.fac_v)) {
             S vi[NS][NB];
 #pragma unroll
             for (int m = 0; m < NS; m++)

@@ -414,8 +414,9 @@ __global__ void dense_rows_kernel(const double *x, int K, const double **xp)
         xp[k] = x + (size_t)k * kContractN;
 }
 
-// dA[i][j] = sum over splits, in split order, of partial[split][j][i]
-__global__ void reduce_partials_kernel(const double *part, int nparts, double *dA)
+// dA[i][j] = sum over splits, in split order, of partial[split][j][i]; NaN
+// everywhere when a wait of the contraction gave up
+__global__ void reduce_partials_kernel(const double *part, int nparts, const unsigned *error, double *dA)
 {
     constexpr int NT = kContractN;
     const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; // k = j * NT + i
@@ -424,6 +425,8 @@ __global__ void reduce_partials_kernel(const double *part, int nparts, double *d
     double s = 0.0;
     for (int c = 0; c < nparts; c++)
         s += part[(size_t)c * NT * NT + k];
+    if (*error)
+        s = __longlong_as_double(0x7ff8000000000000ll);
     const size_t j = k / NT, i = k % NT;
     dA[i * NT + j] = s;
 }
@@ -437,22 +440,19 @@ cudaError_t enqueue_factor_offsets(const int *inst_T, const int *inst_status, in
     return cudaGetLastError();
 }
 
+cudaError_t contract_prepare()
+{
+    return cudaFuncSetAttribute(contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kContractSmem);
+}
+
 cudaError_t enqueue_contract(const ContractParams &p, double *dA, cudaStream_t s)
 {
-    static bool attr = false;
-    if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)kContractSmem);
-        if (e != cudaSuccess)
-            return e;
-        attr = true;
-    }
     contract_kernel<<<kContractTiles * p.splits, 256, kContractSmem, s>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
     constexpr int NN = kContractN * kContractN;
-    reduce_partials_kernel<<<(NN + 255) / 256, 256, 0, s>>>(p.partials, p.splits, dA);
+    reduce_partials_kernel<<<(NN + 255) / 256, 256, 0, s>>>(p.partials, p.splits, p.error, dA);
     return cudaGetLastError();
 }
 
@@ -489,7 +489,7 @@ extern "C" VA_API int32_t va_contract_dA(int32_t K, const double *v, const doubl
         p.partials = part;
         p.splits = splits;
         p.error = err;
-        if (va::enqueue_contract(p, dA, s) != cudaSuccess)
+        if (va::contract_prepare() != cudaSuccess || va::enqueue_contract(p, dA, s) != cudaSuccess)
             st = VA_CUDA_ERROR;
         unsigned e = 0;
         if (cudaMemcpyAsync(&e, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||

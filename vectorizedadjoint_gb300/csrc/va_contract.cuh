@@ -99,10 +99,12 @@ __host__ __device__ __forceinline__ void split_digits(float hi, float lo, int e,
     }
 }
 
-// Entry points of va_contract.cu (CTAs per output tile for a GPU; the row
-// offsets of each instance's factor rows; the contraction plus the
-// fixed-order sum of its partials into dA[256][256]).
+// Entry points of va_contract.cu (CTAs per output tile for a GPU; the
+// kernel's shared-memory attribute, set once before any launch or capture;
+// the row offsets of each instance's factor rows; the contraction plus the
+// fixed-order sum of its partials into dA[256][256], NaN if it failed).
 int contract_splits(int sm_count);
+cudaError_t contract_prepare();
 cudaError_t enqueue_factor_offsets(const int *inst_T, const int *inst_status, int B, int nsv, int *k_base,
                                    cudaStream_t s);
 cudaError_t enqueue_contract(const ContractParams &p, double *dA, cudaStream_t s);

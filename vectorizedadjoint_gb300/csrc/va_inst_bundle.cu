@@ -23,6 +23,7 @@ static void fill_fixed(BundleKernelSet &k)
     k.bwd[I][2] = (const void *)backward_bundle_kernel<NT, NW, Tab, dword, true>;
     k.bwd1[I][2] = (const void *)backward_bundle_kernel<NT, NW, Tab, dword>;
     k.rs_stage[I] = bundle_stage_record_doubles(NT, Tab::S);
+    k.nsv[I] = factor_stages<Tab>();
 }
 
 template <int NT>
@@ -48,6 +49,8 @@ static BundleKernelSet make_bundle(void (*fill_fp64)(BundleKernelSet &))
     k.bwd1[1][2] = (const void *)backward_bundle_kernel<NT, NW, TabCK54, dword>;
     k.rs_stage[0] = bundle_stage_record_doubles(NT, TabDopri5::S);
     k.rs_stage[1] = bundle_stage_record_doubles(NT, TabCK54::S);
+    k.nsv[0] = factor_stages<TabDopri5>();
+    k.nsv[1] = factor_stages<TabCK54>();
     fill_fixed<NT, 3, TabRK4>(k);
     fill_fixed<NT, 4, TabEuler>(k);
     const size_t sz[3] = {sizeof(double), sizeof(float), sizeof(dword)};

@@ -105,6 +105,7 @@ struct BundleKernelSet {
     size_t smem_fwd[3], smem_bwd[3]; // dynamic shared memory per precision
     const void *prepare;   // prepare_A_kernel: A -> A^T and double-word copies
     const void *reduce;    // reduce_dA_kernel: CTA partials -> dA
+    int nsv[kTableaux];    // factor rows per step of the deferred dA (stages that can be non-zero)
 };
 const BundleKernelSet *kernels_glv_shared(int n); // n = 64 or 256
 
