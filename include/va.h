@@ -272,9 +272,17 @@ VA_API va_status va_forward_frozen(va_handle *h, int32_t count, int32_t times_st
                                    const int32_t *n_steps, const double *y0, const double *params,
                                    const double *shared, double *yT, void *stream);
 
-/* Picks the block size and resident blocks per SM of both sweeps by timing
- * candidate launches on the given inputs (device pointers); the choice is
- * kept in the handle.  Runs forward+backward several times. */
+/* Picks the launch shape by timing candidate runs of both sweeps on the given
+ * inputs (device pointers) and keeps it in the handle: for the one-thread
+ * and lane-group models the block size and resident blocks per SM of each
+ * sweep, for the shared-matrix model the bundle width (instances per CTA:
+ * 2 or 4).  Runs forward+backward several times per candidate.  The choice
+ * is also kept on disk, one line per problem (GPU, model, sizes, tableau,
+ * precision, record layout, batch size's power of two), in the file named
+ * by the environment variable VA_AUTOTUNE_CACHE ("" or "off": none), else
+ * $XDG_CACHE_HOME/vectorizedadjoint_gb300/autotune.tsv or
+ * $HOME/.cache/vectorizedadjoint_gb300/autotune.tsv; a later call for the
+ * same problem applies the stored shape without timing anything. */
 VA_API va_status va_autotune(va_handle *h, int32_t cost, const double *y0, const double *params,
                       const double *t0, const double *t1, void *stream);
 

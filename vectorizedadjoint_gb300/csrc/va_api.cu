@@ -5,8 +5,11 @@
 // adjointSolve (lib/include/backpropagation.hpp) for built-in models.
 #include <cuda_runtime.h>
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <initializer_list>
 #include <string>
@@ -98,6 +101,7 @@ struct va_handle {
     double *shared_dA = nullptr;
     double *At = nullptr, *dA_part = nullptr;
     va::dword *Aw = nullptr, *Atw = nullptr;
+    bool bundle_alt = false; // the other bundle width (va_autotune's choice)
     // deferred dA on the tensor pipe (N = 256, double-word sweeps with stage
     // records): factor rows, their x pointers, per-instance row offsets,
     // contraction partials and its error flag
@@ -199,16 +203,43 @@ bool deferred_possible(const va_handle *h)
 }
 bool deferred_now(const va_handle *h) { return deferred_possible(h) && stages_now(h) && h->fac_v && h->shared_dA; }
 
-// the bundle sweep for the current record layout
+// whether the other bundle width is compiled for the handle's tableau and precision
+bool bundle_alt_available(const va_handle *h)
+{
+    const int t = h->opt.tableau, p = h->opt.precision;
+    return h->bks && h->bks->fwd_alt[t][p] && h->bks->bwd_alt[t][p];
+}
+bool use_alt(const va_handle *h) { return h->bundle_alt && bundle_alt_available(h); }
+int bundle_nb(const va_handle *h)
+{
+    const int p = h->opt.precision;
+    return use_alt(h) ? h->bks->nb_alt[p] : h->bks->nb[p];
+}
+size_t bundle_smem_fwd(const va_handle *h)
+{
+    const int p = h->opt.precision;
+    return use_alt(h) ? h->bks->smem_fwd_alt[p] : h->bks->smem_fwd[p];
+}
+size_t bundle_smem_bwd(const va_handle *h)
+{
+    const int p = h->opt.precision;
+    return use_alt(h) ? h->bks->smem_bwd_alt[p] : h->bks->smem_bwd[p];
+}
+
+// the bundle sweep for the current record layout and width
 const void *bundle_fwd(const va_handle *h)
 {
     const int t = h->opt.tableau, p = h->opt.precision;
-    return !stages_now(h) && h->bks->fwd1[t][p] ? h->bks->fwd1[t][p] : h->bks->fwd[t][p];
+    const auto &f = use_alt(h) ? h->bks->fwd_alt : h->bks->fwd;
+    const auto &f1 = use_alt(h) ? h->bks->fwd1_alt : h->bks->fwd1;
+    return !stages_now(h) && f1[t][p] ? f1[t][p] : f[t][p];
 }
 const void *bundle_bwd(const va_handle *h)
 {
     const int t = h->opt.tableau, p = h->opt.precision;
-    return !stages_now(h) && h->bks->bwd1[t][p] ? h->bks->bwd1[t][p] : h->bks->bwd[t][p];
+    const auto &b = use_alt(h) ? h->bks->bwd_alt : h->bks->bwd;
+    const auto &b1 = use_alt(h) ? h->bks->bwd1_alt : h->bks->bwd1;
+    return !stages_now(h) && b1[t][p] ? b1[t][p] : b[t][p];
 }
 
 void record_layout(va_handle *h)
@@ -289,7 +320,8 @@ va_status alloc_buffers(va_handle *h)
     }
     if (h->bks) {
         const size_t NN = (size_t)h->N * h->N;
-        const int nb = std::min({h->bks->nb[0], h->bks->nb[1], h->bks->nb[2]}); // the most CTAs
+        const int nb = std::min({h->bks->nb[0], h->bks->nb[1], h->bks->nb[2], h->bks->nb_alt[0], h->bks->nb_alt[1],
+                                 h->bks->nb_alt[2]}); // the most CTAs
         const size_t grid = ((size_t)B + nb - 1) / nb;
         VA_CUDA(h, cudaMalloc(&h->At, NN * sizeof(double)));
         VA_CUDA(h, cudaMalloc(&h->Aw, NN * sizeof(va::dword)));
@@ -308,11 +340,16 @@ va_status alloc_buffers(va_handle *h)
         }
         for (int t = 0; t < va::kTableaux; t++)
             for (int p = 0; p < 3; p++) {
-                const void *fns[4] = {h->bks->fwd[t][p], h->bks->fwd1[t][p], h->bks->bwd[t][p], h->bks->bwd1[t][p]};
-                for (int f = 0; f < 4; f++)
+                const void *fns[8] = {h->bks->fwd[t][p],     h->bks->fwd1[t][p],     h->bks->bwd[t][p],
+                                      h->bks->bwd1[t][p],    h->bks->fwd_alt[t][p],  h->bks->fwd1_alt[t][p],
+                                      h->bks->bwd_alt[t][p], h->bks->bwd1_alt[t][p]};
+                const size_t sm[8] = {h->bks->smem_fwd[p],     h->bks->smem_fwd[p],     h->bks->smem_bwd[p],
+                                      h->bks->smem_bwd[p],     h->bks->smem_fwd_alt[p], h->bks->smem_fwd_alt[p],
+                                      h->bks->smem_bwd_alt[p], h->bks->smem_bwd_alt[p]};
+                for (int f = 0; f < 8; f++)
                     if (fns[f])
                         VA_CUDA(h, cudaFuncSetAttribute(fns[f], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                        (int)(f < 2 ? h->bks->smem_fwd[p] : h->bks->smem_bwd[p])));
+                                                        (int)sm[f]));
             }
     }
     return VA_OK;
@@ -345,13 +382,13 @@ va::BundleParams bundle_params(va_handle *h)
     bp.Aw = h->Aw;
     bp.Atw = h->Atw;
     bp.dA_part = h->dA_part;
-    bp.nb = h->bks->nb[h->opt.precision];
+    bp.nb = bundle_nb(h);
     return bp;
 }
 
 int bundle_grid(va_handle *h)
 {
-    const int nb = h->bks->nb[h->opt.precision];
+    const int nb = bundle_nb(h);
     return (h->prob.batch + nb - 1) / nb;
 }
 
@@ -475,9 +512,7 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
         va::BundleParams bp = bundle_params(h);
         bp.f = a;
         void *args[] = {&bp};
-        const int p = h->opt.precision;
-        VA_CUDA(h, cudaLaunchKernel(bundle_fwd(h), dim3(bundle_grid(h)), dim3(h->N), args,
-                                    h->bks->smem_fwd[p], s));
+        VA_CUDA(h, cudaLaunchKernel(bundle_fwd(h), dim3(bundle_grid(h)), dim3(h->N), args, bundle_smem_fwd(h), s));
         h->fwd_grid = bundle_grid(h);
         h->fwd_block = h->N;
         return VA_OK;
@@ -543,8 +578,7 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
             bp.fac_xp = h->fac_xp;
             bp.k_base = h->k_base;
         }
-        VA_CUDA(h, cudaLaunchKernel(bundle_bwd(h), dim3(grid), dim3(h->N), args,
-                                    h->bks->smem_bwd[p], s));
+        VA_CUDA(h, cudaLaunchKernel(bundle_bwd(h), dim3(grid), dim3(h->N), args, bundle_smem_bwd(h), s));
         if (defer) {
             va::ContractParams cp{};
             cp.v = h->fac_v;
@@ -607,18 +641,89 @@ struct AutotuneEvents {
     }
 };
 
-// Times every (block size, resident blocks per SM) candidate of both sweeps
-// and leaves the best of each in the handle.
-va_status autotune_sweep(va_handle *h, int32_t cost, const double *y0, const double *params,
-                         const double *t0, const double *t1, cudaStream_t s, AutotuneEvents &ev)
+// A tuned launch shape: block size and resident blocks per SM of each sweep
+// (one-thread and lane-group models) and the bundle width (shared matrix).
+struct TunedShape {
+    int fb = 0, fbps = 0, bb = 0, bbps = 0, alt = 0;
+};
+
+// grid of a sweep launched with `block` threads and at most `bps` resident
+// blocks per SM (never more CTAs than the batch needs)
+int grid_of(va_handle *h, const void *fn, int block, int bps)
 {
+    const int occ = std::max(1, occupancy_of(h, fn, block));
+    const long need = ((long)h->prob.batch * h->ks->tpi + block - 1) / block;
+    return (int)std::max(1L, std::min((long)h->sm_count * std::min(bps, occ), need));
+}
+
+void apply_shape(va_handle *h, const TunedShape &t)
+{
+    if (h->bks) {
+        h->bundle_alt = t.alt != 0 && bundle_alt_available(h);
+        return;
+    }
     const void *ffn = h->ks->fwd[h->opt.tableau][h->opt.precision];
     const void *bfn = h->ks->bwd[h->opt.tableau][h->opt.precision];
+    h->fwd_block = t.fb;
+    h->fwd_grid = grid_of(h, ffn, t.fb, t.fbps);
+    h->bwd_block = t.bb;
+    h->bwd_grid = grid_of(h, bfn, t.bb, t.bbps);
+}
+
+// Forward and backward once untimed, then the best of two timed runs.
+va_status time_sweeps(va_handle *h, int32_t cost, const double *y0, const double *params, const double *t0,
+                      const double *t1, cudaStream_t s, AutotuneEvents &ev, float &tf, float &tb)
+{
+    cudaEvent_t e0 = ev.e[0], e1 = ev.e[1], e2 = ev.e[2];
+    tf = tb = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+        VA_CUDA(h, cudaEventRecord(e0, s));
+        va_status st = enqueue_forward(h, y0, params, t0, t1, h->s_yT, nullptr, nullptr, h->s_status, s);
+        if (st != VA_OK)
+            return st;
+        VA_CUDA(h, cudaEventRecord(e1, s));
+        st = enqueue_backward(h, params, nullptr, nullptr, cost, h->s_dy0, h->s_dpar, h->s_status, s);
+        if (st != VA_OK)
+            return st;
+        VA_CUDA(h, cudaEventRecord(e2, s));
+        VA_CUDA(h, cudaEventSynchronize(e2));
+        float a = 0, b = 0;
+        VA_CUDA(h, cudaEventElapsedTime(&a, e0, e1));
+        VA_CUDA(h, cudaEventElapsedTime(&b, e1, e2));
+        if (rep > 0) {
+            tf = std::min(tf, a);
+            tb = std::min(tb, b);
+        }
+    }
+    return VA_OK;
+}
+
+// Times the candidates and leaves the best shape in `best`.  One-thread and
+// lane-group models: every (block size, resident blocks per SM) of each
+// sweep; shared-matrix bundles: both compiled bundle widths.
+va_status autotune_sweep(va_handle *h, int32_t cost, const double *y0, const double *params,
+                         const double *t0, const double *t1, cudaStream_t s, AutotuneEvents &ev, TunedShape &best)
+{
     for (cudaEvent_t &x : ev.e)
         VA_CUDA(h, cudaEventCreate(&x));
-    cudaEvent_t e0 = ev.e[0], e1 = ev.e[1], e2 = ev.e[2];
+    if (h->bks) {
+        float best_t = 1e30f;
+        for (int alt = 0; alt <= (bundle_alt_available(h) ? 1 : 0); alt++) {
+            h->bundle_alt = alt != 0;
+            float tf, tb;
+            const va_status st = time_sweeps(h, cost, y0, params, t0, t1, s, ev, tf, tb);
+            if (st != VA_OK)
+                return st;
+            if (tf + tb < best_t) {
+                best_t = tf + tb;
+                best.alt = alt;
+            }
+        }
+        return VA_OK;
+    }
+    const void *ffn = h->ks->fwd[h->opt.tableau][h->opt.precision];
+    const void *bfn = h->ks->bwd[h->opt.tableau][h->opt.precision];
     float best_f = 1e30f, best_b = 1e30f;
-    int bf_block = h->fwd_block, bf_grid = h->fwd_grid, bb_block = h->bwd_block, bb_grid = h->bwd_grid;
     const int blocks[] = {64, 128, 256};
     for (int blk : blocks) {
         const int occf = occupancy_of(h, ffn, blk), occb = occupancy_of(h, bfn, blk);
@@ -627,48 +732,104 @@ va_status autotune_sweep(va_handle *h, int32_t cost, const double *y0, const dou
         // backward, issue rate more in the forward)
         const int maxocc = std::max(1, std::max(occf, occb));
         for (int bps = 1; bps <= maxocc; bps++) {
-            h->fwd_block = h->bwd_block = blk;
-            long need = ((long)h->prob.batch * h->ks->tpi + blk - 1) / blk;
-            h->fwd_grid = (int)std::max(1L, std::min((long)h->sm_count * std::min(bps, std::max(occf, 1)), need));
-            h->bwd_grid = (int)std::max(1L, std::min((long)h->sm_count * std::min(bps, std::max(occb, 1)), need));
-            // a warm-up run, then the best of two timed runs
-            float cand_f = 1e30f, cand_b = 1e30f;
-            for (int rep = 0; rep < 3; rep++) {
-                VA_CUDA(h, cudaEventRecord(e0, s));
-                va_status st = enqueue_forward(h, y0, params, t0, t1, h->s_yT, nullptr, nullptr, h->s_status, s);
-                if (st != VA_OK)
-                    return st;
-                VA_CUDA(h, cudaEventRecord(e1, s));
-                st = enqueue_backward(h, params, nullptr, nullptr, cost, h->s_dy0, h->s_dpar, h->s_status, s);
-                if (st != VA_OK)
-                    return st;
-                VA_CUDA(h, cudaEventRecord(e2, s));
-                VA_CUDA(h, cudaEventSynchronize(e2));
-                float tf = 0, tb = 0;
-                VA_CUDA(h, cudaEventElapsedTime(&tf, e0, e1));
-                VA_CUDA(h, cudaEventElapsedTime(&tb, e1, e2));
-                if (rep > 0) {
-                    cand_f = std::min(cand_f, tf);
-                    cand_b = std::min(cand_b, tb);
-                }
+            TunedShape cand{blk, bps, blk, bps, 0};
+            apply_shape(h, cand);
+            float tf, tb;
+            const va_status st = time_sweeps(h, cost, y0, params, t0, t1, s, ev, tf, tb);
+            if (st != VA_OK)
+                return st;
+            if (tf < best_f) {
+                best_f = tf;
+                best.fb = blk;
+                best.fbps = bps;
             }
-            if (cand_f < best_f) {
-                best_f = cand_f;
-                bf_block = blk;
-                bf_grid = h->fwd_grid;
-            }
-            if (cand_b < best_b) {
-                best_b = cand_b;
-                bb_block = blk;
-                bb_grid = h->bwd_grid;
+            if (tb < best_b) {
+                best_b = tb;
+                best.bb = blk;
+                best.bbps = bps;
             }
         }
     }
-    h->fwd_block = bf_block;
-    h->fwd_grid = bf_grid;
-    h->bwd_block = bb_block;
-    h->bwd_grid = bb_grid;
     return VA_OK;
+}
+
+// ------------------------------------------------------ autotune cache
+//
+// One line per tuned problem, "key<TAB>fb fbps bb bbps alt", in the file
+// named by $VA_AUTOTUNE_CACHE ("" or "off": no cache), else
+// $XDG_CACHE_HOME/vectorizedadjoint_gb300/autotune.tsv or
+// $HOME/.cache/vectorizedadjoint_gb300/autotune.tsv.  The key: GPU name and
+// SM count, model (and a model compiled outside the library's name), n,
+// npar, nout, tableau, precision, stage records, checkpoint stride, step
+// factor and the batch size's power of two.  The last matching line wins.
+
+std::string cache_path()
+{
+    const char *e = std::getenv("VA_AUTOTUNE_CACHE");
+    if (e)
+        return (!*e || !std::strcmp(e, "off")) ? std::string() : std::string(e);
+    const char *x = std::getenv("XDG_CACHE_HOME"), *home = std::getenv("HOME");
+    std::string dir = (x && *x) ? std::string(x) : ((home && *home) ? std::string(home) + "/.cache" : std::string());
+    return dir.empty() ? std::string() : dir + "/vectorizedadjoint_gb300/autotune.tsv";
+}
+
+std::string cache_key(const va_handle *h)
+{
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess)
+        return std::string();
+    int lb = 0;
+    while ((1L << (lb + 1)) <= (long)h->prob.batch)
+        lb++;
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s|%d|%d%s%s|%d|%d|%d|%d|%d|%d|%d|%d|%d", prop.name, h->sm_count,
+                  h->prob.model, h->user ? ":" : "", h->user && h->user->name ? h->user->name : "", h->prob.n,
+                  h->prob.npar, h->prob.nout, h->opt.tableau, h->opt.precision, (int)h->stages_on, h->stride,
+                  h->opt.step_pow, lb);
+    for (char *c = buf; *c; c++)
+        if (*c == '\t' || *c == '\n')
+            *c = ' ';
+    return buf;
+}
+
+bool cache_lookup(const std::string &key, TunedShape &t)
+{
+    const std::string path = cache_path();
+    if (path.empty() || key.empty())
+        return false;
+    FILE *f = std::fopen(path.c_str(), "r");
+    if (!f)
+        return false;
+    char line[1024];
+    bool found = false;
+    while (std::fgets(line, sizeof(line), f)) {
+        char *tab = std::strchr(line, '\t');
+        if (!tab)
+            continue;
+        *tab = 0;
+        TunedShape v;
+        if (key == line && std::sscanf(tab + 1, "%d %d %d %d %d", &v.fb, &v.fbps, &v.bb, &v.bbps, &v.alt) == 5) {
+            t = v;
+            found = true;
+        }
+    }
+    std::fclose(f);
+    return found;
+}
+
+void cache_store(const std::string &key, const TunedShape &t)
+{
+    const std::string path = cache_path();
+    if (path.empty() || key.empty())
+        return;
+    // create the directories of the path (an existing one is fine)
+    for (size_t k = path.find('/', 1); k != std::string::npos; k = path.find('/', k + 1))
+        mkdir(path.substr(0, k).c_str(), 0755);
+    FILE *f = std::fopen(path.c_str(), "a");
+    if (!f)
+        return;
+    std::fprintf(f, "%s\t%d %d %d %d %d\n", key.c_str(), t.fb, t.fbps, t.bb, t.bbps, t.alt);
+    std::fclose(f);
 }
 
 void drop_graph(va_handle *h)
@@ -1322,21 +1483,30 @@ va_status va_autotune(va_handle *h, int32_t cost, const double *y0, const double
         st = ensure_scratch(h);
     if (st != VA_OK)
         return st;
-    if (h->bks)
-        return VA_OK; // bundle kernels: one CTA of N threads per bundle, nothing to tune
+    const std::string key = cache_key(h);
+    TunedShape t;
+    if (cache_lookup(key, t) && (h->bks || (t.fb > 0 && t.bb > 0 && t.fbps > 0 && t.bbps > 0))) {
+        apply_shape(h, t);
+        drop_graph(h);
+        return VA_OK;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     // the launch shape before tuning, restored if a candidate run fails
     const int prev[4] = {h->fwd_block, h->fwd_grid, h->bwd_block, h->bwd_grid};
+    const bool prev_alt = h->bundle_alt;
     AutotuneEvents ev;
-    st = autotune_sweep(h, cost, y0, params, t0, t1, s, ev);
+    st = autotune_sweep(h, cost, y0, params, t0, t1, s, ev, t);
     if (st != VA_OK) {
         h->fwd_block = prev[0];
         h->fwd_grid = prev[1];
         h->bwd_block = prev[2];
         h->bwd_grid = prev[3];
+        h->bundle_alt = prev_alt;
         drop_graph(h);
         return st;
     }
+    apply_shape(h, t);
+    cache_store(key, t);
     drop_graph(h);
     h->forward_done = true;
     return VA_OK;

@@ -61,6 +61,20 @@ static BundleKernelSet make_bundle(void (*fill_fp64)(BundleKernelSet &))
     }
     k.prepare = (const void *)prepare_A_kernel<NT>;
     k.reduce = (const void *)reduce_dA_kernel<NT>;
+    if constexpr (NT == 64) {
+        fill_bundle_alt64(k);
+        fill_bundle_alt_fp64_64(k);
+    } else {
+        fill_bundle_alt256(k);
+        fill_bundle_alt_fp64_256(k);
+    }
+    k.nb_alt[0] = k.nb_alt[1] = kBundleNBdw;
+    k.nb_alt[2] = kBundleNB;
+    for (int p = 0; p < 3; p++) {
+        const size_t nb = k.nb_alt[p];
+        k.smem_fwd_alt[p] = sz[p] * NT * nb + sizeof(double) * (NT / 32) * nb + sizeof(int) * nb;
+        k.smem_bwd_alt[p] = 3 * sz[p] * (size_t)TabDopri5::S * NT * nb;
+    }
     return k;
 }
 

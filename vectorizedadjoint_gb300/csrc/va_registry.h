@@ -106,7 +106,19 @@ struct BundleKernelSet {
     const void *prepare;   // prepare_A_kernel: A -> A^T and double-word copies
     const void *reduce;    // reduce_dA_kernel: CTA partials -> dA
     int nsv[kTableaux];    // factor rows per step of the deferred dA (stages that can be non-zero)
+    // the other bundle width, one more point for the autotuner (null where not
+    // compiled: the 5(4) pairs only): FP64 / FP32 bundles of kBundleNBdw,
+    // double-word bundles of kBundleNB
+    int nb_alt[3];
+    const void *fwd_alt[kTableaux][3], *bwd_alt[kTableaux][3];
+    const void *fwd1_alt[kTableaux][3], *bwd1_alt[kTableaux][3];
+    size_t smem_fwd_alt[3], smem_bwd_alt[3];
 };
+// alternate-width bundle kernels (va_inst_bundle_alt.cu, va_inst_bundle_alt_fp64.cu)
+void fill_bundle_alt64(BundleKernelSet &k);
+void fill_bundle_alt256(BundleKernelSet &k);
+void fill_bundle_alt_fp64_64(BundleKernelSet &k);
+void fill_bundle_alt_fp64_256(BundleKernelSet &k);
 const BundleKernelSet *kernels_glv_shared(int n); // n = 64 or 256
 
 } // namespace va
