@@ -64,8 +64,16 @@ DW_FP32_FLOPS = {
     ("vdp", "dopri5"): (1611.2, 1682.2),
     ("dho", "ck54"): (1414.5, 1566.0),
     ("glv", "dopri5"): (16898.1, 25416.7),
-    ("glv_shared", "dopri5"): (6353397.4, 13211627.4),
+    # shared-matrix backward: the A^T v products only; dA is contracted
+    # afterwards on the tensor pipe (a kernel of its own)
+    ("glv_shared", "dopri5"): (6353397.4, 6316765.2),
 }
+
+# Models whose backward phase is more than one kernel: the shared-matrix
+# backward sweep is followed by the dA contraction (ncu launch list: forward
+# 52%, backward sweep 40%, contraction 8%), so the forward sweep is the
+# single dominant kernel whatever the phase times say.
+DOMINANT = {"glv_shared": "forward"}
 
 
 class Clocks:
@@ -253,7 +261,7 @@ def roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted):
     run's attempts and steps) against cuBLAS SGEMM; mixed: the algorithmic
     count, executed in FP32, against SGEMM.  Every mode also reports the
     FP64-equivalent rate (algorithmic FP64 FLOPs / time) against DGEMM."""
-    fwd_dom = fms >= bms
+    fwd_dom = DOMINANT.get(c["model"], "forward" if fms >= bms else "backward") == "forward"
     kernel, ms = ("forward", fms) if fwd_dom else ("backward", bms)
     alg = fl_f if fwd_dom else fl_b
     peak64 = fp64_peak_tflops(torch)

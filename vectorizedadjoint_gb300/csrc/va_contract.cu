@@ -185,6 +185,7 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
         const int i = t & 127, h = t >> 7;
         const double *col = p.v + (size_t)ti * kContractTileM + i;
         float m = 0.0f;
+#pragma unroll
         for (int r = 0; r < 32; r++) {
             const int k = k0 + 32 * h + r;
             if (k < K)
@@ -196,6 +197,7 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
     {
         const int j = t & 63, q = t >> 6;
         float m = 0.0f;
+#pragma unroll
         for (int r = 0; r < 16; r++) {
             const int k = k0 + 16 * q + r;
             if (k < K)
@@ -217,7 +219,7 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
         const int i = t & 127, h = t >> 7;
         const double *col = p.v + (size_t)ti * kContractTileM + i;
         const int e = ev[i];
-#pragma unroll 1
+#pragma unroll 2
         for (int g = 0; g < 4; g++) {
             const int kg = 4 * h + g;
             double vals[8];
@@ -234,7 +236,7 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
         const int j = t & 63, q = t >> 6;
         const int e = ex[j];
         uint8_t *xs = stage + kTileVBytes;
-#pragma unroll 1
+#pragma unroll 2
         for (int g = 0; g < 2; g++) {
             const int kg = 2 * q + g;
             double vals[8];
@@ -245,6 +247,25 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
             }
             slice_row8(vals, e, xs + (size_t)kg * 1024 + j * 16, (size_t)kContractKC * kContractTileN * 2);
         }
+    }
+}
+
+// Prefetch of chunk c's rows of the CTA's tile into L2 (the factor rows are
+// read once from DRAM; the slicing loads then wait on L2 instead)
+__device__ __forceinline__ void prefetch_chunk(const ContractParams &p, int c, int K, int ti, int tj)
+{
+    const int t = threadIdx.x;
+    const int kv = c * kContractKC + (t >> 2);
+    if (kv < K) {
+        const double *row = p.v + (size_t)kv * kContractN + ti * kContractTileM + (t & 3) * 32;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(row));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(row + 16));
+    }
+    const int kx = c * kContractKC + (t & 63);
+    if (t < 128 && kx < K) {
+        const double *row = p.xp[kx] + tj * kContractTileN + (t >> 6) * 32;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(row));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(row + 16));
     }
 }
 
@@ -348,8 +369,11 @@ __global__ void __launch_bounds__(256, 1) contract_kernel(ContractParams p)
     const int n = c1 - c0;
     for (int idx = 0; idx < n; idx++) {
         const int st = idx & 1;
-        if (ok)
+        if (ok) {
             slice_chunk(p, c0 + idx, K, ti, tj, stages[st], ev_s[st], ex_s[st], red);
+            if (idx + 1 < n)
+                prefetch_chunk(p, c0 + idx + 1, K, ti, tj);
+        }
         // the digit planes, written by this CTA's threads, feed the tensor core
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
