@@ -154,13 +154,14 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
 
 // One column's 8 consecutive rows (a core-matrix row of 16 bytes) as Q digit
 // planes: vals are packed double-words, e the column's exponent.
-__device__ __forceinline__ void slice_row8(const double (&vals)[8], int e, uint8_t *plane0, size_t plane_stride)
+__device__ __forceinline__ void slice_row8(const double (&vals)[8], DigitScale sc, uint8_t *plane0,
+                                           size_t plane_stride)
 {
     float d[8][kContractQ];
 #pragma unroll
     for (int r = 0; r < 8; r++) {
         const dword w = dw_unpack(vals[r]);
-        split_digits(w.hi, w.lo, e, d[r]);
+        split_digits(w.hi, w.lo, sc, d[r]);
     }
 #pragma unroll
     for (int s = 0; s < kContractQ; s++) {
@@ -218,7 +219,7 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
     {
         const int i = t & 127, h = t >> 7;
         const double *col = p.v + (size_t)ti * kContractTileM + i;
-        const int e = ev[i];
+        const DigitScale sc = digit_scale(ev[i]);
 #pragma unroll 2
         for (int g = 0; g < 4; g++) {
             const int kg = 4 * h + g;
@@ -228,13 +229,13 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
                 const int k = k0 + 8 * kg + r;
                 vals[r] = k < K ? __ldg(col + (size_t)k * kContractN) : 0.0;
             }
-            slice_row8(vals, e, stage + (size_t)kg * 2048 + i * 16, (size_t)kContractKC * kContractTileM * 2);
+            slice_row8(vals, sc, stage + (size_t)kg * 2048 + i * 16, (size_t)kContractKC * kContractTileM * 2);
         }
     }
     // digits: x planes [slice][kgroup 8][row 64][8] (plane = 8 KB, kgroup = 1 KB)
     {
         const int j = t & 63, q = t >> 6;
-        const int e = ex[j];
+        const DigitScale sc = digit_scale(ex[j]);
         uint8_t *xs = stage + kTileVBytes;
 #pragma unroll 2
         for (int g = 0; g < 2; g++) {
@@ -245,7 +246,7 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
                 const int k = k0 + 8 * kg + r;
                 vals[r] = k < K ? __ldg(p.xp[k] + tj * kContractTileN + j) : 0.0;
             }
-            slice_row8(vals, e, xs + (size_t)kg * 1024 + j * 16, (size_t)kContractKC * kContractTileN * 2);
+            slice_row8(vals, sc, xs + (size_t)kg * 1024 + j * 16, (size_t)kContractKC * kContractTileN * 2);
         }
     }
 }
@@ -299,17 +300,26 @@ __device__ __forceinline__ void issue_chunk(uint32_t tmem_acc, const uint8_t *st
 __device__ __forceinline__ void fold_chunk(uint32_t tmem_row, const int *ev, const int *ex, int row, int col0,
                                            float (&ah)[32], float (&al)[32])
 {
+    // R_g 2^(esum - 8g) = (R_g 2^(-8g)) 2^esum: two exact multiplications by
+    // normal powers of two when -102 <= esum <= 103 (|R_g| < 2^24, so every
+    // product is a normal float); ldexpf for columns outside that range
     int esum[32];
+    float p2[32];
+    bool fast = true;
 #pragma unroll
-    for (int c = 0; c < 32; c++)
+    for (int c = 0; c < 32; c++) {
         esum[c] = ev[row] + ex[col0 + c] - 16;
+        fast = fast && esum[c] >= -102 && esum[c] <= 103;
+        p2[c] = pow2f(min(max(esum[c], -102), 103));
+    }
 #pragma unroll 1
     for (int g = 0; g < kContractQ; g++) {
         float R[32];
         tmem_ld32(tmem_row + g * kContractTileN, R);
+        const float sg = pow2f(-8 * g);
 #pragma unroll
         for (int c = 0; c < 32; c++) {
-            const float v = ldexpf(R[c], esum[c] - 8 * g); // exact (power-of-two scaling)
+            const float v = fast ? (R[c] * sg) * p2[c] : ldexpf(R[c], esum[c] - 8 * g); // exact
             // double-word accumulation: (ah, al) += v
             const float s = ah[c] + v;
             const float bb = s - ah[c];

@@ -79,12 +79,35 @@ struct ContractParams {
     unsigned *error;          // set to 1 when a wait gave up (bounded waits)
 };
 
+// 2^k as a float for -126 <= k <= 127 (a normal power of two)
+__host__ __device__ __forceinline__ float pow2f(int k)
+{
+    union {
+        unsigned u;
+        float f;
+    } c;
+    c.u = (unsigned)(k + 127) << 23;
+    return c.f;
+}
+
+// The digit scale 2^(8 - e) of a column as two normal powers of two
+// (s1 s2 = 2^(8-e); s2 = 1 unless 8 - e > 127, i.e. a column maximum below
+// 2^-119): multiplying by them is x 2^(8-e) rounded once, as ldexpf.
+struct DigitScale {
+    float s1, s2;
+};
+__host__ __device__ __forceinline__ DigitScale digit_scale(int e)
+{
+    const int k = 8 - e, k1 = k < 127 ? k : 127;
+    return {pow2f(k1), pow2f(k - k1)};
+}
+
 // Q digits of the double-word hi + lo (|hi + lo| < 2^e), rounding to
 // nearest at each level: hi + lo = 2^e sum_s d_s 2^(-8(s+1)) + r.
-__host__ __device__ __forceinline__ void split_digits(float hi, float lo, int e, float (&d)[kContractQ])
+__host__ __device__ __forceinline__ void split_digits(float hi, float lo, DigitScale sc, float (&d)[kContractQ])
 {
     // a + b = (hi + lo) 2^(8-e), |a + b| < 256; every step below is exact
-    float a = ldexpf(hi, 8 - e), b = ldexpf(lo, 8 - e);
+    float a = hi * sc.s1 * sc.s2, b = lo * sc.s1 * sc.s2;
 #pragma unroll
     for (int s = 0; s < kContractQ; s++) {
         const float q = rintf(a);
