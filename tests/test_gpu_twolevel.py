@@ -18,9 +18,14 @@ def dev(a):
 
 
 def grads(name, B, **kw):
+    return grads_kw(name, B, **kw)
+
+
+def grads_kw(name, B, tableau=None, **kw):
     w = W.make(name, batch=B)
     c = w["cfg"]
-    s = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], atol=c["tol"], rtol=c["tol"], **kw)
+    s = Solver(c["model"], c["n"], c["npar"], B, tableau=tableau or c["tableau"], atol=c["tol"], rtol=c["tol"],
+               **kw)
     out = s.gradient(c["cost"], dev(w["y0"]), dev(w["params"]), dev(w["t0"]), dev(w["t1"]))
     torch.cuda.synchronize()
     res = {k: v.cpu().numpy() for k, v in out.items()}
@@ -163,8 +168,54 @@ def test_ladder_first_rung_lane_groups(cuda):
     s.close()
 
 
+@pytest.mark.parametrize("precision,stride,tableau", [("fp64", 4, None), ("mixed", 5, None), ("mixed_dw", 8, None),
+                                                       ("fp64", 3, "rkf78"), ("fp64", 6, "rk4"),
+                                                       ("mixed_dw", 4, "euler"), ("fp64", 64, None)])
+def test_lane_group_stride_matches_every_step(cuda, precision, stride, tableau):
+    """GLV N=10 lane groups: every stride-th step stored, segments re-run by
+    the group (backward_group_kernel_2level) -- the gradients equal the
+    every-step sweeps' bit for bit (mixed_dw: the sweeps over [t, dt, y]
+    records, stage_records = 0, whose forward code the segments re-run).  A
+    stride above every instance's step count (64) leaves one segment."""
+    B = 96
+    kw = {"tableau": tableau} if tableau else {}
+    if tableau in ("rk4", "euler"):
+        kw["dt0"] = 1e-2
+    sr = {"stage_records": 0} if precision == "mixed_dw" else {}
+    ref, _ = grads_kw("glv10", B, precision=precision, **sr, **kw)
+    r, info = grads_kw("glv10", B, precision=precision, ckpt_stride=stride, **sr, **kw)
+    assert info["stride"] == stride
+    assert (ref["status"] == 0).all() and (r["status"] == 0).all(), np.unique(r["status"])
+    np.testing.assert_array_equal(r["n_acc"], ref["n_acc"])
+    np.testing.assert_array_equal(r["yT"], ref["yT"])
+    np.testing.assert_array_equal(r["dy0"], ref["dy0"])
+    np.testing.assert_array_equal(r["dp"], ref["dp"])
+
+
+def test_lane_group_automatic_stride_under_budget(cuda):
+    """GLV-10, mixed_dw, ckpt_stride = -1 with a pool ~1/8 of what [t, dt, y]
+    records of every step need: the ladder drops the stage records, then
+    thins the checkpoints until they fit; the gradients are the recompute
+    path's, bit for bit."""
+    B = 96
+    ref, _ = grads("glv10", B, precision="mixed_dw", stage_records=0)
+    w = W.make("glv10", batch=B)
+    c = w["cfg"]
+    plain = int((ref["n_acc"].sum() + B) * 12 * 8)
+    s = Solver(c["model"], c["n"], c["npar"], B, tableau=c["tableau"], precision="mixed_dw", atol=c["tol"],
+               rtol=c["tol"], ckpt_stride=-1, ckpt_budget_bytes=plain // 8, chunk_len=4)
+    P = dev(w["params"])
+    s.forward(dev(w["y0"]), P, dev(w["t0"]), dev(w["t1"]))
+    bw = s.backward(P, torch.ones(B, 1, c["n"], dtype=torch.float64, device="cuda"))
+    torch.cuda.synchronize()
+    info = s.checkpoint_info()
+    assert info["stride"] > 1 and info["capacity_bytes"] <= plain // 8
+    assert (bw["status"].cpu().numpy() == 0).all()
+    np.testing.assert_array_equal(bw["dy0"].cpu().numpy()[:, 0], ref["dy0"])
+    np.testing.assert_array_equal(bw["dp"].cpu().numpy()[:, 0], ref["dp"])
+    s.close()
+
+
 def test_strides_rejected_without_two_level(cuda):
-    with pytest.raises(Exception):
-        Solver("glv", 10, 110, 8, ckpt_stride=4)
     with pytest.raises(Exception):
         Solver("glv_shared", 64, 64, 8, ckpt_stride=4)

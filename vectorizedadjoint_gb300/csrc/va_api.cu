@@ -18,6 +18,7 @@
 #include "../../include/va.h"
 #include "va_bundle.cuh"
 #include "va_contract.cuh"
+#include "va_group_2level.cuh"
 #include "va_kernels.cuh"
 #include "va_order.h"
 #include "va_registry.h"
@@ -392,14 +393,37 @@ int bundle_grid(va_handle *h)
     return (h->prob.batch + nb - 1) / nb;
 }
 
-// Two-level backward launch: 64-thread blocks, at most 4 per SM, so the
-// re-integration scratch stays (stride + 1) records x 256 threads per SM.
+// Two-level backward launch.  One-thread models: 64-thread blocks, at most 4
+// per SM, so the re-integration scratch stays (stride + 1) records x 256
+// threads per SM.  Lane groups: 256-thread blocks (8 warps of 32 / G groups),
+// at most 2 per SM, (stride + 1) records of the group's state per group.
 constexpr int kTwoLevelBlock = 64, kTwoLevelBlocksPerSm = 4;
+constexpr int kTwoLevelGroupBlock = 256, kTwoLevelGroupBlocksPerSm = 2;
+
+int two_level_block(const va_handle *h) { return h->ks->tpi > 1 ? kTwoLevelGroupBlock : kTwoLevelBlock; }
+
+// instances one block of the two-level backward carries at once
+int two_level_per_block(const va_handle *h)
+{
+    const int g = h->ks->tpi;
+    return g > 1 ? kTwoLevelGroupBlock / 32 * (32 / g) : kTwoLevelBlock;
+}
 
 int two_level_grid(va_handle *h)
 {
-    const long need = ((long)h->prob.batch + kTwoLevelBlock - 1) / kTwoLevelBlock;
-    return (int)std::max(1L, std::min(need, (long)h->sm_count * kTwoLevelBlocksPerSm));
+    const long per = two_level_per_block(h);
+    const long need = ((long)h->prob.batch + per - 1) / per;
+    const long bps = h->ks->tpi > 1 ? kTwoLevelGroupBlocksPerSm : kTwoLevelBlocksPerSm;
+    return (int)std::max(1L, std::min(need, (long)h->sm_count * bps));
+}
+
+// doubles of re-integration scratch the two-level backward needs
+size_t two_level_scratch_doubles(va_handle *h)
+{
+    const size_t carriers = (size_t)two_level_grid(h) * two_level_per_block(h);
+    if (h->ks->tpi > 1)
+        return carriers * (size_t)va::group_scratch_doubles(h->N, h->stride);
+    return carriers * (h->stride + 1) * scratch_record_doubles(h);
 }
 
 // Scratch for the current stride; never called during stream capture.
@@ -407,8 +431,7 @@ va_status ensure_scratch(va_handle *h)
 {
     if (h->stride <= 1)
         return VA_OK;
-    const size_t need =
-        (size_t)two_level_grid(h) * kTwoLevelBlock * (h->stride + 1) * scratch_record_doubles(h);
+    const size_t need = two_level_scratch_doubles(h);
     if (need <= h->scratch_doubles)
         return VA_OK;
     if (h->scratch)
@@ -604,8 +627,7 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
     if (h->hist)
         h->hist_done = true;
     if (h->stride > 1) {
-        if (h->scratch_doubles <
-            (size_t)two_level_grid(h) * kTwoLevelBlock * (h->stride + 1) * scratch_record_doubles(h))
+        if (h->scratch_doubles < two_level_scratch_doubles(h))
             return fail(h, VA_BAD_ARGS, "two-level scratch not sized for the stride%s");
         a.stride = h->stride;
         a.inst_t1 = h->inst_t1;
@@ -617,7 +639,8 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
         a.max_fail = h->opt.max_rejects;
         a.step_pow = h->opt.step_pow;
         VA_CUDA(h, cudaMemsetAsync(&h->ctl->adj_next, 0, sizeof(unsigned int), s));
-        VA_CUDA(h, launch(h, h->ks->bwd2[h->opt.tableau][h->opt.precision], two_level_grid(h), kTwoLevelBlock, &a, s));
+        VA_CUDA(h, launch(h, h->ks->bwd2[h->opt.tableau][h->opt.precision], two_level_grid(h), two_level_block(h),
+                          &a, s));
         return VA_OK;
     }
     const void *fn = h->ks->bwd[h->opt.tableau][h->opt.precision];
@@ -964,11 +987,10 @@ va_status create_handle(const va_problem *prob, const va_options *opt, const va:
     if (prob->n != N || prob->npar != P)
         return VA_BAD_ARGS;
     // checkpoint stride: -1 automatic, 0/1 every step, k > 1 every k-th step
-    // (two-level checkpointing: one-thread-per-instance models only)
-    // strides > 1 need a two-level backward (one-thread models); -1 also
-    // serves the others, whose ladder stops after dropping the stage records
-    if (o.ckpt_stride < -1 ||
-        (o.ckpt_stride > 1 && !(ks && ks->tpi == 1 && ks->bwd2[o.tableau][o.precision])))
+    // (two-level checkpointing: one-thread and lane-group models); -1 also
+    // serves the shared-matrix bundles, whose ladder stops after dropping
+    // the stage records
+    if (o.ckpt_stride < -1 || (o.ckpt_stride > 1 && !(ks && ks->bwd2[o.tableau][o.precision])))
         return VA_BAD_ARGS;
     va_handle *h = new va_handle();
     h->stride = o.ckpt_stride > 1 ? o.ckpt_stride : 1;
@@ -1101,7 +1123,7 @@ va_status va_forward(va_handle *h, const double *y0, const double *params, const
         // (where a two-level backward exists)
         if (stages_now(h))
             h->stages_on = false;
-        else if (h->ks && h->ks->tpi == 1 && h->ks->bwd2[h->opt.tableau][h->opt.precision])
+        else if (h->ks && h->ks->bwd2[h->opt.tableau][h->opt.precision])
             h->stride *= 4;
         else
             break;

@@ -123,6 +123,37 @@ struct ModelGLVLane {
     }
 };
 
+// accept_state for a lane group (lane i's component): the state after an
+// accepted attempt restarts, for double-word stages, from the FP64 value a
+// checkpoint stores (so a two-level re-integration from that checkpoint runs
+// the same bits), and f(y_new) is reused only when every lane's component
+// round-trips; the decision is the group's, since f exchanges components.
+template <class M, class Tab, class S>
+__device__ __forceinline__ void accept_state_group(double (&y)[1], S (&ys)[1], S (&k0)[1], const double (&ynew)[1],
+                                                   const S (&ynew_s)[1], const S (&knew)[1], const S (&p)[M::P],
+                                                   double t, unsigned mask)
+{
+    bool same = true;
+    if constexpr (std::is_same<S, dword>::value) {
+        y[0] = to_d(ynew_s[0]);
+        if ((y[0] - (double)ynew_s[0].hi) == (double)ynew_s[0].lo &&
+            ynew_s[0].hi + ynew_s[0].lo == ynew_s[0].hi) {
+            ys[0] = ynew_s[0];
+        } else {
+            ys[0] = from_d<S>(y[0]);
+            same = false;
+        }
+        same = __all_sync(mask, same);
+    } else {
+        y[0] = ynew[0];
+        ys[0] = ynew_s[0];
+    }
+    if (Tab::FSAL && same)
+        k0[0] = knew[0];
+    else
+        M::template rhs<S>(ys, p, from_d<S>(t), k0);
+}
+
 // ------------------------------------------------------------ forward sweep
 
 template <class M, class Tab, class S>
@@ -223,6 +254,10 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
             a.inst_T[b] = count;
             a.inst_last[b] = chunk;
             a.inst_status[b] = status;
+            if (a.inst_t1)
+                a.inst_t1[b] = t1;
+            if (Tab::FIXED && a.inst_t0)
+                a.inst_t0[b] = t_start;
             note_work(a, b, count + rej);
             if (a.n_acc_out)
                 a.n_acc_out[b] = count;
@@ -250,11 +285,14 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
                 status = ST_MAX_STEPS;
                 continue;
             }
-            if (!reserve()) {
-                status = ST_CKPT_BUDGET;
-                continue;
+            // every stride-th accepted step is checkpointed (stride <= 1: all)
+            if (a.stride <= 1 || count % a.stride == 0) {
+                if (!reserve()) {
+                    status = ST_CKPT_BUDGET;
+                    continue;
+                }
+                write();
             }
-            write();
             if (!Tab::FIXED && (t + dt) - t1 > kDblEps)
                 dt = t1 - t;
             fails = 0;
@@ -280,15 +318,7 @@ __global__ void __launch_bounds__(256) forward_group_kernel(FwdParams a)
                 t += dt;
                 dt = increase_step<Tab, S>(dt, err, a.step_pow, li == 0 ? &a.ctl->pow_undecided : nullptr);
             }
-            ys[0] = ynew_s[0];
-            if constexpr (std::is_same<S, dword>::value)
-                y[0] = to_d(ynew_s[0]);
-            else
-                y[0] = ynew[0];
-            if constexpr (Tab::FSAL)
-                k0[0] = knew[0];
-            else
-                M::template rhs<S>(ys, p, from_d<S>(t), k0);
+            accept_state_group<M, Tab, S>(y, ys, k0, ynew, ynew_s, knew, p, t, mask);
             ok = true;
         }
         if (fails >= a.max_fail) {

@@ -13,10 +13,12 @@ void fill_fp64_glv5(KernelSet &k);
 void fill_fp64_glv10(KernelSet &k);
 void fill_rkf78_glv5(KernelSet &k);
 void fill_rkf78_glv10(KernelSet &k);
+void fill_2level_glv5(KernelSet &k);
+void fill_2level_glv10(KernelSet &k);
 
 template <int NN>
 static KernelSet make_glv(void (*fill_fp64)(KernelSet &), void (*fill_rkf78)(KernelSet &),
-                          void (*fill_fixed)(KernelSet &))
+                          void (*fill_fixed)(KernelSet &), void (*fill_2level)(KernelSet &))
 {
     using M = ModelGLVLane<NN>;
     KernelSet k{};
@@ -41,13 +43,15 @@ static KernelSet make_glv(void (*fill_fp64)(KernelSet &), void (*fill_rkf78)(Ker
     k.dw_records = false; // the [t, dt, y] records of the fallback sweeps are FP64
     fill_rkf78(k);
     fill_fixed(k);
+    fill_2level(k);
     return k;
 }
 
 const KernelSet *kernels_glv(int n)
 {
-    static const KernelSet k5 = make_glv<5>(fill_fp64_glv5, fill_rkf78_glv5, fill_fixed_glv5);
-    static const KernelSet k10 = make_glv<10>(fill_fp64_glv10, fill_rkf78_glv10, fill_fixed_glv10);
+    static const KernelSet k5 = make_glv<5>(fill_fp64_glv5, fill_rkf78_glv5, fill_fixed_glv5, fill_2level_glv5);
+    static const KernelSet k10 =
+        make_glv<10>(fill_fp64_glv10, fill_rkf78_glv10, fill_fixed_glv10, fill_2level_glv10);
     switch (n) {
     case 5:
         return &k5;
