@@ -125,13 +125,14 @@ typedef struct {
                             two-level checkpointing -- every k-th accepted step is
                             stored and the backward sweep re-integrates each segment
                             from its checkpoint into scratch (bit-identical steps,
-                            checked; one extra forward evaluation per step).  -1:
-                            automatic -- va_forward checks the pool after the sweep
-                            (synchronously) and, if it overflowed, reruns: first
-                            without stage records, then with a 4x larger stride
-                            until the checkpoints fit (up to 1024).  Strides > 1:
-                            one-thread-per-instance models; the lane-group and
-                            shared-matrix models take -1 for its first rung only */
+                            checked; one extra forward evaluation per step), for
+                            every model family: one-thread, lane-group (GLV N=5,10)
+                            and shared-matrix bundles.  -1: automatic -- va_forward
+                            (and the first va_gradient call on the handle) checks
+                            the pool after the sweep (synchronously) and, if it
+                            overflowed, reruns: first without stage records, then
+                            with a 4x larger stride until the checkpoints fit (up
+                            to 1024); later va_gradient calls keep that layout  */
     int32_t block_size;  /* 0 = autotuned / default                               */
     int32_t blocks_per_sm; /* 0 = occupancy limit                                 */
     int32_t chunk_len;   /* records per checkpoint chunk (0 = 64)                 */

@@ -216,6 +216,72 @@ def test_lane_group_automatic_stride_under_budget(cuda):
     s.close()
 
 
-def test_strides_rejected_without_two_level(cuda):
+def shared_problem(N, B, seed=11):
+    """The GLV-256 recipe at size N (diag -1, off-diagonal N(0, (0.5/sqrt N)^2))."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    A = rng.normal(0.0, 0.5 / np.sqrt(N), (N, N))
+    A[np.arange(N), np.arange(N)] = -1.0
+    return A, rng.uniform(0.5, 1.5, (B, N)), rng.uniform(0.1, 1.0, (B, N))
+
+
+def shared_grads(N, B, precision, tableau="dopri5", dt0=1e-3, **kw):
+    A, r, x0 = shared_problem(N, B)
+    s = Solver("glv_shared", N, N, B, tableau=tableau, precision=precision, atol=1e-7, rtol=1e-7, dt0=dt0, **kw)
+    dA = torch.empty(N, N, dtype=torch.float64, device="cuda")
+    s.set_shared(dev(A), dA)
+    out = s.gradient("sum", dev(x0), dev(r), dev(np.zeros(B)), dev(np.full(B, 10.0)))
+    torch.cuda.synchronize()
+    res = {k: v.cpu().numpy() for k, v in out.items()}
+    res["dA"] = dA.cpu().numpy()
+    info = s.checkpoint_info()
+    s.close()
+    return res, info
+
+
+@pytest.mark.parametrize("N,B,precision,stride,tableau", [(64, 10, "fp64", 4, "dopri5"), (64, 9, "mixed", 3, "ck54"),
+                                                          (64, 10, "mixed_dw", 5, "dopri5"),
+                                                          (256, 5, "mixed_dw", 8, "dopri5"),
+                                                          (256, 4, "fp64", 16, "dopri5"),
+                                                          (64, 6, "mixed_dw", 7, "rk4")])
+def test_shared_matrix_stride_matches_every_step(cuda, N, B, precision, stride, tableau):
+    """Shared-matrix GLV bundles (backward_bundle_kernel_2level): each
+    instance's gradients equal the every-step sweeps' bit for bit (mixed_dw:
+    the sweeps over [t, dt, y] records with the stage recompute, which the
+    segments' back steps run); the shared dA, whose terms the two sweeps add
+    in another order, agrees to 1e-12 of its largest entry (FP64), 1e-9
+    (double-word) or 1e-5 (float stages: each step's terms are summed in
+    float before they reach the FP64 partial, over the instances stepping
+    together)."""
+    dt0 = 1e-2 if tableau == "rk4" else 1e-3
+    sr = {"stage_records": 0} if precision == "mixed_dw" else {}
+    ref, _ = shared_grads(N, B, precision, tableau, dt0, **sr)
+    r, info = shared_grads(N, B, precision, tableau, dt0, ckpt_stride=stride, **sr)
+    assert info["stride"] == stride
+    assert (ref["status"] == 0).all() and (r["status"] == 0).all(), np.unique(r["status"])
+    np.testing.assert_array_equal(r["n_acc"], ref["n_acc"])
+    np.testing.assert_array_equal(r["yT"], ref["yT"])
+    np.testing.assert_array_equal(r["dy0"], ref["dy0"])
+    np.testing.assert_array_equal(r["dp"], ref["dp"])
+    tol = {"fp64": 1e-12, "mixed_dw": 1e-9, "mixed": 1e-5}[precision]
+    assert np.abs(r["dA"] - ref["dA"]).max() <= tol * np.abs(ref["dA"]).max()
+
+
+def test_shared_matrix_automatic_stride_under_budget(cuda):
+    """GLV-256 bundles, mixed_dw, ckpt_stride = -1 with a budget far below
+    every-step stage records: the ladder drops the stage records, then
+    thins the checkpoints; per-instance gradients equal the recompute
+    path's bit for bit."""
+    N, B = 256, 6
+    ref, _ = shared_grads(N, B, "mixed_dw", stage_records=0)
+    plain = int((ref["n_acc"].sum() + B) * (N + 2) * 8)
+    r, info = shared_grads(N, B, "mixed_dw", ckpt_stride=-1, ckpt_budget_bytes=plain // 6, chunk_len=4)
+    assert info["stride"] > 1 and info["capacity_bytes"] <= plain // 6
+    assert (r["status"] == 0).all()
+    np.testing.assert_array_equal(r["dy0"], ref["dy0"])
+    np.testing.assert_array_equal(r["dp"], ref["dp"])
+    assert np.abs(r["dA"] - ref["dA"]).max() <= 1e-9 * np.abs(ref["dA"]).max()
+
+
+def test_invalid_stride_rejected(cuda):
     with pytest.raises(Exception):
-        Solver("glv_shared", 64, 64, 8, ckpt_stride=4)
+        Solver("glv_shared", 64, 64, 8, ckpt_stride=-2)

@@ -18,6 +18,7 @@
 #include "../../include/va.h"
 #include "va_bundle.cuh"
 #include "va_contract.cuh"
+#include "va_bundle_2level.cuh"
 #include "va_group_2level.cuh"
 #include "va_kernels.cuh"
 #include "va_order.h"
@@ -76,6 +77,7 @@ struct va_handle {
 
     int fwd_block = 128, fwd_grid = 0, bwd_block = 128, bwd_grid = 0;
     bool forward_done = false;
+    bool ladder_settled = false; // ckpt_stride = -1: va_gradient ran the memory ladder once
     std::string err;
 
     cudaGraphExec_t graph = nullptr;
@@ -190,7 +192,8 @@ int grid_for(va_handle *h, const void *fn, int block, int instances)
 bool stages_now(const va_handle *h)
 {
     if (h->bks)
-        return h->stages_on && h->opt.precision == VA_PREC_MIXED_DW && h->bks->rs_stage[h->opt.tableau] > 0;
+        return h->stages_on && h->stride <= 1 && h->opt.precision == VA_PREC_MIXED_DW &&
+               h->bks->rs_stage[h->opt.tableau] > 0;
     return va::stage_records_on(h->ks, h->opt.tableau, h->opt.precision, h->stride, h->stages_on);
 }
 
@@ -351,6 +354,9 @@ va_status alloc_buffers(va_handle *h)
                     if (fns[f])
                         VA_CUDA(h, cudaFuncSetAttribute(fns[f], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                         (int)sm[f]));
+                if (h->bks->bwd2[t][p])
+                    VA_CUDA(h, cudaFuncSetAttribute(h->bks->bwd2[t][p], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)h->bks->smem_bwd2[p]));
             }
     }
     return VA_OK;
@@ -420,6 +426,8 @@ int two_level_grid(va_handle *h)
 // doubles of re-integration scratch the two-level backward needs
 size_t two_level_scratch_doubles(va_handle *h)
 {
+    if (h->bks) // (stride + 1) [t, -, y] records per instance
+        return (size_t)h->prob.batch * va::bundle_scratch_doubles(h->N, h->stride);
     const size_t carriers = (size_t)two_level_grid(h) * two_level_per_block(h);
     if (h->ks->tpi > 1)
         return carriers * (size_t)va::group_scratch_doubles(h->N, h->stride);
@@ -586,6 +594,38 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
         va::OrderArgs o{a.B, h->inst_T, nullptr, nullptr, nullptr, nullptr, h->order_work, h->order_bwd, reuse};
         VA_CUDA(h, va::enqueue_order(o, s));
         a.order = h->order_bwd;
+    }
+    if (h->bks && h->stride > 1) {
+        // two-level: segments re-run from the strided checkpoints, in bundles
+        // of the precision's default width
+        if (h->scratch_doubles < two_level_scratch_doubles(h))
+            return fail(h, VA_BAD_ARGS, "two-level scratch not sized for the stride%s");
+        const int p = h->opt.precision;
+        va::BundleParams bp = bundle_params(h);
+        bp.nb = h->bks->nb[p];
+        a.stride = h->stride;
+        a.inst_t1 = h->inst_t1;
+        a.inst_t0 = h->inst_t0;
+        a.scratch = h->scratch;
+        a.atol = h->opt.atol;
+        a.rtol = h->opt.rtol;
+        a.dt0 = h->opt.dt0;
+        a.max_fail = h->opt.max_rejects;
+        a.step_pow = h->opt.step_pow;
+        bp.g = a;
+        void *args[] = {&bp};
+        int grid = (h->prob.batch + bp.nb - 1) / bp.nb;
+        VA_CUDA(h, cudaLaunchKernel(h->bks->bwd2[h->opt.tableau][p], dim3(grid), dim3(h->N), args,
+                                    h->bks->smem_bwd2[p], s));
+        if (h->shared_dA) {
+            const int NN = h->N * h->N;
+            int dw = p == VA_PREC_MIXED_DW;
+            void *rargs[] = {(void *)&h->dA_part, (void *)&grid, (void *)&dw, (void *)&h->shared_dA};
+            VA_CUDA(h, cudaLaunchKernel(h->bks->reduce, dim3((NN + 255) / 256), dim3(256), rargs, 0, s));
+        }
+        h->bwd_grid = grid;
+        h->bwd_block = h->N;
+        return VA_OK;
     }
     if (h->bks) {
         va::BundleParams bp = bundle_params(h);
@@ -987,10 +1027,10 @@ va_status create_handle(const va_problem *prob, const va_options *opt, const va:
     if (prob->n != N || prob->npar != P)
         return VA_BAD_ARGS;
     // checkpoint stride: -1 automatic, 0/1 every step, k > 1 every k-th step
-    // (two-level checkpointing: one-thread and lane-group models); -1 also
-    // serves the shared-matrix bundles, whose ladder stops after dropping
-    // the stage records
-    if (o.ckpt_stride < -1 || (o.ckpt_stride > 1 && !(ks && ks->bwd2[o.tableau][o.precision])))
+    // (two-level checkpointing: every model family whose two-level backward
+    // is compiled for the tableau and precision)
+    if (o.ckpt_stride < -1 ||
+        (o.ckpt_stride > 1 && !(ks && ks->bwd2[o.tableau][o.precision]) && !(bks && bks->bwd2[o.tableau][o.precision])))
         return VA_BAD_ARGS;
     va_handle *h = new va_handle();
     h->stride = o.ckpt_stride > 1 ? o.ckpt_stride : 1;
@@ -1123,7 +1163,8 @@ va_status va_forward(va_handle *h, const double *y0, const double *params, const
         // (where a two-level backward exists)
         if (stages_now(h))
             h->stages_on = false;
-        else if (h->ks && h->ks->bwd2[h->opt.tableau][h->opt.precision])
+        else if ((h->ks && h->ks->bwd2[h->opt.tableau][h->opt.precision]) ||
+                 (h->bks && h->bks->bwd2[h->opt.tableau][h->opt.precision]))
             h->stride *= 4;
         else
             break;
@@ -1172,6 +1213,16 @@ va_status va_gradient(va_handle *h, int32_t cost, const double *y0, const double
     if (st != VA_OK)
         return st;
     cudaStream_t s = (cudaStream_t)stream;
+    if (h->opt.ckpt_stride == -1 && !h->ladder_settled) {
+        // automatic checkpointing: the first call runs the forward with its
+        // memory ladder (synchronous checks of the pool between reruns), then
+        // the backward; later calls capture the layout it settled on
+        st = va_forward(h, y0, params, t0, t1, yT, n_acc, nullptr, status, stream);
+        if (st != VA_OK)
+            return st;
+        h->ladder_settled = true;
+        return enqueue_backward(h, params, nullptr, nullptr, cost, dy0, dparams, status, s);
+    }
     GraphKey key;
     key.cost = cost;
     const void *ptrs[10] = {y0, params, t0, t1, yT, dy0, dparams, n_acc, status, h->shared_A};

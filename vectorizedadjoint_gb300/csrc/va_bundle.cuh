@@ -66,6 +66,16 @@ __host__ __device__ constexpr int factor_stages()
     return Tab::S - (Tab::b(Tab::S - 1) == 0.0 ? 1 : 0);
 }
 
+// the value as a double-word (used where S is dword; other S never reach it)
+template <class S>
+__device__ __forceinline__ dword dword_of(S v)
+{
+    if constexpr (std::is_same<S, dword>::value)
+        return v;
+    else
+        return dword(0.0f, 0.0f);
+}
+
 template <class S>
 __device__ __forceinline__ S load_A(const double *A, const dword *Aw, size_t k)
 {
@@ -154,6 +164,92 @@ __device__ __forceinline__ void bundle_matvec(const double *Mt, const dword *Mtw
     for (int b = 0; b < NB; b++)
         z[b] = S(0);
     bundle_matvec_acc<NT, NB, S, UNR>(Mt, Mtw, xs, z);
+}
+
+// ------------------------------------------------- per-instance arithmetic
+// (shared by the forward, the backward's stage recompute and the two-level
+// re-integration, so that all three form the same bits)
+
+// stage point X_m = y + h sum_{j<m} a_mj K_j of instance b (thread i's
+// component): FP64 in the oracle's order, else a stage-precision sum
+template <class Tab, class S, int NB>
+__device__ __forceinline__ S bundle_stage_point(int m, int b, double y, S ys, const S (&K)[Tab::S][NB], double h,
+                                                S sh)
+{
+    constexpr int NS = Tab::S;
+    if constexpr (std::is_same<S, double>::value) {
+        double acc = y;
+#pragma unroll
+        for (int j = 0; j < NS - 1; j++)
+            if (j < m)
+                acc = acc + (Tab::a(m, j) * h) * K[j][b];
+        return acc;
+    } else {
+        S acc = S(0);
+#pragma unroll
+        for (int j = 0; j < NS - 1; j++)
+            if (j < m)
+                acc = madd(S(Tab::a(m, j)), K[j][b], acc);
+        return madd(acc, sh, ys);
+    }
+}
+
+// y_new = y + dt sum_j b_j K_j of instance b: ynew_s in stage precision and
+// ynew in FP64
+template <class Tab, class S, int NB>
+__device__ __forceinline__ void bundle_solution(int b, double y, S ys, const S (&K)[Tab::S][NB], double dt, S sdt,
+                                                S &ynew_s, double &ynew)
+{
+    constexpr int NS = Tab::S;
+    if constexpr (std::is_same<S, double>::value) {
+        double acc = y;
+#pragma unroll
+        for (int j = 0; j < NS; j++)
+            if (Tab::b(j) != 0.0)
+                acc = acc + (Tab::b(j) * dt) * K[j][b];
+        ynew = acc;
+        ynew_s = acc;
+    } else {
+        S acc = S(0);
+#pragma unroll
+        for (int j = 0; j < NS; j++)
+            if (Tab::b(j) != 0.0)
+                acc = madd(S(Tab::b(j)), K[j][b], acc);
+        ynew_s = madd(acc, sdt, ys);
+        ynew = to_d(ynew_s);
+    }
+}
+
+// thread i's ratio |e_i| / (atol + rtol (|y_i| + |dt| |k0_i|)) of instance b
+template <class Tab, class S, int NB>
+__device__ __forceinline__ double bundle_error_ratio(int b, double y, const S (&K)[Tab::S][NB], S knew, double dt,
+                                                     double atol, double rtol)
+{
+    constexpr int NS = Tab::S;
+    if constexpr (std::is_same<S, double>::value) {
+        double acc = 0.0;
+        bool first = true;
+#pragma unroll
+        for (int j = 0; j < NS; j++)
+            if (Tab::e(j) != 0.0) {
+                const double term = (Tab::e(j) * dt) * K[j][b];
+                acc = first ? term : acc + term;
+                first = false;
+            }
+        if constexpr (Tab::FSAL)
+            acc = acc + (Tab::E_NEW * dt) * knew;
+        return fabs(acc) / (atol + rtol * (1.0 * fabs(y) + fabs(dt) * fabs(K[0][b])));
+    } else {
+        S acc = S(0);
+#pragma unroll
+        for (int j = 0; j < NS; j++)
+            if (Tab::e(j) != 0.0)
+                acc = madd(S(Tab::e(j)), K[j][b], acc);
+        if constexpr (Tab::FSAL)
+            acc = madd(S(Tab::E_NEW), knew, acc);
+        const double e = dt * to_d(acc);
+        return fabs(e) / (atol + rtol * (1.0 * fabs(y) + fabs(dt) * fabs(to_d(K[0][b]))));
+    }
 }
 
 // ------------------------------------------------------------ forward sweep
@@ -245,6 +341,15 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
     }
     __syncthreads();
 
+    // whether instance b's loop has ended (fixed steps: while ((t + dt) - t1
+    // <= eps), runge_kutta.hpp:54)
+    auto ended = [&](int b) -> bool {
+        return Tab::FIXED ? !((t[b] + dt[b]) - t1[b] <= kDblEps) : !(t1[b] - t[b] > kDblEps);
+    };
+    // whether the top of instance b's step stores a record: every step, or
+    // every stride-th (two-level checkpointing) and the last
+    auto stores = [&](int b) -> bool { return a.stride <= 1 || count[b] % a.stride == 0 || ended(b); };
+
     for (;;) {
         // top of step for every live instance: loop test, record, end clamp.
         // Chunk allocation needs one thread and a barrier, so it is done for
@@ -254,8 +359,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
         for (int b = 0; b < NB; b++) {
             if (!active[b] || status[b] != ST_OK || !at_top[b])
                 continue;
-            // fixed steps: while ((t + dt) - t1 <= eps) (runge_kutta.hpp:54)
-            if (Tab::FIXED ? !((t[b] + dt[b]) - t1[b] <= kDblEps) : !(t1[b] - t[b] > kDblEps)) {
+            if (ended(b)) {
                 // finished: write the final record, like the single-thread sweep
                 if (slot[b] == CH)
                     need_chunk = true;
@@ -265,7 +369,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
                 status[b] = ST_MAX_STEPS;
                 continue;
             }
-            if (slot[b] == CH)
+            if (slot[b] == CH && stores(b))
                 need_chunk = true;
         }
         if (need_chunk) {
@@ -273,7 +377,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
 #pragma unroll
                 for (int b = 0; b < NB; b++) {
                     int c = chunk[b];
-                    if (active[b] && status[b] == ST_OK && at_top[b] && slot[b] == CH) {
+                    if (active[b] && status[b] == ST_OK && at_top[b] && slot[b] == CH && stores(b)) {
                         c = (int)atomicAdd(&a.ctl->pool_next, 1u);
                         if (c >= a.pool.n_chunks) {
                             c = -1;
@@ -288,7 +392,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
             __syncthreads();
 #pragma unroll
             for (int b = 0; b < NB; b++) {
-                if (active[b] && status[b] == ST_OK && at_top[b] && slot[b] == CH) {
+                if (active[b] && status[b] == ST_OK && at_top[b] && slot[b] == CH && stores(b)) {
                     chunk[b] = ichunk[b];
                     slot[b] = 0;
                     if (chunk[b] < 0)
@@ -302,7 +406,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
         for (int b = 0; b < NB; b++) {
             if (!active[b] || !at_top[b])
                 continue;
-            if (status[b] == ST_OK) {
+            if (status[b] == ST_OK && stores(b)) {
                 double *rec = record_ptr<RS>(a.pool, chunk[b], slot[b]);
                 if (i == 0)
                     *reinterpret_cast<double2 *>(rec) = make_double2(t[b], dt[b]);
@@ -310,13 +414,16 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
                     rec[2 + i] = dw_pack(ys[b]);
                     rec[2 + NS * NT + i] = dw_pack(z0[b]);
                     rec_cur[b] = rec;
+                } else if (std::is_same<S, dword>::value && a.stride > 1) {
+                    // two-level checkpoints of the double-word sweep: the
+                    // exact double-word state, which a re-integration resumes
+                    rec[2 + i] = dw_pack(dword_of(ys[b]));
                 } else {
                     rec[2 + i] = y[b];
                 }
                 slot[b]++;
             }
-            if (status[b] != ST_OK ||
-                (Tab::FIXED ? !((t[b] + dt[b]) - t1[b] <= kDblEps) : !(t1[b] - t[b] > kDblEps))) {
+            if (status[b] != ST_OK || ended(b)) {
                 // instance done: outputs
                 if (__syncthreads_or(isfinite(y[b]) ? 0 : 1) && status[b] == ST_OK)
                     status[b] = ST_NONFINITE;
@@ -326,6 +433,10 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
                     a.inst_T[inst[b]] = count[b];
                     a.inst_last[inst[b]] = status[b] == ST_OK ? chunk[b] : -1;
                     a.inst_status[inst[b]] = status[b];
+                    if (a.inst_t1)
+                        a.inst_t1[inst[b]] = t1[b];
+                    if (Tab::FIXED && a.inst_t0)
+                        a.inst_t0[inst[b]] = t_start[b];
                     if (a.n_acc_out)
                         a.n_acc_out[inst[b]] = count[b];
                     if (a.n_rej_out)
@@ -355,25 +466,8 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
 #pragma unroll
         for (int m = 1; m < NS; m++) {
 #pragma unroll
-            for (int b = 0; b < NB; b++) {
-                S X;
-                if constexpr (std::is_same<S, double>::value) {
-                    double acc = y[b];
-#pragma unroll
-                    for (int j = 0; j < NS - 1; j++)
-                        if (j < m)
-                            acc = acc + (Tab::a(m, j) * dt[b]) * K[j][b];
-                    X = acc;
-                } else {
-                    S acc = S(0);
-#pragma unroll
-                    for (int j = 0; j < NS - 1; j++)
-                        if (j < m)
-                            acc = madd(S(Tab::a(m, j)), K[j][b], acc);
-                    X = madd(acc, sdt[b], ys[b]);
-                }
-                xs[i * NB + b] = X;
-            }
+            for (int b = 0; b < NB; b++)
+                xs[i * NB + b] = bundle_stage_point<Tab, S, NB>(m, b, y[b], ys[b], K, dt[b], sdt[b]);
             __syncthreads();
             S z[NB];
             bundle_matvec<NT, NB, S, 16>(bp.At, bp.Atw, xs, z);
@@ -397,23 +491,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
         double ynew[NB];
 #pragma unroll
         for (int b = 0; b < NB; b++) {
-            if constexpr (std::is_same<S, double>::value) {
-                double acc = y[b];
-#pragma unroll
-                for (int j = 0; j < NS; j++)
-                    if (Tab::b(j) != 0.0)
-                        acc = acc + (Tab::b(j) * dt[b]) * K[j][b];
-                ynew[b] = acc;
-                ynew_s[b] = acc;
-            } else {
-                S acc = S(0);
-#pragma unroll
-                for (int j = 0; j < NS; j++)
-                    if (Tab::b(j) != 0.0)
-                        acc = madd(S(Tab::b(j)), K[j][b], acc);
-                ynew_s[b] = madd(acc, sdt[b], ys[b]);
-                ynew[b] = to_d(ynew_s[b]);
-            }
+            bundle_solution<Tab, S, NB>(b, y[b], ys[b], K, dt[b], sdt[b], ynew_s[b], ynew[b]);
             xs[i * NB + b] = ynew_s[b];
         }
         S znew[NB];
@@ -428,32 +506,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
         double ratio[NB];
 #pragma unroll
         for (int b = 0; b < NB; b++) {
-            double e;
-            if constexpr (std::is_same<S, double>::value) {
-                double acc = 0.0;
-                bool first = true;
-#pragma unroll
-                for (int j = 0; j < NS; j++)
-                    if (Tab::e(j) != 0.0) {
-                        const double term = (Tab::e(j) * dt[b]) * K[j][b];
-                        acc = first ? term : acc + term;
-                        first = false;
-                    }
-                if constexpr (Tab::FSAL)
-                    acc = acc + (Tab::E_NEW * dt[b]) * knew[b];
-                e = acc;
-                ratio[b] = fabs(e) / (a.atol + a.rtol * (1.0 * fabs(y[b]) + fabs(dt[b]) * fabs(K[0][b])));
-            } else {
-                S acc = S(0);
-#pragma unroll
-                for (int j = 0; j < NS; j++)
-                    if (Tab::e(j) != 0.0)
-                        acc = madd(S(Tab::e(j)), K[j][b], acc);
-                if constexpr (Tab::FSAL)
-                    acc = madd(S(Tab::E_NEW), knew[b], acc);
-                e = dt[b] * to_d(acc);
-                ratio[b] = fabs(e) / (a.atol + a.rtol * (1.0 * fabs(y[b]) + fabs(dt[b]) * fabs(to_d(K[0][b]))));
-            }
+            ratio[b] = bundle_error_ratio<Tab, S, NB>(b, y[b], K, knew[b], dt[b], a.atol, a.rtol);
             if (!active[b] || at_top[b] || Tab::FIXED)
                 ratio[b] = 0.0; // (fixed steps: no error estimate, every attempt accepted)
         }
@@ -518,6 +571,176 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
 }
 
 // ----------------------------------------------------------- backward sweep
+
+// One back_prop_step (detail/backpropagation.hpp:160-229) for the bundle's
+// instances with step[b]: from the stage record srec[b] (ST) or the state
+// y[b] (the stages recomputed), with step h[b]; lambda and mu updated, the
+// matrix gradient either written as factor rows (ST with bp.fac_v) or added
+// into the CTA's partial part.  j[b] is the step index (factor rows).
+template <int NT, int NB, class Tab, class S, bool ST>
+__device__ __forceinline__ void bundle_back_step(const BundleParams &bp, S *xall, S *vall, S *zall,
+                                                 const bool (&step)[NB], const double (&y)[NB],
+                                                 const double (&h)[NB], const S (&ys)[NB], const S (&sh)[NB],
+                                                 const double *const (&srec)[NB], const S (&r)[NB],
+                                                 const int (&inst)[NB], const int (&j)[NB], double *part,
+                                                 double (&lam)[NB], double (&mu)[NB])
+{
+    constexpr int NS = Tab::S;
+    const int i = threadIdx.x;
+    if constexpr (ST) {
+        // the forward's stage points and products A X_m
+#pragma unroll
+        for (int m = 0; m < NS; m++)
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+                S X = S(0), z = S(0);
+                if (step[b]) {
+                    X = dw_unpack(__ldcs(srec[b] + 2 + m * NT + i));
+                    z = dw_unpack(__ldcs(srec[b] + 2 + (NS + m) * NT + i));
+                }
+                xall[((size_t)m * NT + i) * NB + b] = X;
+                zall[((size_t)m * NT + i) * NB + b] = z;
+            }
+        __syncthreads();
+    }
+    // recompute the stages (compute_intermediate_states)
+    S K[NS][NB];
+#pragma unroll
+    for (int m = 0; m < NS && !ST; m++) {
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+            xall[((size_t)m * NT + i) * NB + b] = bundle_stage_point<Tab, S, NB>(m, b, y[b], ys[b], K, h[b], sh[b]);
+        __syncthreads();
+        S z[NB];
+        bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xall + (size_t)m * NT * NB, z);
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            zall[((size_t)m * NT + i) * NB + b] = z[b];
+            K[m][b] = xall[((size_t)m * NT + i) * NB + b] * (r[b] + z[b]);
+        }
+    }
+    // seeds and the stage loop s..1 (back_prop_step)
+    S Kbar[NS][NB];
+    double ybar[NB];
+    S gsum[NB], vsum[NB];
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+        ybar[b] = lam[b];
+#pragma unroll
+        for (int m = 0; m < NS; m++) {
+            if constexpr (std::is_same<S, double>::value)
+                Kbar[m][b] = (Tab::b(m) * h[b]) * lam[b];
+            else
+                Kbar[m][b] = (S(Tab::b(m)) * sh[b]) * from_d<S>(lam[b]);
+        }
+    }
+#pragma unroll
+    for (int m = NS - 1; m >= 0; m--) {
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            const S x = xall[((size_t)m * NT + i) * NB + b];
+            vall[((size_t)m * NT + i) * NB + b] = step[b] ? Kbar[m][b] * x : S(0);
+        }
+        __syncthreads();
+        // g = w (r + z), then += A_ji v_j for j ascending (the oracle's
+        // order); A[j][i] is read row-major, coalesced across threads
+        S g_all[NB];
+#pragma unroll
+        for (int b = 0; b < NB; b++)
+            g_all[b] = Kbar[m][b] * (r[b] + zall[((size_t)m * NT + i) * NB + b]);
+        bundle_matvec_acc<NT, NB, S, 16>(bp.A, bp.Aw, vall + (size_t)m * NT * NB, g_all);
+#pragma unroll
+        for (int b = 0; b < NB; b++) {
+            if (!step[b])
+                continue;
+            const S v = vall[((size_t)m * NT + i) * NB + b];
+            const S g = g_all[b];
+            if constexpr (std::is_same<S, double>::value) {
+                ybar[b] += g;
+                mu[b] += v;
+            } else {
+                gsum[b] = (m == NS - 1) ? g : gsum[b] + g;
+                vsum[b] = (m == NS - 1) ? v : vsum[b] + v;
+            }
+#pragma unroll
+            for (int k = 0; k < NS - 1; k++)
+                if (k < m) {
+                    if constexpr (std::is_same<S, double>::value)
+                        Kbar[k][b] += g * Tab::a(m, k) * h[b];
+                    else
+                        Kbar[k][b] = madd(g * S(Tab::a(m, k)), sh[b], Kbar[k][b]);
+                }
+        }
+        __syncthreads();
+    }
+    if constexpr (ST) {
+        if (bp.fac_v) {
+            // deferred dA: this step's factor rows v_m (and pointers to X_m)
+            constexpr int NSV = factor_stages<Tab>();
+#pragma unroll
+            for (int b = 0; b < NB; b++) {
+                if (!step[b])
+                    continue;
+                const size_t k0 = (size_t)bp.k_base[inst[b]] + (size_t)j[b] * NSV;
+#pragma unroll
+                for (int m = 0; m < NSV; m++) {
+                    bp.fac_v[(k0 + m) * NT + i] = dw_pack(vall[((size_t)m * NT + i) * NB + b]);
+                    if (i == 0)
+                        bp.fac_xp[k0 + m] = srec[b] + 2 + (size_t)m * NT;
+                }
+            }
+        }
+    }
+    // dA partial: part[jj][i] += sum_{m,b} v_{m,b,i} x_{m,b,jj}
+    if (!(ST && bp.fac_v)) {
+        S vi[NS][NB];
+#pragma unroll
+        for (int m = 0; m < NS; m++)
+#pragma unroll
+            for (int b = 0; b < NB; b++)
+                vi[m][b] = vall[((size_t)m * NT + i) * NB + b];
+        if constexpr (std::is_same<S, dword>::value) {
+            // the partial stays a double-word (packed in the 8-byte
+            // slot): accumulating it in FP64 cost four FP64-pipe
+            // operations per element and step.  Eight rows per
+            // iteration keep eight partial loads in flight (the
+            // partials of all CTAs exceed L2: DRAM latency)
+#pragma unroll 8
+            for (int jj = 0; jj < NT; jj++) {
+                dacc acc{0.0f, 0.0f};
+#pragma unroll
+                for (int m = NS - 1; m >= 0; m--)
+#pragma unroll
+                    for (int b = 0; b < NB; b++)
+                        dacc_fma(acc, vi[m][b], xall[((size_t)m * NT + jj) * NB + b]);
+                double &pe = part[(size_t)jj * NT + i];
+                pe = dw_pack(dw_unpack(pe) + dacc_get(acc));
+            }
+        } else {
+            for (int jj = 0; jj < NT; jj++) {
+                S acc = S(0);
+#pragma unroll
+                for (int m = NS - 1; m >= 0; m--)
+#pragma unroll
+                    for (int b = 0; b < NB; b++)
+                        acc = madd(vi[m][b], xall[((size_t)m * NT + jj) * NB + b], acc);
+                part[(size_t)jj * NT + i] += to_d(acc);
+            }
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+        if (!step[b])
+            continue;
+        if constexpr (std::is_same<S, double>::value) {
+            lam[b] = ybar[b];
+        } else {
+            lam[b] += to_d(gsum[b]);
+            mu[b] += to_d(vsum[b]);
+        }
+    }
+}
+
 
 // bundles of two: two CTAs per SM (128 registers per thread); larger
 // bundles: no minimum (0), the compiler's own register choice
@@ -612,174 +835,12 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel(Bu
             ys[b] = from_d<S>(y[b]);
             sh[b] = from_d<S>(h[b]);
         }
-        if constexpr (ST) {
-            // the forward's stage points and products A X_m
-#pragma unroll
-            for (int m = 0; m < NS; m++)
-#pragma unroll
-                for (int b = 0; b < NB; b++) {
-                    S X = S(0), z = S(0);
-                    if (step[b]) {
-                        X = dw_unpack(__ldcs(srec[b] + 2 + m * NT + i));
-                        z = dw_unpack(__ldcs(srec[b] + 2 + (NS + m) * NT + i));
-                    }
-                    xall[((size_t)m * NT + i) * NB + b] = X;
-                    zall[((size_t)m * NT + i) * NB + b] = z;
-                }
-            __syncthreads();
-        }
-        // recompute the stages (compute_intermediate_states)
-        S K[NS][NB];
-#pragma unroll
-        for (int m = 0; m < NS && !ST; m++) {
-#pragma unroll
-            for (int b = 0; b < NB; b++) {
-                S X;
-                if constexpr (std::is_same<S, double>::value) {
-                    double acc = y[b];
-#pragma unroll
-                    for (int jj = 0; jj < NS - 1; jj++)
-                        if (jj < m)
-                            acc = acc + (Tab::a(m, jj) * h[b]) * K[jj][b];
-                    X = acc;
-                } else {
-                    S acc = S(0);
-#pragma unroll
-                    for (int jj = 0; jj < NS - 1; jj++)
-                        if (jj < m)
-                            acc = madd(S(Tab::a(m, jj)), K[jj][b], acc);
-                    X = madd(acc, sh[b], ys[b]);
-                }
-                xall[((size_t)m * NT + i) * NB + b] = X;
-            }
-            __syncthreads();
-            S z[NB];
-            bundle_matvec<NT, NB, S>(bp.At, bp.Atw, xall + (size_t)m * NT * NB, z);
-#pragma unroll
-            for (int b = 0; b < NB; b++) {
-                zall[((size_t)m * NT + i) * NB + b] = z[b];
-                K[m][b] = xall[((size_t)m * NT + i) * NB + b] * (r[b] + z[b]);
-            }
-        }
-        // seeds and the stage loop s..1 (back_prop_step)
-        S Kbar[NS][NB];
-        double ybar[NB];
-        S gsum[NB], vsum[NB];
-#pragma unroll
-        for (int b = 0; b < NB; b++) {
-            ybar[b] = lam[b];
-#pragma unroll
-            for (int m = 0; m < NS; m++) {
-                if constexpr (std::is_same<S, double>::value)
-                    Kbar[m][b] = (Tab::b(m) * h[b]) * lam[b];
-                else
-                    Kbar[m][b] = (S(Tab::b(m)) * sh[b]) * from_d<S>(lam[b]);
-            }
-        }
-#pragma unroll
-        for (int m = NS - 1; m >= 0; m--) {
-#pragma unroll
-            for (int b = 0; b < NB; b++) {
-                const S x = xall[((size_t)m * NT + i) * NB + b];
-                vall[((size_t)m * NT + i) * NB + b] = step[b] ? Kbar[m][b] * x : S(0);
-            }
-            __syncthreads();
-            // g = w (r + z), then += A_ji v_j for j ascending (the oracle's
-            // order); A[j][i] is read row-major, coalesced across threads
-            S g_all[NB];
-#pragma unroll
-            for (int b = 0; b < NB; b++)
-                g_all[b] = Kbar[m][b] * (r[b] + zall[((size_t)m * NT + i) * NB + b]);
-            bundle_matvec_acc<NT, NB, S, 16>(bp.A, bp.Aw, vall + (size_t)m * NT * NB, g_all);
-#pragma unroll
-            for (int b = 0; b < NB; b++) {
-                if (!step[b])
-                    continue;
-                const S v = vall[((size_t)m * NT + i) * NB + b];
-                const S g = g_all[b];
-                if constexpr (std::is_same<S, double>::value) {
-                    ybar[b] += g;
-                    mu[b] += v;
-                } else {
-                    gsum[b] = (m == NS - 1) ? g : gsum[b] + g;
-                    vsum[b] = (m == NS - 1) ? v : vsum[b] + v;
-                }
-#pragma unroll
-                for (int k = 0; k < NS - 1; k++)
-                    if (k < m) {
-                        if constexpr (std::is_same<S, double>::value)
-                            Kbar[k][b] += g * Tab::a(m, k) * h[b];
-                        else
-                            Kbar[k][b] = madd(g * S(Tab::a(m, k)), sh[b], Kbar[k][b]);
-                    }
-            }
-            __syncthreads();
-        }
-        if constexpr (ST) {
-            if (bp.fac_v) {
-                // deferred dA: this step's factor rows v_m (and pointers to X_m)
-                constexpr int NSV = factor_stages<Tab>();
-#pragma unroll
-                for (int b = 0; b < NB; b++) {
-                    if (!step[b])
-                        continue;
-                    const size_t k0 = (size_t)bp.k_base[inst[b]] + (size_t)j[b] * NSV;
-#pragma unroll
-                    for (int m = 0; m < NSV; m++) {
-                        bp.fac_v[(k0 + m) * NT + i] = dw_pack(vall[((size_t)m * NT + i) * NB + b]);
-                        if (i == 0)
-                            bp.fac_xp[k0 + m] = srec[b] + 2 + (size_t)m * NT;
-                    }
-                }
-            }
-        }
-        // dA partial: part[jj][i] += sum_{m,b} v_{m,b,i} x_{m,b,jj}
-        if (!(ST && bp.fac_v)) {
-            S vi[NS][NB];
-#pragma unroll
-            for (int m = 0; m < NS; m++)
-#pragma unroll
-                for (int b = 0; b < NB; b++)
-                    vi[m][b] = vall[((size_t)m * NT + i) * NB + b];
-            if constexpr (std::is_same<S, dword>::value) {
-                // the partial stays a double-word (packed in the 8-byte
-                // slot): accumulating it in FP64 cost four FP64-pipe
-                // operations per element and step.  Eight rows per
-                // iteration keep eight partial loads in flight (the
-                // partials of all CTAs exceed L2: DRAM latency)
-#pragma unroll 8
-                for (int jj = 0; jj < NT; jj++) {
-                    dacc acc{0.0f, 0.0f};
-#pragma unroll
-                    for (int m = NS - 1; m >= 0; m--)
-#pragma unroll
-                        for (int b = 0; b < NB; b++)
-                            dacc_fma(acc, vi[m][b], xall[((size_t)m * NT + jj) * NB + b]);
-                    double &pe = part[(size_t)jj * NT + i];
-                    pe = dw_pack(dw_unpack(pe) + dacc_get(acc));
-                }
-            } else {
-                for (int jj = 0; jj < NT; jj++) {
-                    S acc = S(0);
-#pragma unroll
-                    for (int m = NS - 1; m >= 0; m--)
-#pragma unroll
-                        for (int b = 0; b < NB; b++)
-                            acc = madd(vi[m][b], xall[((size_t)m * NT + jj) * NB + b], acc);
-                    part[(size_t)jj * NT + i] += to_d(acc);
-                }
-            }
-        }
+        bundle_back_step<NT, NB, Tab, S, ST>(bp, xall, vall, zall, step, y, h, ys, sh, srec, r, inst, j, part, lam,
+                                             mu);
 #pragma unroll
         for (int b = 0; b < NB; b++) {
             if (!step[b])
                 continue;
-            if constexpr (std::is_same<S, double>::value) {
-                lam[b] = ybar[b];
-            } else {
-                lam[b] += to_d(gsum[b]);
-                mu[b] += to_d(vsum[b]);
-            }
             t_next[b] = tn[b];
             j[b]--;
             if (j[b] < 0) {

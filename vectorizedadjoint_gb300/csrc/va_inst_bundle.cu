@@ -68,6 +68,12 @@ static BundleKernelSet make_bundle(void (*fill_fp64)(BundleKernelSet &))
         fill_bundle_alt256(k);
         fill_bundle_alt_fp64_256(k);
     }
+    if constexpr (NT == 64)
+        fill_bundle_2level64(k);
+    else
+        fill_bundle_2level256(k);
+    for (int p = 0; p < 3; p++)
+        k.smem_bwd2[p] = k.smem_bwd[p] + sizeof(double) * (NT / 32) * k.nb[p];
     k.nb_alt[0] = k.nb_alt[1] = kBundleNBdw;
     k.nb_alt[2] = kBundleNB;
     for (int p = 0; p < 3; p++) {

@@ -113,7 +113,14 @@ struct BundleKernelSet {
     const void *fwd_alt[kTableaux][3], *bwd_alt[kTableaux][3];
     const void *fwd1_alt[kTableaux][3], *bwd1_alt[kTableaux][3];
     size_t smem_fwd_alt[3], smem_bwd_alt[3];
+    // two-level backward (checkpoint stride > 1) in bundles of nb[precision];
+    // its dynamic shared memory is smem_bwd2[precision]
+    const void *bwd2[kTableaux][3];
+    size_t smem_bwd2[3];
 };
+// two-level bundle kernels (va_inst_bundle_2level.cu, va_inst_bundle_2level_fp64.cu)
+void fill_bundle_2level64(BundleKernelSet &k);
+void fill_bundle_2level256(BundleKernelSet &k);
 // alternate-width bundle kernels (va_inst_bundle_alt.cu, va_inst_bundle_alt_fp64.cu)
 void fill_bundle_alt64(BundleKernelSet &k);
 void fill_bundle_alt256(BundleKernelSet &k);
