@@ -177,7 +177,7 @@ __device__ __forceinline__ void slice_row8(const double (&vals)[8], DigitScale s
 // Slices chunk c of the CTA's tile into one shared-memory stage and stores
 // the column exponents (e_v[128], e_x[64]).
 __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int K, int ti, int tj, uint8_t *stage,
-                                            int *ev, int *ex, float *red)
+                                            int *ev, int *ex, float *red, const double *const *xrow)
 {
     const int t = threadIdx.x;
     const int k0 = c * kContractKC;
@@ -202,7 +202,7 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
         for (int r = 0; r < 16; r++) {
             const int k = k0 + 16 * q + r;
             if (k < K)
-                m = fmaxf(m, dw_abs_hi(__ldg(p.xp[k] + tj * kContractTileN + j)));
+                m = fmaxf(m, dw_abs_hi(__ldg(xrow[16 * q + r] + tj * kContractTileN + j)));
         }
         red[256 + t] = m;
     }
@@ -244,16 +244,19 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
 #pragma unroll
             for (int r = 0; r < 8; r++) {
                 const int k = k0 + 8 * kg + r;
-                vals[r] = k < K ? __ldg(p.xp[k] + tj * kContractTileN + j) : 0.0;
+                vals[r] = k < K ? __ldg(xrow[8 * kg + r] + tj * kContractTileN + j) : 0.0;
             }
             slice_row8(vals, sc, xs + (size_t)kg * 1024 + j * 16, (size_t)kContractKC * kContractTileN * 2);
         }
     }
 }
 
-// Prefetch of chunk c's rows of the CTA's tile into L2 (the factor rows are
-// read once from DRAM; the slicing loads then wait on L2 instead)
-__device__ __forceinline__ void prefetch_chunk(const ContractParams &p, int c, int K, int ti, int tj)
+// The x-row pointers of chunk c into xrow[64] (rows past K: null, never
+// dereferenced), and a prefetch of the chunk's rows of the CTA's tile into
+// L2 (the factor rows are read once from DRAM; the slicing loads then wait
+// on L2 instead)
+__device__ __forceinline__ void prefetch_chunk(const ContractParams &p, int c, int K, int ti, int tj,
+                                               const double **xrow)
 {
     const int t = threadIdx.x;
     const int kv = c * kContractKC + (t >> 2);
@@ -263,10 +266,15 @@ __device__ __forceinline__ void prefetch_chunk(const ContractParams &p, int c, i
         asm volatile("prefetch.global.L2 [%0];" ::"l"(row + 16));
     }
     const int kx = c * kContractKC + (t & 63);
-    if (t < 128 && kx < K) {
-        const double *row = p.xp[kx] + tj * kContractTileN + (t >> 6) * 32;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(row));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(row + 16));
+    if (t < 128) {
+        const double *base = kx < K ? p.xp[kx] : nullptr;
+        if (t < 64)
+            xrow[t] = base;
+        if (base) {
+            const double *row = base + tj * kContractTileN + (t >> 6) * 32;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(row));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(row + 16));
+        }
     }
 }
 
@@ -340,6 +348,7 @@ __global__ void __launch_bounds__(256, 1) contract_kernel(ContractParams p)
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 2);
     __shared__ int ev_s[2][kContractTileM], ex_s[2][kContractTileN];
     __shared__ float red[512];
+    __shared__ const double *xrow_s[2][kContractKC]; // x-row pointers of the chunk in each stage
 
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int tile = blockIdx.x % kContractTiles, split = blockIdx.x / kContractTiles;
@@ -377,12 +386,15 @@ __global__ void __launch_bounds__(256, 1) contract_kernel(ContractParams p)
     bool ok = true;
     int issued = 0, waited = 0; // chunks committed / chunks whose commit was awaited
     const int n = c1 - c0;
+    if (n > 0)
+        prefetch_chunk(p, c0, K, ti, tj, xrow_s[0]);
+    __syncthreads();
     for (int idx = 0; idx < n; idx++) {
         const int st = idx & 1;
         if (ok) {
-            slice_chunk(p, c0 + idx, K, ti, tj, stages[st], ev_s[st], ex_s[st], red);
+            slice_chunk(p, c0 + idx, K, ti, tj, stages[st], ev_s[st], ex_s[st], red, xrow_s[st]);
             if (idx + 1 < n)
-                prefetch_chunk(p, c0 + idx + 1, K, ti, tj);
+                prefetch_chunk(p, c0 + idx + 1, K, ti, tj, xrow_s[st ^ 1]);
         }
         // the digit planes, written by this CTA's threads, feed the tensor core
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
