@@ -240,14 +240,15 @@ DW_TRAFFIC = {("vdpb", "forward"): 100.6e6 + 5552.3e6, ("vdpb", "backward"): 565
 
 def pipe_rates():
     """This GPU's arithmetic pipe rates from the library's probes
-    (va_probe_rate): FP64 FMA, FP32 FMA and FP64 tensor-core MMA, TFLOP/s."""
+    (va_probe_rate): FP64 FMA, FP32 FMA and FP64 tensor-core MMA, TFLOP/s;
+    INT8 dp4a, tera-operations/s (8 per instruction and lane)."""
     import ctypes
 
     from vectorizedadjoint_gb300 import _lib
     L = _lib.load()
     out = {}
     for kind, name, iters in [(0, "fp64_fma", 4096), (1, "fp32_fma", 65536), (2, "fp64_mma_m8n8k4", 2048),
-                              (3, "fp64_mma_m16n8k16", 512)]:
+                              (3, "fp64_mma_m16n8k16", 512), (4, "int8_dp4a_tops", 65536)]:
         tf, ms = ctypes.c_double(), ctypes.c_double()
         st = L.va_probe_rate(kind, iters, ctypes.byref(tf), ctypes.byref(ms))
         out[name] = tf.value if st == 0 else None

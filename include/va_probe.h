@@ -18,7 +18,7 @@ extern "C" {
 #endif
 
 /* kind 0: FP64 FMA, 1: FP32 FMA, 2: FP64 MMA m8n8k4 (mma.sync), 3: FP64 MMA
- * m16n8k16 (mma.sync).  Runs `iters` iterations of eight independent chains
+ * m16n8k16 (mma.sync), 4: INT8 dot product dp4a (8 operations each).  Runs `iters` iterations of eight independent chains
  * per thread (or warp) on 8 blocks of 256 threads per SM of the current
  * device, best of three timed launches; writes TFLOP/s (FMA = 2 FLOPs) and
  * the launch time in ms (ms_out may be NULL).  Allocates a small output

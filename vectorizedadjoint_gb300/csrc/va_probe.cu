@@ -109,11 +109,32 @@ __global__ void probe_dmma_m16n8k16(int iters, double *sink)
     sink[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// INT8 dot products with INT32 accumulation (dp4a: four multiply-adds per
+// instruction and lane; counted as 8 operations)
+__global__ void probe_dp4a(int iters, double *sink)
+{
+    int acc[kChains];
+    const int a = 0x01020304 + threadIdx.x, b = 0x05060708 ^ threadIdx.x;
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+        acc[c] = c;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int c = 0; c < kChains; c++)
+            acc[c] = __dp4a(a, b, acc[c]);
+    }
+    int s = 0;
+#pragma unroll
+    for (int c = 0; c < kChains; c++)
+        s += acc[c];
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = (double)s;
+}
+
 } // namespace
 
 extern "C" VA_API int32_t va_probe_rate(int32_t kind, int32_t iters, double *tflops, double *ms_out)
 {
-    if (!tflops || iters <= 0 || kind < 0 || kind > 3)
+    if (!tflops || iters <= 0 || kind < 0 || kind > 4)
         return VA_BAD_ARGS;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -130,7 +151,8 @@ extern "C" VA_API int32_t va_probe_rate(int32_t kind, int32_t iters, double *tfl
         case 0: probe_fp64_fma<<<blocks, threads>>>(n, sink); break;
         case 1: probe_fp32_fma<<<blocks, threads>>>(n, sink); break;
         case 2: probe_dmma_m8n8k4<<<blocks, threads>>>(n, sink); break;
-        default: probe_dmma_m16n8k16<<<blocks, threads>>>(n, sink); break;
+        case 3: probe_dmma_m16n8k16<<<blocks, threads>>>(n, sink); break;
+        default: probe_dp4a<<<blocks, threads>>>(n, sink); break;
         }
     };
     launch(iters / 8 + 1); // warm-up
@@ -151,8 +173,9 @@ extern "C" VA_API int32_t va_probe_rate(int32_t kind, int32_t iters, double *tfl
     cudaFree(sink);
     if (err != cudaSuccess)
         return VA_CUDA_ERROR;
-    const double ops_per_iter = kind <= 1 ? 2.0 * kChains * threads                  // per thread FMAs
-                                          : (kind == 2 ? 2.0 * 8 * 8 * 4 : 2.0 * 16 * 8 * 16) * kChains * threads / 32;
+    const double ops_per_iter = kind <= 1   ? 2.0 * kChains * threads // per thread FMAs
+                                : kind == 4 ? 8.0 * kChains * threads // per thread dp4a
+                                            : (kind == 2 ? 2.0 * 8 * 8 * 4 : 2.0 * 16 * 8 * 16) * kChains * threads / 32;
     const double flop = ops_per_iter * blocks * (double)iters;
     *tflops = flop / (best * 1e-3) / 1e12;
     if (ms_out)
