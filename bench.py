@@ -252,6 +252,10 @@ def pipe_rates():
         tf, ms = ctypes.c_double(), ctypes.c_double()
         st = L.va_probe_rate(kind, iters, ctypes.byref(tf), ctypes.byref(ms))
         out[name] = tf.value if st == 0 else None
+    for n in (16, 32, 64, 128, 256):
+        tf, ms = ctypes.c_double(), ctypes.c_double()
+        st = L.va_probe_mma_bf16(n, 8192, ctypes.byref(tf), ctypes.byref(ms))
+        out[f"bf16_tcgen05_m128n{n}k16"] = tf.value if st == 0 else None
     return out
 
 

@@ -26,7 +26,8 @@ EXPORTS = ["va_default_options", "va_create", "va_destroy", "va_forward", "va_ba
            "va_get_launch", "va_checkpoint_info",
            "va_trajectory", "va_set_adjoint_history", "va_adjoint_history", "va_adjoint_history_buffer",
            "va_set_shared", "va_last_error", "va_status_string", "va_probe_rate",
-           "va_step_pow_undecided", "va_create_model", "va_forward_frozen", "va_contract_dA"]
+           "va_step_pow_undecided", "va_create_model", "va_forward_frozen", "va_contract_dA",
+           "va_probe_mma_bf16"]
 
 
 class VaProblem(ctypes.Structure):
@@ -98,6 +99,8 @@ def load():
     L.va_step_pow_undecided.argtypes = [H, ctypes.POINTER(ctypes.c_int64)]
     L.va_probe_rate.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                                 ctypes.POINTER(ctypes.c_double)]
+    L.va_probe_mma_bf16.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double)]
     for name in EXPORTS:
         f = getattr(L, name)
         if f.restype is ctypes.c_int:  # default restype

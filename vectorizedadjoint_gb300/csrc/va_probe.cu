@@ -14,6 +14,7 @@
 
 #include "va.h"
 #include "va_probe.h"
+#include "va_tcgen05.cuh"
 
 namespace {
 
@@ -130,7 +131,97 @@ __global__ void probe_dp4a(int iters, double *sink)
     sink[blockIdx.x * blockDim.x + threadIdx.x] = (double)s;
 }
 
+// tcgen05.mma kind::f16 (bf16 inputs, FP32 accumulator in tensor memory),
+// M = 128, N = n, K = 16: one CTA per SM, one thread issuing `iters` MMAs
+// into one accumulator (as the K loop of a GEMM does), then a commit and a
+// bounded wait.  Operands: zeros in the no-swizzle K-major layout.
+constexpr int kProbeTmemCols = 256;
+__global__ void __launch_bounds__(128) probe_tcgen05(int n, int iters, unsigned *error)
+{
+    __shared__ __align__(1024) uint8_t a_s[2 * 128 * 16]; // [kgroup 2][row 128][8 bf16]
+    __shared__ __align__(1024) uint8_t b_s[2 * 256 * 16]; // [kgroup 2][row n][8 bf16]
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tmem_slot;
+    const int t = threadIdx.x;
+    for (int k = t; k < (int)sizeof(a_s) / 4; k += blockDim.x)
+        reinterpret_cast<uint32_t *>(a_s)[k] = 0u;
+    for (int k = t; k < (int)sizeof(b_s) / 4; k += blockDim.x)
+        reinterpret_cast<uint32_t *>(b_s)[k] = 0u;
+    if (t < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(va::smem_u32(&tmem_slot)),
+                     "r"(kProbeTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (t == 0) {
+        va::mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    va::tc_fence_before();
+    __syncthreads();
+    va::tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    bool ok = true;
+    if (t == 0) {
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+        const uint64_t ad = va::umma_desc(va::smem_u32(a_s), 128 * 16, 128);
+        const uint64_t bd = va::umma_desc(va::smem_u32(b_s), (uint32_t)n * 16, 128);
+        for (int it = 0; it < iters; it++)
+            va::umma_bf16(tmem, ad, bd, idesc, it > 0 ? 1u : 0u);
+        va::umma_commit(&bar);
+        ok = va::mbar_wait_bounded(&bar, 0, error);
+        if (!ok) // once more (bounded) before the tensor memory is released
+            (void)va::mbar_wait_bounded(&bar, 0, error);
+    }
+    __syncthreads();
+    va::tc_fence_after();
+    if (t < 32)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kProbeTmemCols) : "memory");
+}
+
 } // namespace
+
+// tcgen05 bf16 MMA rate at M = 128, K = 16 and the given N (16..256, a
+// multiple of 16): TFLOP/s (2 M N K per MMA) over one CTA per SM.
+extern "C" VA_API int32_t va_probe_mma_bf16(int32_t n, int32_t iters, double *tflops, double *ms_out)
+{
+    if (!tflops || iters <= 0 || n < 16 || n > 256 || n % 16)
+        return VA_BAD_ARGS;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return VA_CUDA_ERROR;
+    unsigned *err = nullptr;
+    if (cudaMalloc(&err, sizeof(unsigned)) != cudaSuccess)
+        return VA_CUDA_ERROR;
+    cudaMemset(err, 0, sizeof(unsigned));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    probe_tcgen05<<<sms, 128>>>(n, iters / 8 + 1, err); // warm-up
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(e0);
+        probe_tcgen05<<<sms, 128>>>(n, iters, err);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best)
+            best = ms;
+    }
+    unsigned herr = 0;
+    const cudaError_t ce = cudaMemcpy(&herr, err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(err);
+    if (ce != cudaSuccess || cudaGetLastError() != cudaSuccess || herr)
+        return VA_CUDA_ERROR;
+    *tflops = 2.0 * 128 * n * 16 * (double)iters * sms / (best * 1e-3) / 1e12;
+    if (ms_out)
+        *ms_out = best;
+    return VA_OK;
+}
 
 extern "C" VA_API int32_t va_probe_rate(int32_t kind, int32_t iters, double *tflops, double *ms_out)
 {
