@@ -252,10 +252,10 @@ def pipe_rates():
         tf, ms = ctypes.c_double(), ctypes.c_double()
         st = L.va_probe_rate(kind, iters, ctypes.byref(tf), ctypes.byref(ms))
         out[name] = tf.value if st == 0 else None
-    for n in (16, 32, 64, 128, 256):
+    for n, ctas in ((16, 1), (16, 2), (32, 1), (32, 2), (64, 1), (64, 2), (128, 1), (128, 2), (256, 1)):
         tf, ms = ctypes.c_double(), ctypes.c_double()
-        st = L.va_probe_mma_bf16(n, 8192, ctypes.byref(tf), ctypes.byref(ms))
-        out[f"bf16_tcgen05_m128n{n}k16"] = tf.value if st == 0 else None
+        st = L.va_probe_mma_bf16(n, 1, ctas, 8192, ctypes.byref(tf), ctypes.byref(ms))
+        out[f"bf16_tcgen05_m128n{n}k16_{ctas}cta"] = tf.value if st == 0 else None
     return out
 
 

@@ -27,10 +27,12 @@ VA_API int32_t va_probe_rate(int32_t kind, int32_t iters, double *tflops, double
 
 /* The bf16 tensor-core MMA rate (tcgen05.mma kind::f16, FP32 accumulation
  * in tensor memory) at M = 128, K = 16 and N = n (16..256, a multiple of 16):
- * one CTA per SM issuing `iters` MMAs into one accumulator; TFLOP/s
- * (2 M N K per MMA) and the launch time in ms (ms_out may be NULL).
- * Returns a va_status (VA_CUDA_ERROR also when the bounded wait gave up). */
-VA_API int32_t va_probe_mma_bf16(int32_t n, int32_t iters, double *tflops, double *ms_out);
+ * `ctas` CTAs per SM (1 or 2), each issuing `iters` MMAs (a multiple of 8)
+ * round-robin into `naccs` independent accumulators (1..8, naccs * n <= 256); TFLOP/s (2 M N K per MMA) and the launch
+ * time in ms (ms_out may be NULL).  Returns a va_status (VA_CUDA_ERROR also
+ * when the bounded wait gave up). */
+VA_API int32_t va_probe_mma_bf16(int32_t n, int32_t naccs, int32_t ctas, int32_t iters, double *tflops,
+                                 double *ms_out);
 
 /* The tensor-core contraction the shared-matrix GLV backward sweep uses for
  * its matrix gradient, on caller data: dA[256][256] = sum_k v_k x_k^T for

@@ -99,8 +99,8 @@ def load():
     L.va_step_pow_undecided.argtypes = [H, ctypes.POINTER(ctypes.c_int64)]
     L.va_probe_rate.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                                 ctypes.POINTER(ctypes.c_double)]
-    L.va_probe_mma_bf16.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
-                                    ctypes.POINTER(ctypes.c_double)]
+    L.va_probe_mma_bf16.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     for name in EXPORTS:
         f = getattr(L, name)
         if f.restype is ctypes.c_int:  # default restype

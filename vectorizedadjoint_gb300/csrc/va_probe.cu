@@ -133,10 +133,11 @@ __global__ void probe_dp4a(int iters, double *sink)
 
 // tcgen05.mma kind::f16 (bf16 inputs, FP32 accumulator in tensor memory),
 // M = 128, N = n, K = 16: one CTA per SM, one thread issuing `iters` MMAs
-// into one accumulator (as the K loop of a GEMM does), then a commit and a
+// (a multiple of 8, unrolled by 8 with the accumulator addresses computed
+// beforehand) round-robin into naccs accumulators, then a commit and a
 // bounded wait.  Operands: zeros in the no-swizzle K-major layout.
 constexpr int kProbeTmemCols = 256;
-__global__ void __launch_bounds__(128) probe_tcgen05(int n, int iters, unsigned *error)
+__global__ void __launch_bounds__(128) probe_tcgen05(int n, int iters, int naccs, unsigned *error)
 {
     __shared__ __align__(1024) uint8_t a_s[2 * 128 * 16]; // [kgroup 2][row 128][8 bf16]
     __shared__ __align__(1024) uint8_t b_s[2 * 256 * 16]; // [kgroup 2][row n][8 bf16]
@@ -162,16 +163,24 @@ __global__ void __launch_bounds__(128) probe_tcgen05(int n, int iters, unsigned 
     __syncthreads();
     va::tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    bool ok = true;
     if (t == 0) {
         const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
         const uint64_t ad = va::umma_desc(va::smem_u32(a_s), 128 * 16, 128);
         const uint64_t bd = va::umma_desc(va::smem_u32(b_s), (uint32_t)n * 16, 128);
-        for (int it = 0; it < iters; it++)
-            va::umma_bf16(tmem, ad, bd, idesc, it > 0 ? 1u : 0u);
+        uint32_t acc[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            acc[u] = tmem + (uint32_t)((u % naccs) * n);
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            va::umma_bf16(acc[u], ad, bd, idesc, u >= naccs ? 1u : 0u);
+        for (int it = 8; it < iters; it += 8) {
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                va::umma_bf16(acc[u], ad, bd, idesc, 1u);
+        }
         va::umma_commit(&bar);
-        ok = va::mbar_wait_bounded(&bar, 0, error);
-        if (!ok) // once more (bounded) before the tensor memory is released
+        if (!va::mbar_wait_bounded(&bar, 0, error)) // once more (bounded) before the tensor memory is released
             (void)va::mbar_wait_bounded(&bar, 0, error);
     }
     __syncthreads();
@@ -183,10 +192,15 @@ __global__ void __launch_bounds__(128) probe_tcgen05(int n, int iters, unsigned 
 } // namespace
 
 // tcgen05 bf16 MMA rate at M = 128, K = 16 and the given N (16..256, a
-// multiple of 16): TFLOP/s (2 M N K per MMA) over one CTA per SM.
-extern "C" VA_API int32_t va_probe_mma_bf16(int32_t n, int32_t iters, double *tflops, double *ms_out)
+// multiple of 16), issued round-robin into naccs independent accumulators
+// (naccs * n <= 256) by ctas CTAs per SM (1 or 2): TFLOP/s (2 M N K per MMA).
+extern "C" VA_API int32_t va_probe_mma_bf16(int32_t n, int32_t naccs, int32_t ctas, int32_t iters, double *tflops,
+                                            double *ms_out)
 {
-    if (!tflops || iters <= 0 || n < 16 || n > 256 || n % 16)
+    if (ctas < 1 || ctas > 2)
+        return VA_BAD_ARGS;
+    if (!tflops || iters < 8 || iters % 8 || n < 16 || n > 256 || n % 16 || naccs < 1 || naccs > 8 ||
+        naccs * n > kProbeTmemCols)
         return VA_BAD_ARGS;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -198,11 +212,11 @@ extern "C" VA_API int32_t va_probe_mma_bf16(int32_t n, int32_t iters, double *tf
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    probe_tcgen05<<<sms, 128>>>(n, iters / 8 + 1, err); // warm-up
+    probe_tcgen05<<<sms * ctas, 128>>>(n, 8 * (iters / 64 + 1), naccs, err); // warm-up
     float best = 1e30f;
     for (int rep = 0; rep < 3; rep++) {
         cudaEventRecord(e0);
-        probe_tcgen05<<<sms, 128>>>(n, iters, err);
+        probe_tcgen05<<<sms * ctas, 128>>>(n, iters, naccs, err);
         cudaEventRecord(e1);
         cudaEventSynchronize(e1);
         float ms = 0.0f;
@@ -217,7 +231,7 @@ extern "C" VA_API int32_t va_probe_mma_bf16(int32_t n, int32_t iters, double *tf
     cudaFree(err);
     if (ce != cudaSuccess || cudaGetLastError() != cudaSuccess || herr)
         return VA_CUDA_ERROR;
-    *tflops = 2.0 * 128 * n * 16 * (double)iters * sms / (best * 1e-3) / 1e12;
+    *tflops = 2.0 * 128 * n * 16 * (double)iters * sms * ctas / (best * 1e-3) / 1e12;
     if (ms_out)
         *ms_out = best;
     return VA_OK;
