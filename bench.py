@@ -77,8 +77,12 @@ DOMINANT = {"glv_shared": "forward"}
 
 
 class Clocks:
-    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+    """Samples SM clocks and clock-event (throttle) reasons DURING the timed
+    region: read-only NVML queries (libnvidia-ml through ctypes) from a
+    background thread every 2 ms, kept only between __enter__ and __exit__;
+    nvidia-smi at 200 ms where NVML cannot be loaded.  Nothing is set."""
 
+    NAMES = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown", 0x4: "sw_power_cap"}
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
@@ -86,8 +90,53 @@ class Clocks:
     def __init__(self, index=0):
         self.index = index
         self.p = None
+        self.samples = []  # (sm_mhz, max_mhz, reason bits)
+        self.nvml = None
+
+    def _nvml_open(self):
+        import ctypes
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return False
+        if lib.nvmlInit_v2() != 0:
+            return False
+        h = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(h)) != 0:
+            return False
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons", None)
+        if reasons is None:
+            return False
+        self.nvml = (lib, h, reasons)
+        return True
+
+    def _nvml_sample(self):
+        import ctypes
+        lib, h, reasons = self.nvml
+        clk, mx, bits = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        if (lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(clk)) == 0 and  # NVML_CLOCK_SM
+                lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0 and reasons(h, ctypes.byref(bits)) == 0):
+            return clk.value, mx.value, bits.value
+        return None
+
+    def _poll(self):
+        while not self.stop.is_set():
+            v = self._nvml_sample()
+            if v is not None:
+                self.samples.append(v)
+            time.sleep(0.002)
 
     def __enter__(self):
+        import threading
+        if self._nvml_open():
+            self.stop = threading.Event()
+            v = self._nvml_sample()  # the first sample before the timed work starts
+            if v is not None:
+                self.samples.append(v)
+            self.thread = threading.Thread(target=self._poll, daemon=True)
+            self.thread.start()
+            return self
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
                                        "--format=csv,noheader,nounits", "-lms", "200"],
@@ -97,7 +146,11 @@ class Clocks:
         return self
 
     def __exit__(self, *a):
-        self.lines = []
+        if self.nvml:
+            self.stop.set()
+            self.thread.join(timeout=5)
+            self.nvml[0].nvmlShutdown()
+            return
         if self.p:
             time.sleep(0.3)
             self.p.terminate()
@@ -106,23 +159,20 @@ class Clocks:
             except subprocess.TimeoutExpired:
                 self.p.kill()
                 out = ""
-            self.lines = [l for l in out.splitlines() if l.strip()]
+            for l in out.splitlines():
+                f = [x.strip() for x in l.split(",")]
+                try:
+                    bits = sum(bit for bit, v in zip((0x8, 0x40, 0x20, 0x4), f[4:8]) if v.lower() == "active")
+                    self.samples.append((float(f[1]), float(f[2]), bits))
+                except (ValueError, IndexError):
+                    continue
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in getattr(self, "lines", []):
-            f = [x.strip() for x in l.split(",")]
-            try:
-                sm.append(float(f[1]))
-                mx = float(f[2])
-            except (ValueError, IndexError):
-                continue
-            for nm, v in zip(names, f[4:8]):
-                if v.lower() == "active":
-                    reasons.add(nm)
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        sm = [x[0] for x in self.samples]
+        mx = self.samples[-1][1] if self.samples else None
+        reasons = sorted({nm for x in self.samples for bit, nm in self.NAMES.items() if x[2] & bit})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(sm), "source": "nvml" if self.nvml else "nvidia-smi"}
 
 
 def cpu_baseline(cfg_name, w, seconds=10.0, threads=None):
