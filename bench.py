@@ -282,10 +282,14 @@ def gemm_tflops(torch, dtype, n):
     return 2 * n ** 3 / (best * 1e-3) / 1e12
 
 
-# DRAM bytes per launch of the one-thread double-word kernels on the Van der
-# Pol batch (262,144 instances), one ncu capture each: the forward writes the
-# stage records (112 B per accepted step), the backward reads them back.
-DW_TRAFFIC = {("vdpb", "forward"): 100.6e6 + 5552.3e6, ("vdpb", "backward"): 5655.6e6 + 22.5e6}
+# DRAM bytes (read + write) per launch of the dominant double-word kernel of
+# each workload at its full size, one ncu capture each of the timed launch
+# (dram__bytes_read.sum, dram__bytes_write.sum): the forwards write the stage
+# records (128 B per accepted step for the two-state models, 24.6 KB for the
+# shared-matrix GLV), the backwards read them back.
+DW_TRAFFIC = {("vdpb", "forward"): 121.0e6 + 5557.4e6, ("vdpb", "backward"): 5655.6e6 + 20.8e6,
+              ("dho", "forward"): 9.2e6 + 1586.3e6, ("glv10", "backward"): 745.5e6 + 4.3e6,
+              ("vdp1", "forward"): 0.05e6, ("glv256", "forward"): 12.6e6 + 1179.1e6}
 
 
 def pipe_rates():
