@@ -15,7 +15,10 @@
 // bundle.  The matrix gradient goes into the CTA's partial (reduced in CTA
 // order afterwards); its summation order differs from the every-step
 // sweep's, so dA agrees to rounding while each instance's gradients are
-// equal bit for bit.
+// equal bit for bit.  An instance whose re-integration does not land on its
+// checkpoint (VA_RECOMPUTE_MISMATCH; the same code from the same bits, so
+// not expected) may already have added steps into the partial: the CTA's
+// partial is then set to NaN, and so is dA.
 #pragma once
 
 #include "va_bundle.cuh"
@@ -68,8 +71,11 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel_2l
             slot[b]--;
         }
     };
+    bool poisoned = false; // a re-integration failed after contributing to the dA partial (CTA-uniform)
     auto fail_instance = [&](int b, int st) {
         const double nan = __longlong_as_double(0x7ff8000000000000ll);
+        if (st == ST_RECOMPUTE_MISMATCH)
+            poisoned = true;
         a.dy0[(size_t)inst[b] * NT + i] = nan;
         a.dpar[(size_t)inst[b] * NT + i] = nan;
         if (a.status_out && i == 0)
@@ -325,6 +331,9 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel_2l
             __syncthreads();
         }
     }
+    if (poisoned)
+        for (int jj = 0; jj < NT; jj++)
+            part[(size_t)jj * NT + i] = __longlong_as_double(0x7ff8000000000000ll);
 }
 
 } // namespace va
