@@ -156,6 +156,79 @@ __device__ __forceinline__ void bundle_matvec_acc(const double *Mt, const dword 
     }
 }
 
+// cp.async of 8 bytes global -> shared (this thread's own element), and the
+// waits on this thread's own groups of copies (no spin: the hardware wait)
+__device__ __forceinline__ void cp_async8(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// The double-word matrix-vector products of bundle_matvec with the matrix
+// rows streamed through a shared-memory ring of R rows (ring[R][NT]): thread
+// i copies and then reads only column i, so R rows of lookahead cost no
+// registers and need no barrier; groups of G rows per cp.async group.  The
+// same operations in the same order as bundle_matvec_acc: the same bits.
+constexpr int kRingRows = 16, kRingGroup = 4;
+template <int NT, int NB>
+__device__ __forceinline__ void bundle_matvec_dw_ring(const dword *Mtw, const dword *xs /* [NT][NB] */,
+                                                      dword (&z)[NB], dword *ring /* [kRingRows][NT] */)
+{
+    constexpr int R = kRingRows, G = kRingGroup;
+    static_assert(NT % G == 0 && R % G == 0 && R <= NT, "ring shape");
+    const int i = threadIdx.x;
+    dacc zc[NB];
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+        zc[b] = dacc{0.0f, 0.0f};
+#pragma unroll
+    for (int g = 0; g < R / G; g++) {
+#pragma unroll
+        for (int u = 0; u < G; u++)
+            cp_async8(ring + (size_t)(g * G + u) * NT + i, Mtw + (size_t)(g * G + u) * NT + i);
+        cp_async_commit();
+    }
+#pragma unroll 2
+    for (int j0 = 0; j0 < NT; j0 += G) {
+        cp_async_wait<R / G - 1>(); // rows j0 .. j0 + G - 1 have landed
+#pragma unroll
+        for (int u = 0; u < G; u++) {
+            const int j = j0 + u;
+            const dword a = ring[(size_t)(j % R) * NT + i];
+#pragma unroll
+            for (int b = 0; b < NB; b++)
+                dacc_fma(zc[b], a, xs[j * NB + b]);
+        }
+        if (j0 + R < NT) {
+#pragma unroll
+            for (int u = 0; u < G; u++)
+                cp_async8(ring + (size_t)((j0 + u) % R) * NT + i, Mtw + (size_t)(j0 + R + u) * NT + i);
+        }
+        cp_async_commit(); // (empty near the end: the group count stays uniform)
+    }
+    cp_async_wait<0>();
+#pragma unroll
+    for (int b = 0; b < NB; b++)
+        z[b] = dacc_get(zc[b]);
+}
+
+// dynamic shared memory of forward_bundle_kernel<NT, NB, *, S>: the stage
+// vectors xs[NT][NB], the reduction slots, the chunk slots and, for the
+// double-word sweep, the matrix-row ring (16-byte aligned)
+template <int NT, int NB, class S>
+__host__ __device__ constexpr size_t bundle_fwd_smem_bytes()
+{
+    const size_t base = sizeof(S) * NT * NB + sizeof(double) * (NT / 32) * NB + sizeof(int) * NB;
+    return std::is_same<S, dword>::value ? ((base + 15) & ~(size_t)15) + sizeof(dword) * kRingRows * NT : base;
+}
+
 template <int NT, int NB, class S, int UNR = 8>
 __device__ __forceinline__ void bundle_matvec(const double *Mt, const dword *Mtw, const S *xs /* [NT][NB] */,
                                               S (&z)[NB])
@@ -267,8 +340,18 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
     S *xs = reinterpret_cast<S *>(smem_raw);                               // [NT][NB]
     double *red = reinterpret_cast<double *>(smem_raw + sizeof(S) * NT * NB); // [NT/32][NB]
     int *ichunk = reinterpret_cast<int *>(red + (NT / 32) * NB);            // [NB]
+    // double-word sweep: the ring that streams A's rows (bundle_matvec_dw_ring)
+    dword *ring = reinterpret_cast<dword *>(
+        smem_raw + ((sizeof(S) * NT * NB + sizeof(double) * (NT / 32) * NB + sizeof(int) * NB + 15) & ~(size_t)15));
     const int i = threadIdx.x;
     const int CH = a.pool.chunk_len;
+    // z = A x for the bundle's vectors in xs
+    auto matvec = [&](S (&z)[NB]) {
+        if constexpr (std::is_same<S, dword>::value)
+            bundle_matvec_dw_ring<NT, NB>(bp.Atw, xs, z, ring);
+        else
+            bundle_matvec<NT, NB, S, 16>(bp.At, bp.Atw, xs, z);
+    };
 
     double y[NB], t[NB], t1[NB], dt[NB], t_start[NB];
     S ys[NB], r[NB], K[NS][NB], knew[NB];
@@ -332,7 +415,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
     }
     {
         S z[NB];
-        bundle_matvec<NT, NB, S, 16>(bp.At, bp.Atw, xs, z);
+        matvec(z);
 #pragma unroll
         for (int b = 0; b < NB; b++) {
             K[0][b] = ys[b] * (r[b] + z[b]);
@@ -470,7 +553,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
                 xs[i * NB + b] = bundle_stage_point<Tab, S, NB>(m, b, y[b], ys[b], K, dt[b], sdt[b]);
             __syncthreads();
             S z[NB];
-            bundle_matvec<NT, NB, S, 16>(bp.At, bp.Atw, xs, z);
+            matvec(z);
 #pragma unroll
             for (int b = 0; b < NB; b++) {
                 const S X = xs[i * NB + b];
@@ -497,7 +580,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
         S znew[NB];
         if constexpr (Tab::FSAL) {
             __syncthreads();
-            bundle_matvec<NT, NB, S, 16>(bp.At, bp.Atw, xs, znew);
+            matvec(znew);
 #pragma unroll
             for (int b = 0; b < NB; b++)
                 knew[b] = ynew_s[b] * (r[b] + znew[b]);
@@ -559,7 +642,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
                 xs[i * NB + b] = ys[b];
             __syncthreads();
             S z[NB];
-            bundle_matvec<NT, NB, S, 16>(bp.At, bp.Atw, xs, z);
+            matvec(z);
 #pragma unroll
             for (int b = 0; b < NB; b++) {
                 K[0][b] = ys[b] * (r[b] + z[b]);

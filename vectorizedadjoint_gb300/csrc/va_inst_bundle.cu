@@ -54,9 +54,11 @@ static BundleKernelSet make_bundle(void (*fill_fp64)(BundleKernelSet &))
     fill_fixed<NT, 3, TabRK4>(k);
     fill_fixed<NT, 4, TabEuler>(k);
     const size_t sz[3] = {sizeof(double), sizeof(float), sizeof(dword)};
+    k.smem_fwd[0] = bundle_fwd_smem_bytes<NT, NB, double>();
+    k.smem_fwd[1] = bundle_fwd_smem_bytes<NT, NB, float>();
+    k.smem_fwd[2] = bundle_fwd_smem_bytes<NT, NW, dword>();
     for (int p = 0; p < 3; p++) {
         const size_t nb = k.nb[p];
-        k.smem_fwd[p] = sz[p] * NT * nb + sizeof(double) * (NT / 32) * nb + sizeof(int) * nb;
         k.smem_bwd[p] = 3 * sz[p] * (size_t)TabDopri5::S * NT * nb;
     }
     k.prepare = (const void *)prepare_A_kernel<NT>;
@@ -76,9 +78,11 @@ static BundleKernelSet make_bundle(void (*fill_fp64)(BundleKernelSet &))
         k.smem_bwd2[p] = k.smem_bwd[p] + sizeof(double) * (NT / 32) * k.nb[p];
     k.nb_alt[0] = k.nb_alt[1] = kBundleNBdw;
     k.nb_alt[2] = kBundleNB;
+    k.smem_fwd_alt[0] = bundle_fwd_smem_bytes<NT, NW, double>();
+    k.smem_fwd_alt[1] = bundle_fwd_smem_bytes<NT, NW, float>();
+    k.smem_fwd_alt[2] = bundle_fwd_smem_bytes<NT, NB, dword>();
     for (int p = 0; p < 3; p++) {
         const size_t nb = k.nb_alt[p];
-        k.smem_fwd_alt[p] = sz[p] * NT * nb + sizeof(double) * (NT / 32) * nb + sizeof(int) * nb;
         k.smem_bwd_alt[p] = 3 * sz[p] * (size_t)TabDopri5::S * NT * nb;
     }
     return k;
