@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(256) forward_kernel_dw(FwdParams a)
         if (chunk < 0)
             return false;
         if (slot == CH) {
-            int c = (int)atomicAdd(&a.ctl->pool_next, 1u);
+            const int c = (int)atomicAdd(&a.ctl->pool_next, 1u);
             if (c >= a.pool.n_chunks) {
                 atomicOr(&a.ctl->pool_fail, 1u);
                 return false;
@@ -818,14 +818,21 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
     constexpr int PF = 1;
     double nv[PF][RS];
 
+    // the chain link of the walk's chunk, read a few records before the walk
+    // crosses into the previous chunk (the record load there does not wait
+    // on a dependent load of the link)
+    int prev_chunk = -1;
     // move the load walk one record back and load it into dst
     auto step_back_load = [&](double (&dst)[RS]) {
         if (slot == 0) {
-            chunk = a.pool.chunk_prev[chunk];
+            chunk = prev_chunk >= 0 ? prev_chunk : a.pool.chunk_prev[chunk];
+            prev_chunk = -1;
             slot = CH - 1;
         } else {
             slot--;
         }
+        if (slot == 4 || (slot < 4 && prev_chunk < 0 && slot > 0))
+            prev_chunk = a.pool.chunk_prev[chunk];
         const double *r = record_ptr<RS>(a.pool, chunk, slot);
         if constexpr (STAGES) {
 #pragma unroll
@@ -844,6 +851,7 @@ __global__ void __launch_bounds__(256) backward_kernel_dw(AdjParams a)
     auto start_seed = [&]() {
         chunk = last;
         slot = T % a.pool.chunk_len;
+        prev_chunk = -1;
         dword yTl[N], dtr;
         read_record_dw<N>(record_ptr<RS>(a.pool, chunk, slot), t_next, dtr, yTl);
         seed_lambda_dw<N>(a, (size_t)b * a.nout + q, yTl, lam);
