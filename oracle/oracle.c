@@ -841,17 +841,28 @@ typedef struct {
     const orc_problem *pb;
     int cost;
     long lo, hi;
+    long *next; /* the shared counter of the next unclaimed instance */
     const double *y0, *p, *t0, *t1;
     double *yT, *dy0, *dp;
     long *n_acc, *n_rej;
     int *status;
 } batch_job;
 
+// Instances are handed out in chunks of kBatchChunk from a shared counter
+// (instance lengths vary by an order of magnitude: a static partition left
+// cores idle while the thread with the longest instances finished).
+enum { kBatchChunk = 32 };
+
 static void *batch_worker(void *arg)
 {
     batch_job *J = (batch_job *)arg;
     int n = J->pb->n, np = J->pb->npar;
-    for (long b = J->lo; b < J->hi; b++) {
+    for (;;) {
+        const long lo = __atomic_fetch_add(J->next, (long)kBatchChunk, __ATOMIC_RELAXED);
+        if (lo >= J->hi)
+            break;
+        const long hi = lo + kBatchChunk < J->hi ? lo + kBatchChunk : J->hi;
+        for (long b = lo; b < hi; b++) {
         long na = 0, nr = 0;
         int st = orc_gradient(J->pb, J->cost, J->y0 + b * n, J->p + b * np, J->t0[b], J->t1[b],
                               J->yT ? J->yT + b * n : NULL, J->dy0 + b * n, J->dp + b * np, &na,
@@ -862,6 +873,7 @@ static void *batch_worker(void *arg)
             J->n_rej[b] = nr;
         if (J->status)
             J->status[b] = st;
+        }
     }
     return NULL;
 }
@@ -877,16 +889,13 @@ int orc_gradient_batch(const orc_problem *pb, int cost, long B, const double *y0
     pthread_t th[256];
     int created[256];
     batch_job jobs[256];
-    long per = (B + nthreads - 1) / nthreads;
+    long next = 0;
     for (int k = 0; k < nthreads; k++) {
-        long lo = k * per, hi = lo + per < B ? lo + per : B;
-        batch_job J = {pb, cost, lo, lo < hi ? hi : lo, y0, p, t0, t1, yT, dy0, dp, n_acc, n_rej, status};
+        batch_job J = {pb, cost, 0, B, &next, y0, p, t0, t1, yT, dy0, dp, n_acc, n_rej, status};
         jobs[k] = J;
         created[k] = 0;
     }
     for (int k = 0; k < nthreads; k++) {
-        if (jobs[k].lo >= jobs[k].hi)
-            continue;
         if (pthread_create(&th[k], NULL, batch_worker, &jobs[k]) == 0)
             created[k] = 1;
         else
