@@ -27,6 +27,17 @@ void sf_dd(int k, double x, double *ph, double *pl)
     default: va::step_pow_dd<8>(x, *ph, *pl); break;
     }
 }
+// the first pass of cr_step_pow: ln x from the float logarithm
+void sf_dd_fastln(int k, double x, double *ph, double *pl)
+{
+    const double lnx = (double)logf((float)x);
+    switch (k) {
+    case 3: va::step_pow_dd_ln<3>(x, lnx, *ph, *pl); break;
+    case 5: va::step_pow_dd_ln<5>(x, lnx, *ph, *pl); break;
+    case 6: va::step_pow_dd_ln<6>(x, lnx, *ph, *pl); break;
+    default: va::step_pow_dd_ln<8>(x, 0.0, *ph, *pl); break;
+    }
+}
 // the Newton root the fast controller uses
 double sf_inv_root(int k, double x)
 {

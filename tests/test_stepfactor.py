@@ -7,7 +7,9 @@ as the FP64 kernels are built).
   binary128 evaluation, over the controller's whole argument range
   (increase_step: 5^-p <= err < 0.5; decrease_step: 1 < err < 1e30).
 - Its double-double value before rounding is within 2^-98 of the power (the
-  bound Ziv's rounding test relies on, with a window of 2^-95).
+  bound Ziv's rounding test relies on, with a window of 2^-95); the first
+  pass, with ln x from the float logarithm, within 2^-71.5 (its window is
+  2^-70).
 - glibc's pow, which odeint calls, is not correctly rounded on a small
   fraction of these arguments: the reason the library's default controller
   is the correctly rounded one rather than a copy of one libm.
@@ -34,6 +36,9 @@ def sf(tmp_path_factory):
     L.sf_dd.restype = None
     L.sf_dd.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                         ctypes.POINTER(ctypes.c_double)]
+    L.sf_dd_fastln.restype = None
+    L.sf_dd_fastln.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_double)]
     L.sf_inv_root.restype = ctypes.c_double
     L.sf_inv_root.argtypes = [ctypes.c_int, ctypes.c_double]
     return L
@@ -73,6 +78,24 @@ def test_dd_value_within_bound(sf):
             ex = mpmath.power(mpmath.mpf(x), y)
             worst = max(worst, float(abs((mpmath.mpf(ph.value) + mpmath.mpf(pl.value) - ex) / ex)))
     assert worst < 2.0 ** -98, worst
+
+
+def test_first_pass_within_its_window(sf):
+    """cr_step_pow's first pass (ln x from logf) is within 2^-71.5 of the
+    power, inside its rounding-test window of 2^-70 (the analysis bounds it
+    by 2^-72.5 plus the double-double steps' 2^-98)."""
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.prec = 300
+    ph, pl = ctypes.c_double(), ctypes.c_double()
+    worst = 0.0
+    for k in KS:
+        y = mpmath.mpf(-1.0 / k)
+        for x in args(k, 3000, 20 + k):
+            x = float(x)
+            sf.sf_dd_fastln(k, x, ctypes.byref(ph), ctypes.byref(pl))
+            ex = mpmath.power(mpmath.mpf(x), y)
+            worst = max(worst, float(abs((mpmath.mpf(ph.value) + mpmath.mpf(pl.value) - ex) / ex)))
+    assert worst < 2.0 ** -71.5, worst
 
 
 def test_cr_pow_equals_oracle_binary128(sf, oracle):

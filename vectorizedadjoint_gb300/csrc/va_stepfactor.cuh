@@ -187,9 +187,10 @@ struct StepPowExp {
     static constexpr double e_over_k = (K == 5 ? 0x1p-54 : (K == 8 ? 0.0 : -0x1p-54)) / K;
 };
 
-// Steps 1-4: x^y = ph + pl within 2^-98 relative (0 < x < 1e30)
+// Steps 1-4 with ln x given: x^y = ph + pl within 2^-98 relative plus
+// (e/K) |ln x - lnx| (0 < x < 1e30)
 template <int K>
-VA_HD inline void step_pow_dd(double x, double &ph, double &pl)
+VA_HD inline void step_pow_dd_ln(double x, double lnx, double &ph, double &pl)
 {
     const double r0 = inv_root<K, 2>(x);
     // rho = 1 - x r0^K (1 - q.hi is exact: q.hi is within 2^-48 of 1)
@@ -201,7 +202,7 @@ VA_HD inline void step_pow_dd(double x, double &ph, double &pl)
     // R^e - 1 = u + u^2/2, u = e ln R = -(e/K) ln x
     double v = 0.0;
     if constexpr (K != 8) {
-        const double u = -StepPowExp<K>::e_over_k * log(x);
+        const double u = -StepPowExp<K>::e_over_k * lnx;
         v = fma(0.5 * u, u, u);
     }
     const double w = fma(c, v, c + v);
@@ -212,13 +213,33 @@ VA_HD inline void step_pow_dd(double x, double &ph, double &pl)
     pl = s.lo + t.lo;
 }
 
-// Step 5 and the domain ends.
+// Steps 1-4: x^y = ph + pl within 2^-98 relative (0 < x < 1e30)
+template <int K>
+VA_HD inline void step_pow_dd(double x, double &ph, double &pl)
+{
+    step_pow_dd_ln<K>(x, K != 8 ? log(x) : 0.0, ph, pl);
+}
+
+// Step 5 and the domain ends, in two passes.  The first takes ln x from
+// the float logarithm, (double)logf((float)x): within 2^-24 (the rounding
+// of x to float) + 1 ulp of |ln x| < 70, i.e. < 2^-16.9 absolute, which
+// moves u by < 2^-72.5 relative (|e/K| <= 2^-55.6); its rounding test uses
+// the window 2^-70 and decides all but ~2^-17 of the calls.  The others
+// take the second pass with the double logarithm and the window 2^-95.
+// Both return the correctly rounded value: the same double either way.
 template <int K>
 VA_HD_NOINLINE double cr_step_pow(double x, unsigned int *undecided)
 {
     if (!(x < 1e30))
         return x != x ? x : 0.0;
     double ph, pl;
+    if constexpr (K != 8) {
+        step_pow_dd_ln<K>(x, (double)logf((float)x), ph, pl);
+        const double E1 = 0x1p-70 * ph;
+        const double a1 = ph + (pl - E1), b1 = ph + (pl + E1);
+        if (a1 == b1)
+            return ph + pl;
+    }
     step_pow_dd<K>(x, ph, pl);
     // Ziv's rounding test over [P - E, P + E], E = 2^-95 ph
     const double E = 0x1p-95 * ph;
