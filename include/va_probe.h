@@ -45,6 +45,16 @@ VA_API int32_t va_probe_mma_bf16(int32_t n, int32_t naccs, int32_t ctas, int32_t
  * (VA_CUDA_ERROR also when a bounded wait in the kernel gave up). */
 VA_API int32_t va_contract_dA(int32_t K, const double *v, const double *x, double *dA, void *stream);
 
+/* The batched tensor-core product of the shared-matrix GLV backward sweep,
+ * on caller data: G[b][i] = sum_k A[k][i] V[b][k] (G = A^T V per instance)
+ * for DEVICE arrays A[256][256] (FP64, row-major), V[B][256] and G[B][256]
+ * (double-words packed in 8-byte slots).  Seven 8-bit digits per factor,
+ * K in quarters of 64, exact digit products on tcgen05 (bf16 inputs, FP32
+ * tensor-memory accumulators); the truncation leaves ~2^-56 of the
+ * quarter's maxima per term.  Allocates scratch, synchronises `stream`.
+ * Returns a va_status (VA_CUDA_ERROR also when a bounded wait gave up). */
+VA_API int32_t va_matT_tc(int32_t B, const double *A, const double *V, double *G, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,7 +27,7 @@ EXPORTS = ["va_default_options", "va_create", "va_destroy", "va_forward", "va_ba
            "va_trajectory", "va_set_adjoint_history", "va_adjoint_history", "va_adjoint_history_buffer",
            "va_set_shared", "va_last_error", "va_status_string", "va_probe_rate",
            "va_step_pow_undecided", "va_create_model", "va_forward_frozen", "va_contract_dA",
-           "va_probe_mma_bf16"]
+           "va_probe_mma_bf16", "va_matT_tc"]
 
 
 class VaProblem(ctypes.Structure):
@@ -96,6 +96,7 @@ def load():
                                   ctypes.POINTER(H)]
     L.va_forward_frozen.argtypes = [H, ctypes.c_int32, ctypes.c_int32, dp, ip, dp, dp, dp, dp, vp]
     L.va_contract_dA.argtypes = [ctypes.c_int32, dp, dp, dp, vp]
+    L.va_matT_tc.argtypes = [ctypes.c_int32, dp, dp, dp, vp]
     L.va_step_pow_undecided.argtypes = [H, ctypes.POINTER(ctypes.c_int64)]
     L.va_probe_rate.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double),
                                 ctypes.POINTER(ctypes.c_double)]

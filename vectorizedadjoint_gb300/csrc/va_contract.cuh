@@ -103,13 +103,15 @@ __host__ __device__ __forceinline__ DigitScale digit_scale(int e)
 }
 
 // Q digits of the double-word hi + lo (|hi + lo| < 2^e), rounding to
-// nearest at each level: hi + lo = 2^e sum_s d_s 2^(-8(s+1)) + r.
-__host__ __device__ __forceinline__ void split_digits(float hi, float lo, DigitScale sc, float (&d)[kContractQ])
+// nearest at each level: hi + lo = 2^e sum_s d_s 2^(-8(s+1)) + r,
+// |d_0| <= 256, |d_s| <= 128, |r| <= 2^(e - 8Q - 1).
+template <int Q>
+__host__ __device__ __forceinline__ void split_digits(float hi, float lo, DigitScale sc, float (&d)[Q])
 {
     // a + b = (hi + lo) 2^(8-e), |a + b| < 256; every step below is exact
     float a = hi * sc.s1 * sc.s2, b = lo * sc.s1 * sc.s2;
 #pragma unroll
-    for (int s = 0; s < kContractQ; s++) {
+    for (int s = 0; s < Q; s++) {
         const float q = rintf(a);
         d[s] = q;
         const float r = a - q; // exact: q is the integer nearest a
