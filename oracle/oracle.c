@@ -841,27 +841,29 @@ typedef struct {
     const orc_problem *pb;
     int cost;
     long lo, hi;
-    long *next; /* the shared counter of the next unclaimed instance */
+    long *next;  /* the shared counter of the next unclaimed instance */
+    long chunk;  /* instances claimed at a time */
     const double *y0, *p, *t0, *t1;
     double *yT, *dy0, *dp;
     long *n_acc, *n_rej;
     int *status;
 } batch_job;
 
-// Instances are handed out in chunks of kBatchChunk from a shared counter
-// (instance lengths vary by an order of magnitude: a static partition left
-// cores idle while the thread with the longest instances finished).
-enum { kBatchChunk = 32 };
+// Instances are handed out in chunks from a shared counter (instance
+// lengths vary by an order of magnitude: a static partition left cores idle
+// while the thread with the longest instances finished); a chunk is at most
+// 32 instances and at most 1/8 of a thread's share, so that small batches
+// still spread over every thread.
 
 static void *batch_worker(void *arg)
 {
     batch_job *J = (batch_job *)arg;
     int n = J->pb->n, np = J->pb->npar;
     for (;;) {
-        const long lo = __atomic_fetch_add(J->next, (long)kBatchChunk, __ATOMIC_RELAXED);
+        const long lo = __atomic_fetch_add(J->next, J->chunk, __ATOMIC_RELAXED);
         if (lo >= J->hi)
             break;
-        const long hi = lo + kBatchChunk < J->hi ? lo + kBatchChunk : J->hi;
+        const long hi = lo + J->chunk < J->hi ? lo + J->chunk : J->hi;
         for (long b = lo; b < hi; b++) {
         long na = 0, nr = 0;
         int st = orc_gradient(J->pb, J->cost, J->y0 + b * n, J->p + b * np, J->t0[b], J->t1[b],
@@ -889,9 +891,20 @@ int orc_gradient_batch(const orc_problem *pb, int cost, long B, const double *y0
     pthread_t th[256];
     int created[256];
     batch_job jobs[256];
+    if (B < 1)
+        return ORC_OK;
+    if (nthreads > B)
+        nthreads = (int)B; /* no idle threads to create */
+    long chunk = B / (8L * nthreads);
+    chunk = chunk < 1 ? 1 : (chunk > 32 ? 32 : chunk);
     long next = 0;
+    if (nthreads == 1) { /* on the calling thread */
+        batch_job J = {pb, cost, 0, B, &next, chunk, y0, p, t0, t1, yT, dy0, dp, n_acc, n_rej, status};
+        batch_worker(&J);
+        return ORC_OK;
+    }
     for (int k = 0; k < nthreads; k++) {
-        batch_job J = {pb, cost, 0, B, &next, y0, p, t0, t1, yT, dy0, dp, n_acc, n_rej, status};
+        batch_job J = {pb, cost, 0, B, &next, chunk, y0, p, t0, t1, yT, dy0, dp, n_acc, n_rej, status};
         jobs[k] = J;
         created[k] = 0;
     }
