@@ -88,38 +88,41 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
 {
     const int t = threadIdx.x;
     const int k0 = c * kContractKC;
-    // v: column i = t & 127, rows 32 h .. 32 h + 31 (h = t >> 7)
+    // v: column i = t & 127, rows 16 h .. 16 h + 15 (h = t >> 7)
     {
         const int i = t & 127, h = t >> 7;
         const double *col = p.v + (size_t)ti * kContractTileM + i;
         float m = 0.0f;
 #pragma unroll
-        for (int r = 0; r < 32; r++) {
-            const int k = k0 + 32 * h + r;
+        for (int r = 0; r < 16; r++) {
+            const int k = k0 + 16 * h + r;
             if (k < K)
                 m = fmaxf(m, dw_abs_hi(__ldg(col + (size_t)k * kContractN)));
         }
         red[t] = m;
     }
-    // x: column j = t & 63, rows 16 q .. 16 q + 15 (q = t >> 6)
+    // x: column j = t & 63, rows 8 q .. 8 q + 7 (q = t >> 6)
     {
         const int j = t & 63, q = t >> 6;
         float m = 0.0f;
 #pragma unroll
-        for (int r = 0; r < 16; r++) {
-            const int k = k0 + 16 * q + r;
+        for (int r = 0; r < 8; r++) {
+            const int k = k0 + 8 * q + r;
             if (k < K)
-                m = fmaxf(m, dw_abs_hi(__ldg(xrow[16 * q + r] + tj * kContractTileN + j)));
+                m = fmaxf(m, dw_abs_hi(__ldg(xrow[8 * q + r] + tj * kContractTileN + j)));
         }
-        red[256 + t] = m;
+        red[kContractThreads + t] = m;
     }
     __syncthreads();
-    if (t < 128)
-        ev[t] = bound_exponent(fmaxf(red[t], red[t + 128]));
-    else if (t < 192) {
+    if (t < 128) {
+        ev[t] = bound_exponent(fmaxf(fmaxf(red[t], red[t + 128]), fmaxf(red[t + 256], red[t + 384])));
+    } else if (t < 192) {
         const int j = t - 128;
-        ex[j] = bound_exponent(fmaxf(fmaxf(red[256 + j], red[256 + j + 64]),
-                                     fmaxf(red[256 + j + 128], red[256 + j + 192])));
+        float m = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+            m = fmaxf(m, red[kContractThreads + j + 64 * q]);
+        ex[j] = bound_exponent(m);
     }
     __syncthreads();
     // digits: v planes [slice][kgroup 8][row 128][8] (plane = 16 KB, kgroup = 2 KB)
@@ -127,9 +130,9 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
         const int i = t & 127, h = t >> 7;
         const double *col = p.v + (size_t)ti * kContractTileM + i;
         const DigitScale sc = digit_scale(ev[i]);
-#pragma unroll 2
-        for (int g = 0; g < 4; g++) {
-            const int kg = 4 * h + g;
+#pragma unroll
+        for (int g = 0; g < 2; g++) {
+            const int kg = 2 * h + g;
             double vals[8];
 #pragma unroll
             for (int r = 0; r < 8; r++) {
@@ -144,9 +147,8 @@ __device__ __forceinline__ void slice_chunk(const ContractParams &p, int c, int 
         const int j = t & 63, q = t >> 6;
         const DigitScale sc = digit_scale(ex[j]);
         uint8_t *xs = stage + kTileVBytes;
-#pragma unroll 2
-        for (int g = 0; g < 2; g++) {
-            const int kg = 2 * q + g;
+        {
+            const int kg = q;
             double vals[8];
 #pragma unroll
             for (int r = 0; r < 8; r++) {
@@ -166,22 +168,18 @@ __device__ __forceinline__ void prefetch_chunk(const ContractParams &p, int c, i
                                                const double **xrow)
 {
     const int t = threadIdx.x;
-    const int kv = c * kContractKC + (t >> 2);
-    if (kv < K) {
-        const double *row = p.v + (size_t)kv * kContractN + ti * kContractTileM + (t & 3) * 32;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(row));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(row + 16));
-    }
+    // v: 64 rows of 128 doubles, 8 threads a row; x: 64 rows of 64, 4 threads a row
+    const int kv = c * kContractKC + (t >> 3);
+    if (kv < K)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(p.v + (size_t)kv * kContractN + ti * kContractTileM +
+                                                      (t & 7) * 16));
     const int kx = c * kContractKC + (t & 63);
-    if (t < 128) {
+    if (t < 256) {
         const double *base = kx < K ? p.xp[kx] : nullptr;
         if (t < 64)
             xrow[t] = base;
-        if (base) {
-            const double *row = base + tj * kContractTileN + (t >> 6) * 32;
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(row));
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(row + 16));
-        }
+        if (base)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(base + tj * kContractTileN + (t >> 6) * 16));
     }
 }
 
@@ -213,27 +211,28 @@ __device__ __forceinline__ void issue_chunk(uint32_t tmem_acc, const uint8_t *st
 // Folds one chunk's group sums into the double-word accumulators of this
 // thread's row and 32 columns: acc += R_g 2^(e_v + e_x - 8(g + 2)).
 __device__ __forceinline__ void fold_chunk(uint32_t tmem_row, const int *ev, const int *ex, int row, int col0,
-                                           float (&ah)[32], float (&al)[32])
+                                           float (&ah)[kContractFoldCols], float (&al)[kContractFoldCols])
 {
+    constexpr int C = kContractFoldCols;
     // R_g 2^(esum - 8g) = (R_g 2^(-8g)) 2^esum: two exact multiplications by
     // normal powers of two when -102 <= esum <= 103 (|R_g| < 2^24, so every
     // product is a normal float); ldexpf for columns outside that range
-    int esum[32];
-    float p2[32];
+    int esum[C];
+    float p2[C];
     bool fast = true;
 #pragma unroll
-    for (int c = 0; c < 32; c++) {
+    for (int c = 0; c < C; c++) {
         esum[c] = ev[row] + ex[col0 + c] - 16;
         fast = fast && esum[c] >= -102 && esum[c] <= 103;
         p2[c] = pow2f(min(max(esum[c], -102), 103));
     }
 #pragma unroll 1
     for (int g = 0; g < kContractQ; g++) {
-        float R[32];
-        tmem_ld32(tmem_row + g * kContractTileN, R);
+        float R[C];
+        tmem_ld16(tmem_row + g * kContractTileN, R);
         const float sg = pow2f(-8 * g);
 #pragma unroll
-        for (int c = 0; c < 32; c++) {
+        for (int c = 0; c < C; c++) {
             const float v = fast ? (R[c] * sg) * p2[c] : ldexpf(R[c], esum[c] - 8 * g); // exact
             // double-word accumulation: (ah, al) += v
             const float s = ah[c] + v;
@@ -246,15 +245,15 @@ __device__ __forceinline__ void fold_chunk(uint32_t tmem_row, const int *ev, con
     }
 }
 
-// grid = tiles x splits, 256 threads, kContractSmem dynamic shared memory
-__global__ void __launch_bounds__(256, 1) contract_kernel(ContractParams p)
+// grid = tiles x splits, kContractThreads threads, kContractSmem dynamic shared memory
+__global__ void __launch_bounds__(kContractThreads, 1) contract_kernel(ContractParams p)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *stages[2] = {smem, smem + kStageBytes};
     uint64_t *done = reinterpret_cast<uint64_t *>(smem + 2 * kStageBytes); // [2]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 2);
     __shared__ int ev_s[2][kContractTileM], ex_s[2][kContractTileN];
-    __shared__ float red[512];
+    __shared__ float red[2 * kContractThreads];
     __shared__ const double *xrow_s[2][kContractKC]; // x-row pointers of the chunk in each stage
 
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -280,12 +279,12 @@ __global__ void __launch_bounds__(256, 1) contract_kernel(ContractParams p)
     const uint32_t tmem = *tmem_slot;
 
     // this thread's accumulator row and columns: warp w reads tensor-memory
-    // lanes 32 (w % 4) .. +31, columns 32 (w / 4) .. +31 of each group
-    const int row = 32 * (warp & 3) + lane, col0 = 32 * (warp >> 2);
+    // lanes 32 (w % 4) .. +31, columns 16 (w / 4) .. +15 of each group
+    const int row = 32 * (warp & 3) + lane, col0 = kContractFoldCols * (warp >> 2);
     const uint32_t lane_addr = (uint32_t)(32 * (warp & 3)) << 16;
-    float ah[32], al[32];
+    float ah[kContractFoldCols], al[kContractFoldCols];
 #pragma unroll
-    for (int c = 0; c < 32; c++)
+    for (int c = 0; c < kContractFoldCols; c++)
         ah[c] = al[c] = 0.0f;
 
     // ok stays uniform across the block (a bounded wait that gave up on any
@@ -348,7 +347,7 @@ __global__ void __launch_bounds__(256, 1) contract_kernel(ContractParams p)
     // partial[split][j][i] (transposed, as the fixed-order reduction reads it)
     const int i = ti * kContractTileM + row;
 #pragma unroll
-    for (int c = 0; c < 32; c++) {
+    for (int c = 0; c < kContractFoldCols; c++) {
         const int j = tj * kContractTileN + col0 + c;
         p.partials[((size_t)split * kContractN + j) * kContractN + i] = (double)ah[c] + (double)al[c];
     }
@@ -400,7 +399,7 @@ cudaError_t contract_prepare()
 
 cudaError_t enqueue_contract(const ContractParams &p, double *dA, cudaStream_t s)
 {
-    contract_kernel<<<kContractTiles * p.splits, 256, kContractSmem, s>>>(p);
+    contract_kernel<<<kContractTiles * p.splits, kContractThreads, kContractSmem, s>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;

@@ -62,6 +62,8 @@ constexpr int kContractQ = 4;        // digits per factor
 constexpr int kContractTileM = 128;  // rows of v per CTA tile (tcgen05 M)
 constexpr int kContractTileN = 64;   // columns of x per CTA tile (tcgen05 N)
 constexpr int kContractTiles = (kContractN / kContractTileM) * (kContractN / kContractTileN); // 8
+constexpr int kContractThreads = 512;  // 16 warps: 4 lane quadrants x 4 column groups of the fold
+constexpr int kContractFoldCols = kContractTileN / (kContractThreads / 128); // 16 columns per thread
 constexpr size_t kTileVBytes = (size_t)kContractQ * kContractKC * kContractTileM * 2;       // 64 KB
 constexpr size_t kTileXBytes = (size_t)kContractQ * kContractKC * kContractTileN * 2;       // 32 KB
 constexpr size_t kStageBytes = kTileVBytes + kTileXBytes;
