@@ -155,7 +155,14 @@ typedef struct {
                             takes the reference's accepted steps; 0 -- Newton's
                             inverse root (a few ulps off, ~25% cheaper per attempt).
                             The reduced precisions keep their own controllers     */
-    int32_t reserved[3];
+    int32_t tensor_products; /* shared-matrix GLV, N = 256, mixed_dw, every step
+                            checkpointed with stage records, DOPRI5 / CK54: 0
+                            (default) -- the backward sweep's stage products
+                            A^T v run on the tensor cores (clusters of 8 CTAs
+                            carry 64 instances in lockstep; error-free digit
+                            split), where the GPU can schedule such clusters;
+                            -1 -- double-word dot products on the FP32 pipe  */
+    int32_t reserved[2];
 } va_options;
 
 /* Fills the reference's defaults: DOPRI5, FP64, atol=rtol=1e-6, dt0=1e-3,

@@ -1,0 +1,132 @@
+"""The shared-matrix GLV backward with tensor-core stage products
+(csrc/va_bundle_tc.cuh): clusters of 8 CTAs carry 64 instances in lockstep and
+form each stage's A^T v for the whole tile on tcgen05 with an error-free digit
+split.  Against the double-word bundle backward (FP32-pipe dot products, the
+same forward) and against the FP64 path: per instance the gradients agree to
+the double-word level, dA (the same tensor-core contraction over nearly
+identical factor rows) to 1e-8 of its largest entry."""
+import numpy as np
+import pytest
+import torch
+
+from vectorizedadjoint_gb300 import Solver
+from vectorizedadjoint_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+N = 256
+
+
+def dev(a):
+    return torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def make(B, seed):
+    """The GLV-256 recipe (diag -1, off-diagonal N(0, (0.5/sqrt N)^2))."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    A = rng.normal(0.0, 0.5 / np.sqrt(N), (N, N))
+    A[np.arange(N), np.arange(N)] = -1.0
+    r = rng.uniform(0.5, 1.5, (B, N))
+    x0 = rng.uniform(0.1, 1.0, (B, N))
+    return A, r, x0
+
+
+def run(A, r, x0, t1, precision, tensor_products=0, tol=1e-7, cost="sum", **kw):
+    B = r.shape[0]
+    s = Solver("glv_shared", N, N, B, tableau=kw.pop("tableau", "dopri5"), precision=precision, atol=tol,
+               rtol=tol, tensor_products=tensor_products, **kw)
+    dA = torch.empty(N, N, dtype=torch.float64, device="cuda")
+    s.set_shared(dev(A), dA)
+    out = s.gradient(cost, dev(x0), dev(r), dev(np.zeros(B)), dev(t1))
+    torch.cuda.synchronize()
+    res = {k: v.cpu().numpy() for k, v in out.items()}
+    res["dA"] = dA.cpu().numpy()
+    res["launch"] = s.launch()
+    s.close()
+    return res
+
+
+def rel_inst(a, b):
+    """per-instance max |a - b| / max |b| over [dy0, dr]"""
+    ga = np.concatenate([a["dy0"], a["dp"]], axis=1)
+    gb = np.concatenate([b["dy0"], b["dp"]], axis=1)
+    return np.abs(ga - gb).max(axis=1) / np.abs(gb).max(axis=1)
+
+
+@pytest.mark.parametrize("tableau", ["dopri5", "ck54"])
+@pytest.mark.parametrize("B", [1, 100])
+def test_tc_backward_vs_fp32_pipe_and_fp64(cuda, B, tableau):
+    """Ragged tiles (1 and 100 instances: one partly filled cluster, then
+    one full and one partly filled), both 5(4) pairs."""
+    A, r, x0 = make(B, seed=31 + B)
+    t1 = np.full(B, 10.0)
+    tc = run(A, r, x0, t1, "mixed_dw", 0, tableau=tableau)
+    pipe = run(A, r, x0, t1, "mixed_dw", -1, tableau=tableau)
+    f64 = run(A, r, x0, t1, "fp64", tableau=tableau)
+    assert tc["launch"]["bwd_block"] == 512, tc["launch"]  # the cluster kernel ran
+    assert pipe["launch"]["bwd_block"] == N
+    assert (tc["status"] == 0).all() and (pipe["status"] == 0).all()
+    # same forward sweep
+    np.testing.assert_array_equal(tc["n_acc"], pipe["n_acc"])
+    np.testing.assert_array_equal(tc["yT"], pipe["yT"])
+    assert rel_inst(tc, pipe).max() <= 1e-11, rel_inst(tc, pipe).max()
+    assert rel_inst(tc, f64).max() <= 1e-11, rel_inst(tc, f64).max()
+    scale = np.abs(f64["dA"]).max()
+    assert np.isfinite(tc["dA"]).all()
+    assert np.abs(tc["dA"] - pipe["dA"]).max() <= 1e-8 * scale
+    assert np.abs(tc["dA"] - f64["dA"]).max() <= 1e-8 * scale
+
+
+def test_tc_backward_uneven_lengths_and_failed_instance(cuda):
+    """Instances of very different lengths share a tile (the lockstep runs
+    the longest; finished instances contribute zero columns), and one
+    instance whose forward fails (a NaN initial state) reports the forward's
+    status with NaN gradients while the others match the FP32-pipe backward."""
+    B = 70
+    A, r, x0 = make(B, seed=7)
+    x0[5] = np.nan
+    t1 = np.linspace(0.2, 12.0, B)
+    tc = run(A, r, x0, t1, "mixed_dw", 0)
+    pipe = run(A, r, x0, t1, "mixed_dw", -1)
+    assert tc["launch"]["bwd_block"] == 512
+    np.testing.assert_array_equal(tc["status"], pipe["status"])
+    assert tc["status"][5] != 0 and (np.delete(tc["status"], 5) == 0).all(), tc["status"]
+    assert np.isnan(tc["dy0"][5]).all() and np.isnan(tc["dp"][5]).all()
+    ok = np.arange(B) != 5
+    assert rel_inst({k: tc[k][ok] for k in ("dy0", "dp")}, {k: pipe[k][ok] for k in ("dy0", "dp")}).max() <= 1e-11
+    n = tc["n_acc"][ok]
+    assert n.max() >= 3 * n.min(), (n.min(), n.max())  # the tile really is uneven
+
+
+def test_tc_backward_sumsq_cost_and_workload(cuda):
+    """The benchmark recipe (glv256) with the sum-of-squares cost, 130
+    instances (three clusters), against FP64."""
+    B = 130
+    w = W.make("glv256", batch=B)
+    t1 = np.full(B, 10.0)
+    tc = run(w["shared"], w["params"], w["y0"], t1, "mixed_dw", 0, cost="sumsq")
+    f64 = run(w["shared"], w["params"], w["y0"], t1, "fp64", cost="sumsq")
+    assert tc["launch"]["bwd_block"] == 512
+    assert (tc["status"] == 0).all()
+    assert rel_inst(tc, f64).max() <= 1e-11, rel_inst(tc, f64).max()
+    scale = np.abs(f64["dA"]).max()
+    assert np.abs(tc["dA"] - f64["dA"]).max() <= 1e-8 * scale
+
+
+def test_tc_backward_repeatable(cuda):
+    """Two gradients of one handle (the second replays the captured graph)
+    give the same bits."""
+    B = 64
+    A, r, x0 = make(B, seed=3)
+    s = Solver("glv_shared", N, N, B, precision="mixed_dw", atol=1e-7, rtol=1e-7)
+    dA = torch.empty(N, N, dtype=torch.float64, device="cuda")
+    s.set_shared(dev(A), dA)
+    outs = []
+    for _ in range(2):
+        o = s.gradient("sum", dev(x0), dev(r), dev(np.zeros(B)), dev(np.full(B, 10.0)))
+        torch.cuda.synchronize()
+        outs.append({k: v.cpu().numpy().copy() for k, v in o.items()} | {"dA": dA.cpu().numpy().copy()})
+    assert s.launch()["bwd_block"] == 512
+    s.close()
+    for k in ("dy0", "dp", "dA"):
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])

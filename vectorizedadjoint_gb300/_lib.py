@@ -43,7 +43,7 @@ class VaOptions(ctypes.Structure):
                 ("block_size", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
                 ("chunk_len", ctypes.c_int32), ("schedule", ctypes.c_int32),
                 ("stage_records", ctypes.c_int32), ("step_pow", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 3)]
+                ("tensor_products", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
 
 class VaError(RuntimeError):

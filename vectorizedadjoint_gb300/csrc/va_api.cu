@@ -19,6 +19,7 @@
 #include "va_bundle.cuh"
 #include "va_contract.cuh"
 #include "va_bundle_2level.cuh"
+#include "va_bundle_tc.cuh"
 #include "va_group_2level.cuh"
 #include "va_kernels.cuh"
 #include "va_order.h"
@@ -114,6 +115,11 @@ struct va_handle {
     double *c_part = nullptr;
     unsigned *c_err = nullptr;
     int64_t fac_rows = 0;
+    // tensor-core cluster backward (va_bundle_tc.cuh): digit planes of A^T
+    // and their exponents (null: the bundle backward)
+    uint8_t *bt_adig = nullptr;
+    int *bt_aexp = nullptr;
+    double *bt_rpk = nullptr; // r as packed double-words
 
     bool buffers_ready = false; // ensure_buffers / ensure_staging completed
     bool staging_ready = false;
@@ -206,6 +212,11 @@ bool deferred_possible(const va_handle *h)
            h->bks->rs_stage[h->opt.tableau] > 0 && h->opt.stage_records != 0;
 }
 bool deferred_now(const va_handle *h) { return deferred_possible(h) && stages_now(h) && h->fac_v && h->shared_dA; }
+// the tensor-core cluster backward (with the deferred dA)
+bool tc_backward_now(const va_handle *h)
+{
+    return deferred_now(h) && h->bt_adig && h->opt.tensor_products == 0 && va::bundle_tc_available(h->opt.tableau);
+}
 
 // whether the other bundle width is compiled for the handle's tableau and precision
 bool bundle_alt_available(const va_handle *h)
@@ -341,6 +352,11 @@ va_status alloc_buffers(va_handle *h)
             VA_CUDA(h, cudaMalloc(&h->c_part, (size_t)va::contract_splits(h->sm_count) * NN * sizeof(double)));
             VA_CUDA(h, cudaMalloc(&h->c_err, sizeof(unsigned)));
             VA_CUDA(h, va::contract_prepare());
+            if (h->opt.tensor_products == 0 && va::bundle_tc_available(h->opt.tableau)) {
+                VA_CUDA(h, cudaMalloc(&h->bt_adig, va::kBtADigitBytes));
+                VA_CUDA(h, cudaMalloc(&h->bt_aexp, va::kBtAExpInts * sizeof(int)));
+                VA_CUDA(h, cudaMalloc(&h->bt_rpk, (size_t)B * h->N * sizeof(double)));
+            }
         }
         for (int t = 0; t < va::kTableaux; t++)
             for (int p = 0; p < 3; p++) {
@@ -372,7 +388,8 @@ va_status ensure_buffers(va_handle *h)
                  (void **)&h->inst_status, (void **)&h->ctl, (void **)&h->inst_t1, (void **)&h->inst_t0,
                  (void **)&h->order_fwd, (void **)&h->order_bwd, (void **)&h->order_work, (void **)&h->inst_work,
                  (void **)&h->At, (void **)&h->Aw, (void **)&h->Atw, (void **)&h->dA_part, (void **)&h->fac_v,
-                 (void **)&h->fac_xp, (void **)&h->k_base, (void **)&h->c_part, (void **)&h->c_err});
+                 (void **)&h->fac_xp, (void **)&h->k_base, (void **)&h->c_part, (void **)&h->c_err,
+                 (void **)&h->bt_adig, (void **)&h->bt_aexp, (void **)&h->bt_rpk});
         h->pool_bytes = 0;
         h->fac_rows = 0;
         return st;
@@ -641,7 +658,20 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
             bp.fac_xp = h->fac_xp;
             bp.k_base = h->k_base;
         }
-        VA_CUDA(h, cudaLaunchKernel(bundle_bwd(h), dim3(grid), dim3(h->N), args, bundle_smem_bwd(h), s));
+        const bool tcb = tc_backward_now(h);
+        if (defer)
+            VA_CUDA(h, cudaMemsetAsync(h->c_err, 0, sizeof(unsigned), s));
+        if (tcb) {
+            // clusters of 8 CTAs, 64 instances each, stage products on the tensor cores
+            VA_CUDA(h, va::enqueue_bundle_tc_backward(bp, h->shared_A, h->bt_adig, h->bt_aexp, h->bt_rpk, h->c_err,
+                                                      h->opt.tableau, s));
+            h->bwd_grid = (a.B + va::kBtTile - 1) / va::kBtTile * va::kBtCluster;
+            h->bwd_block = va::kBtThreads;
+        } else {
+            VA_CUDA(h, cudaLaunchKernel(bundle_bwd(h), dim3(grid), dim3(h->N), args, bundle_smem_bwd(h), s));
+            h->bwd_grid = grid;
+            h->bwd_block = h->N;
+        }
         if (defer) {
             va::ContractParams cp{};
             cp.v = h->fac_v;
@@ -650,7 +680,6 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
             cp.partials = h->c_part;
             cp.splits = va::contract_splits(h->sm_count);
             cp.error = h->c_err;
-            VA_CUDA(h, cudaMemsetAsync(h->c_err, 0, sizeof(unsigned), s));
             VA_CUDA(h, va::enqueue_contract(cp, h->shared_dA, s));
         } else if (h->shared_dA) {
             const int NN = h->N * h->N;
@@ -658,8 +687,6 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
             void *rargs[] = {(void *)&h->dA_part, (void *)&grid, (void *)&dw, (void *)&h->shared_dA};
             VA_CUDA(h, cudaLaunchKernel(h->bks->reduce, dim3((NN + 255) / 256), dim3(256), rargs, 0, s));
         }
-        h->bwd_grid = grid;
-        h->bwd_block = h->N;
         return VA_OK;
     }
     a.hist = h->hist;
@@ -1130,7 +1157,7 @@ va_status va_destroy(va_handle *h)
                     h->s_nrej,   h->s_lam,      h->s_mu,    h->At,        h->Aw,
                     h->Atw,      h->dA_part,    h->inst_t1, h->scratch, h->order_fwd,
                     h->order_bwd, h->order_work, h->inst_work, h->inst_t0, h->hist, h->fac_v,
-                    h->fac_xp,    h->k_base,    h->c_part,  h->c_err};
+                    h->fac_xp,    h->k_base,    h->c_part,  h->c_err,     h->bt_adig, h->bt_aexp, h->bt_rpk};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);

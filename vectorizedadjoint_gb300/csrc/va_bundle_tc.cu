@@ -1,0 +1,117 @@
+// Cluster backward sweep of the shared-matrix GLV with tensor-core stage
+// products (va_bundle_tc.cuh): digit planes of A^T, instantiations for the
+// 5(4) pairs, and the launch.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "va_bundle_tc.cuh"
+
+namespace va {
+
+__global__ void __launch_bounds__(256) bt_digits_A_kernel(const double *A, uint8_t *adig, int *aexp)
+{
+    __shared__ float red[8];
+    const int i = blockIdx.x, k = threadIdx.x;
+    const dword v(A[(size_t)k * kBtN + i]); // A^T[i][k]
+    int e[kTcQuarters];
+    tc_quarter_exponents(fabsf(v.hi), red, e);
+    const int q = k / 64, mt = i / 128, row = i % 128;
+    float d[kBtQA];
+    split_digits<kBtQA>(v.hi, v.lo, digit_scale(e[q]), d);
+    uint8_t *blk = adig + (size_t)(mt * 4 + q) * kBtABytes + (size_t)((k % 64) / 8) * (128 * 16) + (size_t)row * 16 +
+                   (size_t)(k % 8) * 2;
+#pragma unroll
+    for (int s = 0; s < kBtQA; s++)
+        *reinterpret_cast<uint16_t *>(blk + (size_t)s * kBtAPlane) = bf16_bits(d[s]);
+    if (k < kTcQuarters)
+        aexp[k * kBtN + i] = e[k];
+}
+
+__global__ void __launch_bounds__(256) bt_pack_r_kernel(const double *par, double *rpk)
+{
+    const size_t x = (size_t)blockIdx.x * kBtN + threadIdx.x;
+    rpk[x] = dw_pack(dword(par[x]));
+}
+
+namespace {
+
+const void *bt_kernel(int tableau)
+{
+    switch (tableau) {
+    case 0:
+        return (const void *)backward_bundle_tc_kernel<TabDopri5>;
+    case 1:
+        return (const void *)backward_bundle_tc_kernel<TabCK54>;
+    default:
+        return nullptr;
+    }
+}
+
+// per device: the kernels' shared-memory attribute is set and a cluster of 8
+// CTAs of kBtSmem bytes fits on this GPU
+struct BtState {
+    std::once_flag once;
+    bool ok = false;
+};
+BtState g_bt[64];
+
+void bt_setup(int dev)
+{
+    bool ok = true;
+    for (int tb = 0; tb < 2 && ok; tb++) {
+        const void *fn = bt_kernel(tb);
+        ok = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBtSmem) == cudaSuccess;
+        if (ok) {
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim = dim3(kBtCluster);
+            cfg.blockDim = dim3(kBtThreads);
+            cfg.dynamicSmemBytes = kBtSmem;
+            cudaLaunchAttribute attr{};
+            attr.id = cudaLaunchAttributeClusterDimension;
+            attr.val.clusterDim.x = kBtCluster;
+            attr.val.clusterDim.y = 1;
+            attr.val.clusterDim.z = 1;
+            cfg.attrs = &attr;
+            cfg.numAttrs = 1;
+            int clusters = 0;
+            ok = cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) == cudaSuccess && clusters > 0;
+        }
+    }
+    (void)cudaGetLastError(); // a refused attribute or query leaves no sticky error
+    g_bt[dev].ok = ok;
+}
+
+} // namespace
+
+bool bundle_tc_available(int tableau)
+{
+    if (!bt_kernel(tableau))
+        return false;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return false;
+    std::call_once(g_bt[dev].once, bt_setup, dev);
+    return g_bt[dev].ok;
+}
+
+cudaError_t enqueue_bundle_tc_backward(const BundleParams &bp, const double *A, uint8_t *adig, int *aexp,
+                                       double *rpk, unsigned *error, int tableau, cudaStream_t s)
+{
+    const void *fn = bt_kernel(tableau);
+    if (!fn)
+        return cudaErrorInvalidValue;
+    bt_digits_A_kernel<<<kBtN, 256, 0, s>>>(A, adig, aexp);
+    bt_pack_r_kernel<<<bp.g.B, 256, 0, s>>>(bp.g.par, rpk);
+    BundleTcParams p{};
+    p.bp = bp;
+    p.adig = adig;
+    p.rpk = rpk;
+    p.aexp = aexp;
+    p.error = error;
+    const int tiles = (bp.g.B + kBtTile - 1) / kBtTile;
+    void *args[] = {&p};
+    return cudaLaunchKernel(fn, dim3(tiles * kBtCluster), dim3(kBtThreads), args, kBtSmem, s);
+}
+
+} // namespace va

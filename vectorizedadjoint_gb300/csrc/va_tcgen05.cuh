@@ -59,7 +59,7 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint
 // instruction descriptor of tcgen05.mma kind::f16: FP32 accumulator (bits 4-5
 // = 1), bf16 A and B (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17,
 // M >> 4 at bit 24
-constexpr uint32_t umma_idesc_bf16(int M, int N)
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
@@ -72,6 +72,22 @@ __device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint6
                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
                  "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
                  : "memory");
+}
+
+// the same MMA with the accumulate flag known at compile time
+template <bool ACC>
+__device__ __forceinline__ void umma_bf16_k(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc)
+{
+    if constexpr (ACC)
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.eq.u32 p, 1, 1;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                     "l"(adesc), "l"(bdesc), "r"(idesc)
+                     : "memory");
+    else
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, 1, 1;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                     "l"(adesc), "l"(bdesc), "r"(idesc)
+                     : "memory");
 }
 
 __device__ __forceinline__ void umma_commit(uint64_t *bar)
@@ -119,6 +135,48 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 #pragma unroll
     for (int c = 0; c < 16; c++)
         v[c] = __uint_as_float(r[c]);
+}
+
+// 8 consecutive FP32 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
+{
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+        v[c] = __uint_as_float(r[c]);
+}
+
+// Groups of 8 FP32 columns at tensor-memory columns taddr + 64 g for NG
+// groups, loaded back to back and waited for once (the wait names the
+// registers, so no use moves above it)
+template <int NG>
+__device__ __forceinline__ void tmem_ld8_groups(uint32_t taddr, int g0, float (&v)[NG][8])
+{
+    uint32_t r[NG][8];
+#pragma unroll
+    for (int g = 0; g < NG; g++)
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                     : "=r"(r[g][0]), "=r"(r[g][1]), "=r"(r[g][2]), "=r"(r[g][3]), "=r"(r[g][4]), "=r"(r[g][5]),
+                       "=r"(r[g][6]), "=r"(r[g][7])
+                     : "r"(taddr + (uint32_t)(64 * (g0 + g)))
+                     : "memory");
+#pragma unroll
+    for (int g = 0; g < NG; g++)
+        asm volatile("tcgen05.wait::ld.sync.aligned;"
+                     : "+r"(r[g][0]), "+r"(r[g][1]), "+r"(r[g][2]), "+r"(r[g][3]), "+r"(r[g][4]), "+r"(r[g][5]),
+                       "+r"(r[g][6]), "+r"(r[g][7])
+                     :
+                     : "memory");
+#pragma unroll
+    for (int g = 0; g < NG; g++)
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+            v[g][c] = __uint_as_float(r[g][c]);
 }
 
 } // namespace va

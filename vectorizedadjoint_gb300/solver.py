@@ -36,12 +36,15 @@ class Solver:
                 values for the backward sweep, 0 recomputes them (va_options)
     step_pow  : FP64 controller: 1 (default) the correctly rounded step factor
                 (odeint's std::pow), 0 the Newton root (va_options)
+    tensor_products : shared-matrix GLV N = 256, mixed_dw: 0 (default) the
+                backward's stage products on the tensor cores, -1 on the FP32
+                pipe (va_options)
     """
 
     def __init__(self, model, n, npar, batch, nout=1, tableau="dopri5", precision="fp64",
                  atol=1e-6, rtol=1e-6, dt0=1e-3, max_steps=1000000, max_rejects=500,
                  ckpt_budget_bytes=0, ckpt_stride=0, block_size=0, blocks_per_sm=0, chunk_len=0,
-                 stage_records=1, step_pow=1, model_kernels=None):
+                 stage_records=1, step_pow=1, model_kernels=None, tensor_products=0):
         self.L = _lib.load()
         if not torch.cuda.is_available():
             raise RuntimeError("vectorizedadjoint_gb300 needs a CUDA device (no CPU fallback)")
@@ -58,6 +61,7 @@ class Solver:
         opt.block_size, opt.blocks_per_sm, opt.chunk_len = block_size, blocks_per_sm, chunk_len
         opt.stage_records = stage_records
         opt.step_pow = step_pow
+        opt.tensor_products = tensor_products
         torch.cuda.init()
         self.h = ctypes.c_void_p()
         if model_kernels is not None:
