@@ -1,10 +1,11 @@
-"""The shared-matrix GLV backward with tensor-core stage products
+"""The shared-matrix GLV sweeps with tensor-core stage products
 (csrc/va_bundle_tc.cuh): clusters of 8 CTAs carry 64 instances in lockstep and
-form each stage's A^T v for the whole tile on tcgen05 with an error-free digit
-split.  Against the double-word bundle backward (FP32-pipe dot products, the
-same forward) and against the FP64 path: per instance the gradients agree to
-the double-word level, dA (the same tensor-core contraction over nearly
-identical factor rows) to 1e-8 of its largest entry."""
+form each stage's A X (forward, DOPRI5) and A^T v (backward, the 5(4) pairs)
+for the whole tile on tcgen05 with an error-free digit split.  Against the
+double-word bundle sweeps (FP32-pipe dot products) and against the FP64
+path: the same accepted steps, y(T) and per-instance gradients at the
+double-word level, dA (the tensor-core contraction over nearly identical
+factor rows) to 1e-8 of its largest entry."""
 import numpy as np
 import pytest
 import torch
@@ -53,28 +54,68 @@ def rel_inst(a, b):
     return np.abs(ga - gb).max(axis=1) / np.abs(gb).max(axis=1)
 
 
+def rel_y(a, b):
+    """per-instance max |a - b| / max |b| of y(T)"""
+    return np.abs(a["yT"] - b["yT"]).max(axis=1) / np.abs(b["yT"]).max(axis=1)
+
+
 @pytest.mark.parametrize("tableau", ["dopri5", "ck54"])
 @pytest.mark.parametrize("B", [1, 100])
-def test_tc_backward_vs_fp32_pipe_and_fp64(cuda, B, tableau):
+def test_tc_sweeps_vs_fp32_pipe_and_fp64(cuda, B, tableau):
     """Ragged tiles (1 and 100 instances: one partly filled cluster, then
-    one full and one partly filled), both 5(4) pairs."""
+    one full and one partly filled), both 5(4) pairs (CK54, not FSAL, keeps
+    the bundle forward)."""
     A, r, x0 = make(B, seed=31 + B)
     t1 = np.full(B, 10.0)
     tc = run(A, r, x0, t1, "mixed_dw", 0, tableau=tableau)
     pipe = run(A, r, x0, t1, "mixed_dw", -1, tableau=tableau)
     f64 = run(A, r, x0, t1, "fp64", tableau=tableau)
-    assert tc["launch"]["bwd_block"] == 512, tc["launch"]  # the cluster kernel ran
-    assert pipe["launch"]["bwd_block"] == N
+    assert tc["launch"]["bwd_block"] == 512, tc["launch"]  # the cluster kernels ran
+    assert tc["launch"]["fwd_block"] == (512 if tableau == "dopri5" else N), tc["launch"]
+    assert pipe["launch"]["bwd_block"] == N and pipe["launch"]["fwd_block"] == N
     assert (tc["status"] == 0).all() and (pipe["status"] == 0).all()
-    # same forward sweep
-    np.testing.assert_array_equal(tc["n_acc"], pipe["n_acc"])
-    np.testing.assert_array_equal(tc["yT"], pipe["yT"])
+    # the accepted steps of the FP64 sweep, y(T) to the double-word level
+    np.testing.assert_array_equal(tc["n_acc"], f64["n_acc"])
+    np.testing.assert_array_equal(pipe["n_acc"], f64["n_acc"])
+    assert rel_y(tc, f64).max() <= 1e-12, rel_y(tc, f64).max()
     assert rel_inst(tc, pipe).max() <= 1e-11, rel_inst(tc, pipe).max()
     assert rel_inst(tc, f64).max() <= 1e-11, rel_inst(tc, f64).max()
     scale = np.abs(f64["dA"]).max()
     assert np.isfinite(tc["dA"]).all()
     assert np.abs(tc["dA"] - pipe["dA"]).max() <= 1e-8 * scale
     assert np.abs(tc["dA"] - f64["dA"]).max() <= 1e-8 * scale
+
+
+def test_tc_forward_trajectory(cuda):
+    """The cluster forward's checkpoint records decode to the FP64 sweep's
+    steps: the same step count, t_n and y_n as close to FP64 as the
+    FP32-pipe double-word forward's (the double-word controller's dt
+    differs from FP64's at ~1e-9, so mid-trajectory states do too)."""
+    B = 70
+    A, r, x0 = make(B, seed=5)
+    t1 = np.full(B, 10.0)
+    out = {}
+    for prec, tp in (("fp64", 0), ("mixed_dw", 0), ("mixed_dw", -1)):
+        s = Solver("glv_shared", N, N, B, precision=prec, atol=1e-7, rtol=1e-7, tensor_products=tp)
+        dA = torch.empty(N, N, dtype=torch.float64, device="cuda")
+        s.set_shared(dev(A), dA)
+        s.gradient("sum", dev(x0), dev(r), dev(np.zeros(B)), dev(t1))
+        torch.cuda.synchronize()
+        out[(prec, tp)] = [s.trajectory(b) for b in (0, 33, 69)]
+        if prec == "mixed_dw":
+            assert s.launch()["fwd_block"] == (512 if tp == 0 else N)
+        s.close()
+    dev_t = {"tc": 0.0, "pipe": 0.0}
+    dev_y = {"tc": 0.0, "pipe": 0.0}
+    for k, key in (("tc", ("mixed_dw", 0)), ("pipe", ("mixed_dw", -1))):
+        for (t64, _, y64), (tdw, _, ydw) in zip(out[("fp64", 0)], out[key]):
+            assert len(t64) == len(tdw)
+            np.testing.assert_allclose(tdw, t64, rtol=1e-7, atol=0)
+            np.testing.assert_allclose(ydw, y64, rtol=1e-7, atol=1e-10)
+            dev_t[k] = max(dev_t[k], float(np.abs(tdw - t64).max()))
+            dev_y[k] = max(dev_y[k], float(np.abs(ydw - y64).max()))
+    assert dev_t["tc"] <= 10 * dev_t["pipe"] + 1e-13, dev_t
+    assert dev_y["tc"] <= 10 * dev_y["pipe"] + 1e-13, dev_y
 
 
 def test_tc_backward_uneven_lengths_and_failed_instance(cuda):

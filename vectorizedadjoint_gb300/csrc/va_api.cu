@@ -120,6 +120,9 @@ struct va_handle {
     uint8_t *bt_adig = nullptr;
     int *bt_aexp = nullptr;
     double *bt_rpk = nullptr; // r as packed double-words
+    uint8_t *bt_adig_f = nullptr; // the forward's digit planes of A (null: the bundle forward)
+    int *bt_aexp_f = nullptr;
+    unsigned *bt_ferr = nullptr;
 
     bool buffers_ready = false; // ensure_buffers / ensure_staging completed
     bool staging_ready = false;
@@ -216,6 +219,12 @@ bool deferred_now(const va_handle *h) { return deferred_possible(h) && stages_no
 bool tc_backward_now(const va_handle *h)
 {
     return deferred_now(h) && h->bt_adig && h->opt.tensor_products == 0 && va::bundle_tc_available(h->opt.tableau);
+}
+// the tensor-core cluster forward (stage records, every step checkpointed)
+bool tc_forward_now(const va_handle *h)
+{
+    return deferred_possible(h) && stages_now(h) && h->bt_adig_f && h->opt.tensor_products == 0 &&
+           va::bundle_tc_forward_available(h->opt.tableau);
 }
 
 // whether the other bundle width is compiled for the handle's tableau and precision
@@ -356,6 +365,11 @@ va_status alloc_buffers(va_handle *h)
                 VA_CUDA(h, cudaMalloc(&h->bt_adig, va::kBtADigitBytes));
                 VA_CUDA(h, cudaMalloc(&h->bt_aexp, va::kBtAExpInts * sizeof(int)));
                 VA_CUDA(h, cudaMalloc(&h->bt_rpk, (size_t)B * h->N * sizeof(double)));
+                if (va::bundle_tc_forward_available(h->opt.tableau)) {
+                    VA_CUDA(h, cudaMalloc(&h->bt_adig_f, va::kBtADigitBytes));
+                    VA_CUDA(h, cudaMalloc(&h->bt_aexp_f, va::kBtAExpInts * sizeof(int)));
+                    VA_CUDA(h, cudaMalloc(&h->bt_ferr, sizeof(unsigned)));
+                }
             }
         }
         for (int t = 0; t < va::kTableaux; t++)
@@ -389,7 +403,8 @@ va_status ensure_buffers(va_handle *h)
                  (void **)&h->order_fwd, (void **)&h->order_bwd, (void **)&h->order_work, (void **)&h->inst_work,
                  (void **)&h->At, (void **)&h->Aw, (void **)&h->Atw, (void **)&h->dA_part, (void **)&h->fac_v,
                  (void **)&h->fac_xp, (void **)&h->k_base, (void **)&h->c_part, (void **)&h->c_err,
-                 (void **)&h->bt_adig, (void **)&h->bt_aexp, (void **)&h->bt_rpk});
+                 (void **)&h->bt_adig, (void **)&h->bt_aexp, (void **)&h->bt_rpk, (void **)&h->bt_adig_f,
+                 (void **)&h->bt_aexp_f, (void **)&h->bt_ferr});
         h->pool_bytes = 0;
         h->fac_rows = 0;
         return st;
@@ -559,6 +574,15 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
         VA_CUDA(h, cudaLaunchKernel(h->bks->prepare, dim3((NN + 255) / 256), dim3(256), pargs, 0, s));
         va::BundleParams bp = bundle_params(h);
         bp.f = a;
+        if (tc_forward_now(h)) {
+            // clusters of 8 CTAs, 64 instances each, stage products on the tensor cores
+            VA_CUDA(h, cudaMemsetAsync(h->bt_ferr, 0, sizeof(unsigned), s));
+            VA_CUDA(h, va::enqueue_bundle_tc_forward(bp, h->shared_A, h->bt_adig_f, h->bt_aexp_f, h->bt_rpk, h->bt_ferr,
+                                                     h->opt.tableau, s));
+            h->fwd_grid = (a.B + va::kBtTile - 1) / va::kBtTile * va::kBtCluster;
+            h->fwd_block = va::kBtThreads;
+            return VA_OK;
+        }
         void *args[] = {&bp};
         VA_CUDA(h, cudaLaunchKernel(bundle_fwd(h), dim3(bundle_grid(h)), dim3(h->N), args, bundle_smem_fwd(h), s));
         h->fwd_grid = bundle_grid(h);
@@ -1157,7 +1181,7 @@ va_status va_destroy(va_handle *h)
                     h->s_nrej,   h->s_lam,      h->s_mu,    h->At,        h->Aw,
                     h->Atw,      h->dA_part,    h->inst_t1, h->scratch, h->order_fwd,
                     h->order_bwd, h->order_work, h->inst_work, h->inst_t0, h->hist, h->fac_v,
-                    h->fac_xp,    h->k_base,    h->c_part,  h->c_err,     h->bt_adig, h->bt_aexp, h->bt_rpk};
+                    h->fac_xp,    h->k_base,    h->c_part,  h->c_err,     h->bt_adig, h->bt_aexp, h->bt_rpk, h->bt_adig_f, h->bt_aexp_f, h->bt_ferr};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);

@@ -9,11 +9,13 @@
 
 namespace va {
 
-__global__ void __launch_bounds__(256) bt_digits_A_kernel(const double *A, uint8_t *adig, int *aexp)
+// digit planes of a matrix M (element (row i, k) = M[i][k]): per row and
+// quarter of k an exponent, 6 digits per entry, in the operand blocks [row
+// tile][quarter] of the cluster sweeps
+__device__ __forceinline__ void bt_digits_row(double m_ik, int i, int k, uint8_t *adig, int *aexp)
 {
     __shared__ float red[8];
-    const int i = blockIdx.x, k = threadIdx.x;
-    const dword v(A[(size_t)k * kBtN + i]); // A^T[i][k]
+    const dword v(m_ik);
     int e[kTcQuarters];
     tc_quarter_exponents(fabsf(v.hi), red, e);
     const int q = k / 64, mt = i / 128, row = i % 128;
@@ -26,6 +28,18 @@ __global__ void __launch_bounds__(256) bt_digits_A_kernel(const double *A, uint8
         *reinterpret_cast<uint16_t *>(blk + (size_t)s * kBtAPlane) = bf16_bits(d[s]);
     if (k < kTcQuarters)
         aexp[k * kBtN + i] = e[k];
+}
+
+__global__ void __launch_bounds__(256) bt_digits_A_kernel(const double *A, uint8_t *adig, int *aexp)
+{
+    const int i = blockIdx.x, k = threadIdx.x;
+    bt_digits_row(A[(size_t)k * kBtN + i], i, k, adig, aexp); // A^T[i][k]
+}
+
+__global__ void __launch_bounds__(256) bt_digits_Af_kernel(const double *A, uint8_t *adig, int *aexp)
+{
+    const int i = blockIdx.x, k = threadIdx.x;
+    bt_digits_row(A[(size_t)i * kBtN + k], i, k, adig, aexp); // A[i][k]
 }
 
 __global__ void __launch_bounds__(256) bt_pack_r_kernel(const double *par, double *rpk)
@@ -48,6 +62,9 @@ const void *bt_kernel(int tableau)
     }
 }
 
+// the forward needs the FSAL pair (DOPRI5)
+const void *bt_fwd_kernel(int tableau) { return tableau == 0 ? (const void *)forward_bundle_tc_kernel<TabDopri5> : nullptr; }
+
 // per device: the kernels' shared-memory attribute is set and a cluster of 8
 // CTAs of kBtSmem bytes fits on this GPU
 struct BtState {
@@ -56,43 +73,66 @@ struct BtState {
 };
 BtState g_bt[64];
 
+bool bt_cluster_fits(const void *fn)
+{
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBtSmem) != cudaSuccess)
+        return false;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(kBtCluster);
+    cfg.blockDim = dim3(kBtThreads);
+    cfg.dynamicSmemBytes = kBtSmem;
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = kBtCluster;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    return cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) == cudaSuccess && clusters > 0;
+}
+
 void bt_setup(int dev)
 {
     bool ok = true;
-    for (int tb = 0; tb < 2 && ok; tb++) {
-        const void *fn = bt_kernel(tb);
-        ok = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBtSmem) == cudaSuccess;
-        if (ok) {
-            cudaLaunchConfig_t cfg{};
-            cfg.gridDim = dim3(kBtCluster);
-            cfg.blockDim = dim3(kBtThreads);
-            cfg.dynamicSmemBytes = kBtSmem;
-            cudaLaunchAttribute attr{};
-            attr.id = cudaLaunchAttributeClusterDimension;
-            attr.val.clusterDim.x = kBtCluster;
-            attr.val.clusterDim.y = 1;
-            attr.val.clusterDim.z = 1;
-            cfg.attrs = &attr;
-            cfg.numAttrs = 1;
-            int clusters = 0;
-            ok = cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) == cudaSuccess && clusters > 0;
-        }
-    }
+    for (int tb = 0; tb < 2 && ok; tb++)
+        ok = bt_cluster_fits(bt_kernel(tb));
+    ok = ok && bt_cluster_fits(bt_fwd_kernel(0));
     (void)cudaGetLastError(); // a refused attribute or query leaves no sticky error
     g_bt[dev].ok = ok;
 }
 
-} // namespace
-
-bool bundle_tc_available(int tableau)
+bool bt_ready()
 {
-    if (!bt_kernel(tableau))
-        return false;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
         return false;
     std::call_once(g_bt[dev].once, bt_setup, dev);
     return g_bt[dev].ok;
+}
+
+} // namespace
+
+bool bundle_tc_available(int tableau) { return bt_kernel(tableau) && bt_ready(); }
+bool bundle_tc_forward_available(int tableau) { return bt_fwd_kernel(tableau) && bt_ready(); }
+
+cudaError_t enqueue_bundle_tc_forward(const BundleParams &bp, const double *A, uint8_t *adig, int *aexp,
+                                      double *rpk, unsigned *error, int tableau, cudaStream_t s)
+{
+    const void *fn = bt_fwd_kernel(tableau);
+    if (!fn)
+        return cudaErrorInvalidValue;
+    bt_digits_Af_kernel<<<kBtN, 256, 0, s>>>(A, adig, aexp);
+    bt_pack_r_kernel<<<bp.f.B, 256, 0, s>>>(bp.f.par, rpk);
+    BundleTcParams p{};
+    p.bp = bp;
+    p.adig = adig;
+    p.rpk = rpk;
+    p.aexp = aexp;
+    p.error = error;
+    const int tiles = (bp.f.B + kBtTile - 1) / kBtTile;
+    void *args[] = {&p};
+    return cudaLaunchKernel(fn, dim3(tiles * kBtCluster), dim3(kBtThreads), args, kBtSmem, s);
 }
 
 cudaError_t enqueue_bundle_tc_backward(const BundleParams &bp, const double *A, uint8_t *adig, int *aexp,

@@ -74,7 +74,8 @@ constexpr size_t kBtVPlane = 8 * kBtVKgroup;         // 8,320 bytes
 constexpr size_t kBtVBytes = kBtQV * kBtVPlane;      // 58,240 bytes
 // received partials: [quarter 4][instance 32][component 64] packed double-words
 constexpr size_t kBtPBytes = (size_t)4 * 32 * 64 * sizeof(double); // 64 KB
-constexpr size_t kBtSmem = kBtABytes + kBtVBytes + kBtPBytes + 1024;  // + exponents, flags, barrier
+constexpr size_t kBtMiscBytes = 1536; // kernel-specific arrays (error maxima, chunks, flags)
+constexpr size_t kBtSmem = kBtABytes + kBtVBytes + kBtPBytes + 256 + 128 + kBtMiscBytes + 16;
 constexpr int kBtTmemCols = 512;          // 7 groups x 64 columns, rounded up
 
 struct BundleTcParams {
@@ -155,6 +156,8 @@ __device__ __forceinline__ float scale_pow2(float x, int k)
 // Digit planes of A^T for the cluster backward: one block of 256 threads (k)
 // per row i of A^T (column i of A); A row-major FP64.
 __global__ void __launch_bounds__(256) bt_digits_A_kernel(const double *A, uint8_t *adig, int *aexp);
+// the same for A itself (the forward's z = A x): one block per row i of A
+__global__ void __launch_bounds__(256) bt_digits_Af_kernel(const double *A, uint8_t *adig, int *aexp);
 
 // r as packed double-words: one block of 256 threads per instance
 __global__ void __launch_bounds__(256) bt_pack_r_kernel(const double *par, double *rpk);
@@ -191,6 +194,254 @@ __device__ __forceinline__ void bt_issue_mmas(const uint8_t *sA, const uint8_t *
     bt_issue_mmas_from(umma_desc(smem_u32(sA), 128 * 16, 128), umma_desc(smem_u32(sV), kBtVKgroup, 128), tmem);
 }
 
+// ------------------------------------------------------- cluster sweep context
+
+// One CTA of a cluster sweep: its shared-memory regions, tensor memory and
+// MMA barrier, and each thread's two roles -- the 4 components j0 .. j0 + 3
+// of tile instance b it carries (digits in, partials out), and the row frow
+// and 16 columns fc .. fc + 15 of the product block it folds.
+struct BtCta {
+    uint8_t *sA, *sV; // operand digit planes (A resident, V per stage)
+    double *sR;       // received partials [quarter 4][instance 32][component 64]
+    int *sEv, *sBad;  // exponents of V per column [64]; non-finite flags [32]
+    uint8_t *misc;    // kernel-specific small arrays (kBtMiscBytes)
+    uint64_t *bar;
+    int t, warp, mt, q, tile;
+    uint32_t tmem, phase;
+    bool ok; // every MMA wait so far ended in time
+    int bl, jg, b, j0;
+    int ea;
+    uint32_t taddr, fold_dst, voff, v_remote, ev_remote;
+    const double *p_mine;
+};
+
+// Shared memory, tensor memory, the resident A block (digit block (mt, q) of
+// adig) and every thread's constants.  Ends with a CTA barrier; the kernel
+// then does its own set-up and one cluster barrier before any access to
+// another CTA's shared memory.
+__device__ __forceinline__ void bt_begin(BtCta &c, uint8_t *smem, const uint8_t *adig, const int *aexp)
+{
+    c.sA = smem;
+    c.sV = smem + kBtABytes;
+    c.sR = reinterpret_cast<double *>(smem + kBtABytes + kBtVBytes);
+    c.sEv = reinterpret_cast<int *>(smem + kBtABytes + kBtVBytes + kBtPBytes);
+    c.sBad = c.sEv + kBtTile;
+    c.misc = reinterpret_cast<uint8_t *>(c.sBad + 32);
+    c.bar = reinterpret_cast<uint64_t *>(c.misc + kBtMiscBytes);
+    uint32_t *slot_tmem = reinterpret_cast<uint32_t *>(c.bar + 1);
+    c.t = threadIdx.x;
+    c.warp = c.t >> 5;
+    const int lane = c.t & 31;
+    const uint32_t rank = cluster_rank();
+    c.mt = (int)(rank >> 2);
+    c.q = (int)(rank & 3);
+    c.tile = blockIdx.x / kBtCluster;
+    if (c.warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot_tmem)),
+                     "r"(kBtTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (c.t == 0) {
+        mbar_init(c.bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    {
+        const uint4 *ga = reinterpret_cast<const uint4 *>(adig + (size_t)(c.mt * 4 + c.q) * kBtABytes);
+        uint4 *sa = reinterpret_cast<uint4 *>(c.sA);
+#pragma unroll 4
+        for (int x = c.t; x < (int)(kBtABytes / 16); x += kBtThreads)
+            sa[x] = __ldg(ga + x);
+    }
+    if (c.t < 32)
+        c.sBad[c.t] = 0;
+    for (int x = c.t; x < (int)(kBtMiscBytes / 4); x += kBtThreads)
+        reinterpret_cast<int *>(c.misc)[x] = 0;
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    c.tmem = *slot_tmem;
+    c.phase = 0;
+    c.ok = true;
+    // carried components: instance b = 32 mt + bl, components 64 q + 4 jg + 0..3
+    c.bl = c.t >> 4;
+    c.jg = c.t & 15;
+    c.b = 32 * c.mt + c.bl;
+    c.j0 = 64 * c.q + 4 * c.jg;
+    // folded element: tensor-memory lane quadrant warp & 3, 16 columns
+    const int fq = c.warp & 3, fc = 16 * (c.warp >> 2);
+    const int frow = 32 * fq + lane;
+    c.ea = aexp[c.q * kBtN + 128 * c.mt + frow];
+    c.taddr = c.tmem + ((uint32_t)(32 * fq) << 16) + (uint32_t)fc;
+    // the fold's row frow is component 128 mt + frow, carried (for the
+    // instances of column half fc / 32) by CTA (fc / 32, 2 mt + frow / 64):
+    // slot q of its partials
+    c.fold_dst = dsmem_addr(c.sR + ((size_t)c.q * 32 + (fc & 31)) * 64 + (frow & 63),
+                            (uint32_t)((fc >> 5) * 4 + 2 * c.mt + (frow >> 6)));
+    c.p_mine = c.sR + (size_t)c.bl * 64 + 4 * c.jg;
+    // where this thread's digits go: plane offset of (column b, components
+    // j0 .. j0 + 3), here and in the partner (1 - mt, q)
+    const uint32_t partner = (uint32_t)((1 - c.mt) * 4 + c.q);
+    c.voff = (uint32_t)((c.jg >> 1) * kBtVKgroup + c.b * 16 + (c.jg & 1) * 8);
+    c.v_remote = dsmem_addr(c.sV + c.voff, partner);
+    c.ev_remote = dsmem_addr(c.sEv + c.b, partner);
+}
+
+// The digits of this thread's 4 values of instance b (the exponent over the
+// instance's 64 components of the quarter: its 16 threads) into the V
+// operand here and in the partner.
+__device__ __forceinline__ void bt_put(const BtCta &c, const dword (&v)[4])
+{
+    float mx = fmaxf(fmaxf(fabsf(v[0].hi), fabsf(v[1].hi)), fmaxf(fabsf(v[2].hi), fabsf(v[3].hi)));
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1)
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const int ev = tc_bound_exponent(mx);
+    const DigitScale sc = digit_scale(ev);
+    // digit s of the four values, packed as 4 bf16 (8 bytes)
+    uint32_t pk[kBtQV][2];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        float d[kBtQV];
+        split_digits<kBtQV>(v[e].hi, v[e].lo, sc, d);
+#pragma unroll
+        for (int s = 0; s < kBtQV; s++) {
+            const uint32_t w = (uint32_t)bf16_bits(d[s]) << (16 * (e & 1));
+            pk[s][e >> 1] = (e & 1) ? (pk[s][e >> 1] | w) : w;
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < kBtQV; s++) {
+        *reinterpret_cast<uint2 *>(c.sV + (size_t)s * kBtVPlane + c.voff) = make_uint2(pk[s][0], pk[s][1]);
+        dsmem_st_u32x2(c.v_remote + (uint32_t)(s * kBtVPlane), pk[s][0], pk[s][1]);
+    }
+    if (c.jg == 0) {
+        c.sEv[c.b] = ev;
+        dsmem_st_s32(c.ev_remote, ev);
+    }
+}
+
+// First half of a stage's product: the digits written by the generic proxy
+// become visible to the tensor core, and a cluster barrier: every CTA's V
+// operand and exponents are in place.
+__device__ __forceinline__ void bt_product_barrier()
+{
+    fence_proxy_async_all();
+    cluster_sync_all();
+}
+
+// Second half: the MMAs, the fold of the 7 group accumulators, every partial
+// pushed to the CTA that carries its (component, instance); a cluster barrier
+// after which every CTA's received partials are complete.
+__device__ __forceinline__ void bt_product_rest(BtCta &c, unsigned *error)
+{
+    // one thread issues the MMAs and alone polls their barrier (threads
+    // polling shared memory slow the tensor core's operand reads); the
+    // others wait at the CTA barrier
+    bool w = true;
+    if (c.ok && c.t == 0) {
+        tc_fence_after();
+        bt_issue_mmas(c.sA, c.sV, c.tmem);
+        umma_commit(c.bar);
+        w = mbar_wait_bounded(c.bar, c.phase, error);
+    }
+    if (c.ok)
+        c.phase ^= 1u;
+    c.ok = __syncthreads_and(c.ok && w) != 0;
+    tc_fence_after();
+    // fold: S = R_0 + R_1 2^-8 + R_2 2^-16 + (R_3 2^-24 + .. + R_6 2^-48)
+    // in units of group 0 (|R_g| < 2^24 integers): the tail is below 1 and
+    // summed in FP32 (error < 2^-23, i.e. 2^-47 of the largest S), the head
+    // with two 2Sums; then the power-of-two scaling 2^(eA + eV - 16)
+    const int fc = 16 * (c.warp >> 2);
+#pragma unroll 1
+    for (int half = 0; half < 2; half++) {
+        const int c0 = fc + 8 * half;
+        const uint32_t dst = c.fold_dst + (uint32_t)(8 * half * 64 * sizeof(double));
+        if (c.ok) {
+            float tail[8];
+            {
+                float R[4][8];
+                tmem_ld8_groups<4>(c.taddr + (uint32_t)(8 * half), 3, R);
+#pragma unroll
+                for (int k = 0; k < 8; k++)
+                    tail[k] = fmaf(R[0][k], 0x1p-24f, fmaf(R[1][k], 0x1p-32f, fmaf(R[2][k], 0x1p-40f, R[3][k] * 0x1p-48f)));
+            }
+            float R[3][8];
+            tmem_ld8_groups<3>(c.taddr + (uint32_t)(8 * half), 0, R);
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                float s1, e1, s2, e2, hi, lo;
+                two_sum(R[0][k], R[1][k] * 0x1p-8f, s1, e1);
+                two_sum(s1, R[2][k] * 0x1p-16f, s2, e2);
+                two_sum(s2, (e1 + e2) + tail[k], hi, lo);
+                const int sc = c.ea + c.sEv[c0 + k] - 16;
+                dsmem_st_f64(dst + (uint32_t)(k * 64 * sizeof(double)), dw_pack(dword(scale_pow2(hi, sc), scale_pow2(lo, sc))));
+            }
+        } else {
+            const double nan = __longlong_as_double(0x7ff8000000000000ll);
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                dsmem_st_f64(dst + (uint32_t)(k * 64 * sizeof(double)), nan);
+        }
+    }
+    tc_fence_before();
+    cluster_sync_all(); // every CTA's partials delivered
+}
+
+__device__ __forceinline__ void bt_product(BtCta &c, unsigned *error)
+{
+    bt_product_barrier();
+    bt_product_rest(c, error);
+}
+
+// The product's value for this thread's (j, b): the four received quarter
+// partials added in quarter order.
+__device__ __forceinline__ void bt_gather(const BtCta &c, dword (&G)[4])
+{
+    double2 v[4][2];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const double2 *src = reinterpret_cast<const double2 *>(c.p_mine + (size_t)k * 32 * 64);
+        v[k][0] = src[0];
+        v[k][1] = src[1];
+    }
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        dword s = dw_unpack(e & 1 ? v[0][e >> 1].y : v[0][e >> 1].x);
+#pragma unroll
+        for (int k = 1; k < 4; k++)
+            s += dw_unpack(e & 1 ? v[k][e >> 1].y : v[k][e >> 1].x);
+        G[e] = s;
+    }
+}
+
+// OR of the four quarter CTAs' non-finite flags for instance column bl
+// (after a cluster barrier)
+__device__ __forceinline__ int bt_bad(const BtCta &c)
+{
+    int bad = c.sBad[c.bl];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        if (k != c.q)
+            bad |= dsmem_ld_s32(dsmem_addr(c.sBad + c.bl, (uint32_t)(c.mt * 4 + k)));
+    return bad;
+}
+
+// Release of the tensor memory (after the kernel's last cluster barrier).
+__device__ __forceinline__ void bt_end(BtCta &c, unsigned *error)
+{
+    if (!c.ok && c.t == 0) // once more (bounded) for MMAs still in flight before the memory is released
+        (void)mbar_wait_bounded(c.bar, c.phase ^ 1u, error);
+    __syncthreads();
+    tc_fence_after();
+    if (c.warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(c.tmem), "r"(kBtTmemCols)
+                     : "memory");
+}
+
+// ------------------------------------------------------------ backward sweep
+
 template <class Tab>
 __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads, 1)
     backward_bundle_tc_kernel(BundleTcParams p)
@@ -200,63 +451,23 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
     constexpr int RS = bundle_stage_record_doubles(kBtN, NS);
     const AdjParams &a = p.bp.g;
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *sA = smem;
-    uint8_t *sV = smem + kBtABytes;
-    double *sR = reinterpret_cast<double *>(smem + kBtABytes + kBtVBytes);
-    int *sEv = reinterpret_cast<int *>(smem + kBtABytes + kBtVBytes + kBtPBytes); // [64] exponents of v per column
-    int *sBad = sEv + kBtTile;                                                     // [32] non-finite results
-    int *sMaxT = sBad + 32;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sMaxT + 2);
-    uint32_t *slot_tmem = reinterpret_cast<uint32_t *>(bar + 1);
-
-    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const uint32_t rank = cluster_rank();
-    const int mt = (int)(rank >> 2), q = (int)(rank & 3);
-    const uint32_t partner = (uint32_t)((1 - mt) * 4 + q);
-    const int tile = blockIdx.x / kBtCluster;
+    BtCta c;
+    bt_begin(c, smem, p.adig, p.aexp);
+    int *sMaxT = reinterpret_cast<int *>(c.misc);
     const int CH = a.pool.chunk_len;
-
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot_tmem)),
-                     "r"(kBtTmemCols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    if (t == 0) {
-        mbar_init(bar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        *sMaxT = 0;
-    }
-    // the A operand of this CTA's block, resident for the whole sweep
-    {
-        const uint4 *ga = reinterpret_cast<const uint4 *>(p.adig + (size_t)(mt * 4 + q) * kBtABytes);
-        uint4 *sa = reinterpret_cast<uint4 *>(sA);
-#pragma unroll 4
-        for (int x = t; x < (int)(kBtABytes / 16); x += kBtThreads)
-            sa[x] = __ldg(ga + x);
-    }
-    if (t < 32)
-        sBad[t] = 0;
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = *slot_tmem;
 
     // lockstep length of the tile: the longest instance (every CTA of the
     // cluster reads the same 64 counts and gets the same value)
-    if (t < kBtTile) {
-        const int inst = tile * kBtTile + t;
+    if (c.t < kBtTile) {
+        const int i = c.tile * kBtTile + c.t;
         int T = 0;
-        if (inst < a.B && a.inst_status[inst] == ST_OK)
-            T = a.inst_T[inst];
+        if (i < a.B && a.inst_status[i] == ST_OK)
+            T = a.inst_T[i];
         atomicMax(sMaxT, T);
     }
 
-    // this thread's instance (tile column b) and four components j0 .. j0 + 3
-    const int bl = t >> 4, jg = t & 15;
-    const int b = 32 * mt + bl;
-    const int inst = tile * kBtTile + b;
-    const int j0 = 64 * q + 4 * jg;
+    const int inst = c.tile * kBtTile + c.b;
+    const int j0 = c.j0;
     const bool inb = inst < a.B;
     bool live = inb && a.inst_status[inst] == ST_OK;
     if (inb && !live) {
@@ -266,7 +477,7 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
             a.dy0[(size_t)inst * kBtN + j0 + e] = nan;
             a.dpar[(size_t)inst * kBtN + j0 + e] = nan;
         }
-        if (a.status_out && q == 0 && jg == 0)
+        if (a.status_out && c.q == 0 && c.jg == 0)
             a.status_out[inst] = a.inst_status[inst];
     }
     // lambda and mu of the four components: compensated sums (each stage's
@@ -308,112 +519,16 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
             bad = bad || !isfinite(l) || !isfinite(d);
         }
         if (bad)
-            atomicOr(&sBad[bl], 1);
+            atomicOr(&c.sBad[c.bl], 1);
     };
     if (live && jstep < 0) { // no accepted step: the seeds are the result
         finish();
         live = false;
     }
-
-    // fold-thread constants: tensor-memory lane quadrant and 16 columns
-    const int fq = warp & 3, fc = 16 * (warp >> 2);
-    const int frow = 32 * fq + lane;
-    const int ea = p.aexp[q * kBtN + 128 * mt + frow];
-    const uint32_t taddr = tmem + ((uint32_t)(32 * fq) << 16) + (uint32_t)fc;
-    // where this thread's digits go: plane offset of (column b, components j0..j0+3)
-    const uint32_t voff = (uint32_t)((jg >> 1) * kBtVKgroup + b * 16 + (jg & 1) * 8);
-    const uint32_t v_remote = dsmem_addr(sV + voff, partner);
-    const uint32_t ev_remote = dsmem_addr(sEv + b, partner);
-    // where this thread reads its partials: rows j0 - 128 (q / 2) of column b in CTAs (q / 2, 0..3)
-    // where this thread's fold results go: row frow of this CTA's row tile is
-    // component j = 128 mt + frow, owned (for the instances of column half
-    // fc / 32) by CTA (fc / 32, 2 mt + frow / 64), slot q of its partials
-    const uint32_t fold_dst = dsmem_addr(sR + ((size_t)q * 32 + (fc & 31)) * 64 + (frow & 63),
-                                         (uint32_t)((fc >> 5) * 4 + 2 * mt + (frow >> 6)));
-    // the four partials of this thread's (j, b) in its own shared memory
-    const double *p_mine = sR + (size_t)bl * 64 + 4 * jg;
-
     __syncthreads();
     const int maxT = *sMaxT;
-    uint32_t phase = 0;
-    bool ok = true; // the MMA waits so far
     // every CTA of the cluster has started before any distributed access
     cluster_sync_all();
-
-    // the stage's product, folded into this CTA's partials
-    auto product = [&]() {
-        fence_proxy_async_all();
-        cluster_sync_all(); // V digits and exponents of the whole tile are in place
-        // one thread issues the MMAs and alone polls their barrier (threads
-        // polling shared memory slow the tensor core's operand reads); the
-        // others wait at the CTA barrier
-        bool w = true;
-        if (ok && t == 0) {
-            tc_fence_after();
-            bt_issue_mmas(sA, sV, tmem);
-            umma_commit(bar);
-            w = mbar_wait_bounded(bar, phase, p.error);
-        }
-        if (ok)
-            phase ^= 1u;
-        ok = __syncthreads_and(ok && w) != 0;
-        tc_fence_after();
-        // fold: S = R_0 + R_1 2^-8 + R_2 2^-16 + (R_3 2^-24 + .. + R_6 2^-48)
-        // in units of group 0 (|R_g| < 2^24 integers): the tail is below 1 and
-        // summed in FP32 (error < 2^-23, i.e. 2^-47 of the largest S), the head
-        // with two 2Sums; then the power-of-two scaling 2^(eA + eV - 16)
-#pragma unroll 1
-        for (int half = 0; half < 2; half++) {
-            const int c0 = fc + 8 * half;
-            const uint32_t dst = fold_dst + (uint32_t)(8 * half * 64 * sizeof(double));
-            if (ok) {
-                float tail[8];
-                {
-                    float R[4][8];
-                    tmem_ld8_groups<4>(taddr + (uint32_t)(8 * half), 3, R);
-#pragma unroll
-                    for (int c = 0; c < 8; c++)
-                        tail[c] = fmaf(R[0][c], 0x1p-24f, fmaf(R[1][c], 0x1p-32f, fmaf(R[2][c], 0x1p-40f, R[3][c] * 0x1p-48f)));
-                }
-                float R[3][8];
-                tmem_ld8_groups<3>(taddr + (uint32_t)(8 * half), 0, R);
-#pragma unroll
-                for (int c = 0; c < 8; c++) {
-                    float s1, e1, s2, e2, hi, lo;
-                    two_sum(R[0][c], R[1][c] * 0x1p-8f, s1, e1);
-                    two_sum(s1, R[2][c] * 0x1p-16f, s2, e2);
-                    two_sum(s2, (e1 + e2) + tail[c], hi, lo);
-                    const int k = ea + sEv[c0 + c] - 16;
-                    dsmem_st_f64(dst + (uint32_t)(c * 64 * sizeof(double)), dw_pack(dword(scale_pow2(hi, k), scale_pow2(lo, k))));
-                }
-            } else {
-                const double nan = __longlong_as_double(0x7ff8000000000000ll);
-#pragma unroll
-                for (int c = 0; c < 8; c++)
-                    dsmem_st_f64(dst + (uint32_t)(c * 64 * sizeof(double)), nan);
-            }
-        }
-        tc_fence_before();
-        cluster_sync_all(); // every CTA's partials delivered
-    };
-    // the four partials of this thread's (j, b): G = P_0 + P_1 + P_2 + P_3
-    auto gather = [&](dword (&G)[4]) {
-        double2 v[4][2];
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const double2 *src = reinterpret_cast<const double2 *>(p_mine + (size_t)k * 32 * 64);
-            v[k][0] = src[0];
-            v[k][1] = src[1];
-        }
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-            dword s = dw_unpack(e & 1 ? v[0][e >> 1].y : v[0][e >> 1].x);
-#pragma unroll
-            for (int k = 1; k < 4; k++)
-                s += dw_unpack(e & 1 ? v[k][e >> 1].y : v[k][e >> 1].x);
-            G[e] = s;
-        }
-    };
 
     // Kbar of the step's stages as compensated sums (seed b_m h lambda plus
     // a_km h g_k of the later stages k)
@@ -427,7 +542,7 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
         if (n > 0) {
             // stage 0 of the previous step: its g, then lambda and mu
             dword G[4];
-            gather(G);
+            bt_gather(c, G);
             if (active) {
 #pragma unroll
                 for (int e = 0; e < 4; e++)
@@ -467,7 +582,7 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
             if (m < NS - 1) {
                 // g of stage m + 1, and its share of the earlier stages' Kbar
                 dword G[4];
-                gather(G);
+                bt_gather(c, G);
                 if (active) {
 #pragma unroll
                     for (int e = 0; e < 4; e++) {
@@ -508,7 +623,7 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
                     double2 *fv = reinterpret_cast<double2 *>(p.bp.fac_v + k0 * kBtN + j0);
                     fv[0] = make_double2(dw_pack(v[0]), dw_pack(v[1]));
                     fv[1] = make_double2(dw_pack(v[2]), dw_pack(v[3]));
-                    if (q == 0 && jg == 0)
+                    if (c.q == 0 && c.jg == 0)
                         p.bp.fac_xp[k0] = srec + 2 + (size_t)m * kBtN;
                 }
             } else {
@@ -516,60 +631,389 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
                 for (int e = 0; e < 4; e++)
                     v[e] = dword(0.0f, 0.0f);
             }
-            // the column exponent over the quarter (the 16 threads of instance b)
-            float mx = fmaxf(fmaxf(fabsf(v[0].hi), fabsf(v[1].hi)), fmaxf(fabsf(v[2].hi), fabsf(v[3].hi)));
-#pragma unroll
-            for (int o = 8; o > 0; o >>= 1)
-                mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            const int ev = tc_bound_exponent(mx);
-            const DigitScale sc = digit_scale(ev);
-            // digit s of the four components, packed as 4 bf16 (8 bytes)
-            uint32_t pk[kBtQV][2];
-#pragma unroll
-            for (int e = 0; e < 4; e++) {
-                float d[kBtQV];
-                split_digits<kBtQV>(v[e].hi, v[e].lo, sc, d);
-#pragma unroll
-                for (int s = 0; s < kBtQV; s++) {
-                    const uint32_t w = (uint32_t)bf16_bits(d[s]) << (16 * (e & 1));
-                    pk[s][e >> 1] = (e & 1) ? (pk[s][e >> 1] | w) : w;
-                }
-            }
-#pragma unroll
-            for (int s = 0; s < kBtQV; s++) {
-                *reinterpret_cast<uint2 *>(sV + (size_t)s * kBtVPlane + voff) = make_uint2(pk[s][0], pk[s][1]);
-                dsmem_st_u32x2(v_remote + (uint32_t)(s * kBtVPlane), pk[s][0], pk[s][1]);
-            }
-            if (jg == 0) {
-                sEv[b] = ev;
-                dsmem_st_s32(ev_remote, ev);
-            }
-            product();
+            bt_put(c, v);
+            bt_product(c, p.error);
         }
     }
     // every partial has been read; then the instances' status from the four
     // quarters' flags (rank 4 mt + k holds quarter k of the same instances)
     cluster_sync_all();
-    if (q == 0 && jg == 0 && inb && a.inst_status[inst] == ST_OK && a.status_out) {
-        int bad = sBad[bl];
-#pragma unroll
-        for (int k = 1; k < 4; k++)
-            bad |= dsmem_ld_s32(dsmem_addr(sBad + bl, (uint32_t)(mt * 4 + k)));
-        a.status_out[inst] = bad ? ST_NONFINITE : ST_OK;
-    }
+    if (c.q == 0 && c.jg == 0 && inb && a.inst_status[inst] == ST_OK && a.status_out)
+        a.status_out[inst] = bt_bad(c) ? ST_NONFINITE : ST_OK;
     cluster_sync_all(); // no CTA leaves while another reads its shared memory
-    if (!ok && t == 0) // once more (bounded) for MMAs still in flight before the memory is released
-        (void)mbar_wait_bounded(bar, phase ^ 1u, p.error);
-    __syncthreads();
-    tc_fence_after();
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kBtTmemCols) : "memory");
+    bt_end(c, p.error);
 }
 
-// Host side (va_bundle_tc.cu): whether the cluster sweep can run for the
-// tableau on this GPU (set up once, before any capture), and its launch:
-// digit planes of A^T, then one cluster of 8 CTAs per tile of 64 instances.
+// ------------------------------------------------------------- forward sweep
+
+// The forward sweep of the same tile in lockstep (DOPRI5: FSAL, controlled):
+// iteration n is one attempt of every instance that has not finished, each
+// with its own t, dt and odeint controller decision.  Per attempt the six
+// products z_m = A X_m (stages 2 .. 6 and f(y_new)) run as in the backward,
+// with A's digit planes (not A^T's).  What needs the whole instance crosses
+// the 4 quarter CTAs (mt, 0..3) that carry its components:
+//   - the error ratio: each CTA's maximum over its 64 components, exchanged
+//     through distributed shared memory (a cluster barrier), then the same
+//     controller decision in each of them (one thread per instance; its 16
+//     threads take the result by shuffle);
+//   - checkpoint chunks: CTA (mt, 0) allocates an instance's next chunk when
+//     its current one fills and hands it to the other three (read at the
+//     next top of step, many cluster barriers later);
+//   - the end: non-finite flags of y(T) gathered by CTA (mt, 0), which
+//     writes the instance's counters and status.
+// Every accepted step writes the same stage record as the bundle forward
+// [t, dt, X_0 .. X_5, z_0 .. z_5]; each CTA its 64 components.  The
+// arithmetic per component is the bundle forward's double-word arithmetic;
+// the error ratio is formed in double-words (|e| / tol by double-word
+// division) instead of FP64.
+template <class Tab>
+__global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads, 1)
+    forward_bundle_tc_kernel(BundleTcParams p)
+{
+    static_assert(Tab::FSAL && !Tab::FIXED, "controlled FSAL pairs");
+    constexpr int NS = Tab::S;
+    constexpr int RS = bundle_stage_record_doubles(kBtN, NS);
+    const FwdParams &a = p.bp.f;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    BtCta c;
+    bt_begin(c, smem, p.adig, p.aexp);
+    double *sErr = reinterpret_cast<double *>(c.misc);    // [4 quarters][32 instances] error-ratio maxima
+    int *sChunk = reinterpret_cast<int *>(c.misc + 1024); // [32] next checkpoint chunk
+    int *sAct = sChunk + 32;                              // [8] CTAs with an attempt this iteration
+    const int CH = a.pool.chunk_len;
+    const int inst = c.tile * kBtTile + c.b;
+    const int j0 = c.j0;
+    const bool inb = inst < a.B;
+    const bool lead = c.jg == 0; // runs instance b's controller and allocations
+    const int lead_lane = (c.t & 31) & 16;
+    const uint32_t rank = (uint32_t)(4 * c.mt + c.q);
+
+    // instance state, the same in the 64 threads (4 CTAs x 16) that carry it
+    int status = ST_OK, count = 0, rej = 0, fails = 0, chunk = -1, slot = 0;
+    double t = 0.0, t1 = 0.0, dt = a.dt0;
+    bool at_top = true, done = !inb;
+    double *rec = nullptr; // the current step's record
+    dword ys[4], z0[4], K[NS][4];
+    const double2 *rp = reinterpret_cast<const double2 *>(p.rpk + (size_t)(inb ? inst : 0) * kBtN + j0);
+    auto rv = [&](int e) -> dword {
+        const double2 r2 = __ldg(rp + (e >> 1));
+        return dw_unpack(e & 1 ? r2.y : r2.x);
+    };
+    if (inb) {
+        t = a.t0[inst];
+        t1 = a.t1[inst];
+        const double2 *y2 = reinterpret_cast<const double2 *>(a.y0 + (size_t)inst * kBtN + j0);
+        const double2 y01 = y2[0], y23 = y2[1];
+        ys[0] = dword(y01.x);
+        ys[1] = dword(y01.y);
+        ys[2] = dword(y23.x);
+        ys[3] = dword(y23.y);
+    } else {
+#pragma unroll
+        for (int e = 0; e < 4; e++)
+            ys[e] = dword(0.0f, 0.0f);
+    }
+    const dword datol(a.atol), drtol(a.rtol);
+    // every CTA of the cluster has started before any distributed access
+    cluster_sync_all();
+
+    // the instance's next chunk, from CTA (mt, 0) to the four quarter CTAs
+    auto alloc_chunk = [&](int prev) {
+        int ch = (int)atomicAdd(&a.ctl->pool_next, 1u);
+        if (ch >= a.pool.n_chunks) {
+            ch = -1;
+            atomicOr(&a.ctl->pool_fail, 1u);
+        } else {
+            a.pool.chunk_prev[ch] = prev;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            dsmem_st_s32(dsmem_addr(sChunk + c.bl, (uint32_t)(c.mt * 4 + k)), ch);
+    };
+    if (c.q == 0 && lead && inb)
+        alloc_chunk(-1);
+    // k_1 = f(y_0)
+    bt_put(c, ys);
+    bt_product(c, p.error); // (its barriers also deliver the first chunks)
+    {
+        dword G[4];
+        bt_gather(c, G);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            z0[e] = G[e];
+            K[0][e] = ys[e] * (rv(e) + G[e]);
+        }
+    }
+    if (inb) {
+        chunk = sChunk[c.bl];
+        slot = 0;
+        if (chunk < 0)
+            status = ST_CKPT_BUDGET;
+    }
+
+    for (;;) {
+        // top of step of the instances whose last attempt was accepted (or
+        // at the start): loop test, record, end clamp
+        if (!done && at_top) {
+            const bool end = !(t1 - t > kDblEps);
+            bool fin = status != ST_OK;
+            if (!fin && !end && count >= a.max_steps) {
+                status = ST_MAX_STEPS;
+                fin = true;
+            }
+            if (!fin && slot == CH) {
+                chunk = sChunk[c.bl];
+                slot = 0;
+                if (chunk < 0) {
+                    status = ST_CKPT_BUDGET;
+                    fin = true;
+                }
+            }
+            if (!fin) {
+                rec = record_ptr<RS>(a.pool, chunk, slot);
+                if (c.q == 0 && lead)
+                    *reinterpret_cast<double2 *>(rec) = make_double2(t, dt);
+                double2 *x0 = reinterpret_cast<double2 *>(rec + 2 + j0);
+                double2 *zz = reinterpret_cast<double2 *>(rec + 2 + (size_t)NS * kBtN + j0);
+                x0[0] = make_double2(dw_pack(ys[0]), dw_pack(ys[1]));
+                x0[1] = make_double2(dw_pack(ys[2]), dw_pack(ys[3]));
+                zz[0] = make_double2(dw_pack(z0[0]), dw_pack(z0[1]));
+                zz[1] = make_double2(dw_pack(z0[2]), dw_pack(z0[3]));
+                slot++;
+                if (slot == CH && !end && c.q == 0 && lead)
+                    alloc_chunk(chunk);
+                fin = end;
+            }
+            if (fin) {
+                // y(T) of this thread's components and their finiteness
+                done = true;
+                bool bad = false;
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const double y = count > 0 ? to_d(ys[e]) : a.y0[(size_t)inst * kBtN + j0 + e];
+                    if (a.yT)
+                        a.yT[(size_t)inst * kBtN + j0 + e] = y;
+                    bad = bad || !isfinite(y);
+                }
+                if (bad)
+                    atomicOr(&c.sBad[c.bl], 1);
+            } else {
+                if ((t + dt) - t1 > kDblEps)
+                    dt = t1 - t;
+                fails = 0;
+                at_top = false;
+            }
+        }
+        const bool attempt = !done;
+        // whether any instance of the tile attempts: each CTA's flag to all
+        // eight (read after the first stage's cluster barrier)
+        {
+            const int mine = __syncthreads_or(attempt ? 1 : 0);
+            if (c.t < kBtCluster)
+                dsmem_st_s32(dsmem_addr(sAct + rank, (uint32_t)c.t), mine);
+        }
+        const dword sdt = dword(dt);
+        bool stop = false;
+        // stages 2 .. s: X_m = y + dt sum_{j<m} a_mj K_j, K_m = X_m (r + A X_m)
+#pragma unroll
+        for (int m = 1; m < NS; m++) {
+            dword X[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                if (attempt) {
+                    dword acc(0.0f, 0.0f);
+#pragma unroll
+                    for (int j = 0; j < NS - 1; j++)
+                        if (j < m)
+                            acc = madd(dword(Tab::a(m, j)), K[j][e], acc);
+                    X[e] = madd(acc, sdt, ys[e]);
+                } else {
+                    X[e] = dword(0.0f, 0.0f);
+                }
+            }
+            bt_put(c, X);
+            bt_product_barrier();
+            if (m == 1) {
+                int any = 0;
+#pragma unroll
+                for (int k = 0; k < kBtCluster; k++)
+                    any |= sAct[k];
+                if (!any) { // every CTA of the cluster reads the same flags
+                    stop = true;
+                    break;
+                }
+            }
+            bt_product_rest(c, p.error);
+            dword G[4];
+            bt_gather(c, G);
+#pragma unroll
+            for (int e = 0; e < 4; e++)
+                K[m][e] = X[e] * (rv(e) + G[e]);
+            if (attempt) {
+                // every attempt rewrites the step's stage values: the accepted one is the last
+                double2 *xm = reinterpret_cast<double2 *>(rec + 2 + (size_t)m * kBtN + j0);
+                double2 *zm = reinterpret_cast<double2 *>(rec + 2 + (size_t)(NS + m) * kBtN + j0);
+                xm[0] = make_double2(dw_pack(X[0]), dw_pack(X[1]));
+                xm[1] = make_double2(dw_pack(X[2]), dw_pack(X[3]));
+                zm[0] = make_double2(dw_pack(G[0]), dw_pack(G[1]));
+                zm[1] = make_double2(dw_pack(G[2]), dw_pack(G[3]));
+            }
+        }
+        if (stop)
+            break;
+        // y_new = y + dt sum_j b_j K_j and f(y_new)
+        dword yn[4], zn[4], kn[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            if (attempt) {
+                dword acc(0.0f, 0.0f);
+#pragma unroll
+                for (int j = 0; j < NS; j++)
+                    if (Tab::b(j) != 0.0)
+                        acc = madd(dword(Tab::b(j)), K[j][e], acc);
+                yn[e] = madd(acc, sdt, ys[e]);
+            } else {
+                yn[e] = dword(0.0f, 0.0f);
+            }
+        }
+        bt_put(c, yn);
+        bt_product(c, p.error);
+        {
+            dword G[4];
+            bt_gather(c, G);
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                zn[e] = G[e];
+                kn[e] = yn[e] * (rv(e) + G[e]);
+            }
+        }
+        // error ratio |dt sum_j e_j K_j| / (atol + rtol (|y| + |dt| |K_1|)),
+        // its maximum over the instance's components (a NaN ratio makes it
+        // NaN, as in the bundle forward)
+        dword rmax(0.0f, 0.0f);
+        bool nanr = false;
+        if (attempt) {
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                dword acc(0.0f, 0.0f);
+#pragma unroll
+                for (int j = 0; j < NS; j++)
+                    if (Tab::e(j) != 0.0)
+                        acc = madd(dword(Tab::e(j)), K[j][e], acc);
+                acc = madd(dword(Tab::E_NEW), kn[e], acc);
+                const dword tol = datol + drtol * (dabs(ys[e]) + dabs(sdt) * dabs(K[0][e]));
+                const dword ratio = dabs(acc * sdt) / tol;
+                if (ratio.hi != ratio.hi)
+                    nanr = true;
+                else if (dw_greater(ratio, rmax))
+                    rmax = ratio;
+            }
+        }
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+            const dword other(__shfl_xor_sync(0xffffffffu, rmax.hi, o), __shfl_xor_sync(0xffffffffu, rmax.lo, o));
+            if (dw_greater(other, rmax))
+                rmax = other;
+        }
+        nanr = ((__ballot_sync(0xffffffffu, nanr) >> lead_lane) & 0xffffu) != 0;
+        if (lead) {
+            const double ep = nanr ? __longlong_as_double(0x7ff8000000000000ll) : to_d(rmax);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                dsmem_st_f64(dsmem_addr(sErr + c.q * 32 + c.bl, (uint32_t)(c.mt * 4 + k)), ep);
+        }
+        cluster_sync_all();
+        // the controller (odeint's try_step), run by the lead thread
+        int accepted = 0;
+        if (attempt && lead) {
+            double err = 0.0;
+            bool nan = false;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const double x = sErr[32 * k + c.bl];
+                nan = nan || x != x;
+                err = fmax(err, x);
+            }
+            if (nan)
+                err = __longlong_as_double(0x7ff8000000000000ll);
+            if (err != err) {
+                status = ST_NONFINITE;
+                at_top = true;
+            } else {
+                bool ok;
+                if (err > 1.0) {
+                    dt = decrease_step<Tab, dword>(dt, err, a.step_pow, nullptr);
+                    rej++;
+                    ok = false;
+                } else {
+                    t = t + dt;
+                    dt = increase_step<Tab, dword>(dt, err, a.step_pow, nullptr);
+                    accepted = 1;
+                    ok = true;
+                }
+                if (fails >= a.max_fail) {
+                    status = ST_MAX_REJECTS;
+                    at_top = true;
+                } else {
+                    fails++;
+                    if (ok) {
+                        count++;
+                        at_top = true;
+                    } else if (!(dt > 0.0) || !isfinite(dt)) {
+                        status = ST_NONFINITE;
+                        at_top = true;
+                    }
+                }
+            }
+        }
+        // the instance's 16 threads take the lead's result
+        t = __shfl_sync(0xffffffffu, t, lead_lane);
+        dt = __shfl_sync(0xffffffffu, dt, lead_lane);
+        status = __shfl_sync(0xffffffffu, status, lead_lane);
+        count = __shfl_sync(0xffffffffu, count, lead_lane);
+        rej = __shfl_sync(0xffffffffu, rej, lead_lane);
+        fails = __shfl_sync(0xffffffffu, fails, lead_lane);
+        at_top = __shfl_sync(0xffffffffu, at_top ? 1 : 0, lead_lane) != 0;
+        accepted = __shfl_sync(0xffffffffu, accepted, lead_lane);
+        if (accepted) {
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                ys[e] = yn[e];
+                K[0][e] = kn[e];
+                z0[e] = zn[e];
+            }
+        }
+    }
+    // counters and status of the tile's instances: y(T)'s finiteness from the
+    // four quarter CTAs
+    cluster_sync_all();
+    if (c.q == 0 && lead && inb) {
+        if (bt_bad(c) && status == ST_OK)
+            status = ST_NONFINITE;
+        a.inst_T[inst] = count;
+        a.inst_last[inst] = status == ST_OK ? chunk : -1;
+        a.inst_status[inst] = status;
+        if (a.inst_t1)
+            a.inst_t1[inst] = t1;
+        if (a.n_acc_out)
+            a.n_acc_out[inst] = count;
+        if (a.n_rej_out)
+            a.n_rej_out[inst] = rej;
+        if (a.status_out)
+            a.status_out[inst] = status;
+    }
+    cluster_sync_all(); // no CTA leaves while another reads its shared memory
+    bt_end(c, p.error);
+}
+
+// Host side (va_bundle_tc.cu): whether the cluster sweeps can run for the
+// tableau on this GPU (set up once, before any capture), and their launches:
+// digit planes of A (forward) or A^T (backward) and r as double-words, then
+// one cluster of 8 CTAs per tile of 64 instances.
 bool bundle_tc_available(int tableau);
+bool bundle_tc_forward_available(int tableau);
+cudaError_t enqueue_bundle_tc_forward(const BundleParams &bp, const double *A, uint8_t *adig, int *aexp,
+                                      double *rpk, unsigned *error, int tableau, cudaStream_t s);
 cudaError_t enqueue_bundle_tc_backward(const BundleParams &bp, const double *A, uint8_t *adig, int *aexp,
                                        double *rpk, unsigned *error, int tableau, cudaStream_t s);
 constexpr size_t kBtADigitBytes = 8 * kBtABytes;
