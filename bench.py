@@ -298,6 +298,16 @@ DW_TRAFFIC = {("vdpb", "forward"): 121.0e6 + 5557.4e6, ("vdpb", "backward"): 565
               ("vdp1", "forward"): 0.05e6, ("glv256", "forward"): 12.6e6 + 1179.1e6}
 
 
+def measured_bf16_peak():
+    """Dense bf16 TFLOP/s from MEASURED_PEAKS.json (the sustained figure: the
+    kernels run inside a multi-millisecond step), else the recipe's fallback."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops_sustained"]), "MEASURED_PEAKS.json bf16_tflops_sustained"
+    except (OSError, KeyError, ValueError):
+        return 1700.0, "fallback (no MEASURED_PEAKS.json): sustained bf16 ~1.7 PFLOP/s"
+
+
 def pipe_rates():
     """This GPU's arithmetic pipe rates from the library's probes
     (va_probe_rate): FP64 FMA, FP32 FMA and FP64 tensor-core MMA, TFLOP/s;
@@ -319,13 +329,27 @@ def pipe_rates():
     return out
 
 
-def roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted):
+def cluster_mma_flops(attempts_per_instance, forward):
+    """bf16 tensor FLOPs the cluster sweeps of the shared-matrix GLV execute
+    (csrc/va_bundle_tc.cuh): per tile of 64 instances, per product, 8 CTAs x
+    108 MMAs of M 128, N 64, K 16.  Forward: f(y_0), then 6 products (5
+    stages and f(y_new)) per attempt of the tile's longest instance; backward:
+    6 per accepted step of the tile's longest instance."""
+    per_product = 8 * 108 * 2 * 128 * 64 * 16
+    a = np.asarray(attempts_per_instance, dtype=np.int64)
+    tiles = [int(a[i:i + 64].max()) for i in range(0, len(a), 64)]
+    return per_product * sum((1 + 6 * m) if forward else 6 * m for m in tiles)
+
+
+def roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted, launch=None, per_inst=None):
     """Roofline of the dominant sweep kernel.  fp64: algorithmic FP64 FLOPs
     against cuBLAS DGEMM.  mixed_dw: the FP32 FLOPs the double-word
     arithmetic executes (ncu-counted per attempt / per step, scaled by this
-    run's attempts and steps) against cuBLAS SGEMM; mixed: the algorithmic
-    count, executed in FP32, against SGEMM.  Every mode also reports the
-    FP64-equivalent rate (algorithmic FP64 FLOPs / time) against DGEMM."""
+    run's attempts and steps) against cuBLAS SGEMM, or, for the shared-matrix
+    cluster sweeps on the tensor cores, their executed bf16 MMA FLOPs against
+    the measured bf16 peak; mixed: the algorithmic count, executed in FP32,
+    against SGEMM.  Every mode also reports the FP64-equivalent rate
+    (algorithmic FP64 FLOPs / time) against DGEMM."""
     fwd_dom = DOMINANT.get(c["model"], "forward" if fms >= bms else "backward") == "forward"
     kernel, ms = ("forward", fms) if fwd_dom else ("backward", bms)
     alg = fl_f if fwd_dom else fl_b
@@ -334,6 +358,17 @@ def roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted):
     out = {"kernel": kernel, "unit": "TFLOP/s", "launch_ms": ms, "forward_ms": fms, "backward_ms": bms,
            "traffic": DW_TRAFFIC.get((args.config, kernel)) if args.precision == "mixed_dw" else None,
            "fp64_equivalent": {"achieved": equiv, "dgemm_peak": peak64, "ratio": equiv / peak64}}
+    cluster = (launch or {}).get("fwd_block" if fwd_dom else "bwd_block") == 512 and c["model"] == "glv_shared"
+    if args.precision == "mixed_dw" and cluster and per_inst is not None:
+        fl = cluster_mma_flops(per_inst[0] if fwd_dom else per_inst[1], fwd_dom)
+        peak, src = measured_bf16_peak()
+        out.update(kernel=kernel + " (tensor-core cluster sweep)", bound="tensor", achieved=fl / (ms * 1e-3) / 1e12,
+                   peak=peak, peak_source=src, flops_per_launch=fl,
+                   traffic=DW_TRAFFIC.get((args.config, "tc_" + kernel)),
+                   flop_count="bf16 MMA FLOPs executed (8 CTAs x 108 MMAs of 128x64x16 per product and tile; "
+                              "per tile the longest instance's attempts)")
+        out["frac"] = out["achieved"] / out["peak"]
+        return out
     dgemm = "cuBLAS DGEMM 4096^3 measured in this run (FP64 is absent from the measured-peaks file)"
     sgemm = "cuBLAS SGEMM 8192^3, TF32 off, measured in this run (FP32 is absent from the measured-peaks file)"
     per = DW_FP32_FLOPS.get((c["model"], c["tableau"]), (None, None))[0 if fwd_dom else 1]
@@ -514,7 +549,8 @@ def _bench(args, rank, world, local, torch, dist):
     attempts, accepted = int((n_acc + n_rej).sum()), int(n_acc.sum())
     fl_f, fl_b = flops(c["model"], c["tableau"], c["n"], attempts, accepted)
     fms, bms = float(np.median(fw_ms)), float(np.median(bw_ms))
-    roofline = roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted)
+    roofline = roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted, launch=s.launch(),
+                           per_inst=(n_acc + n_rej, n_acc))
 
     # the other precision modes on the same batch: throughput and gradient error vs FP64
     def run_mode(precision, step_pow=args.step_pow):
@@ -614,8 +650,11 @@ def _bench(args, rank, world, local, torch, dist):
                        "launch": s.launch(), "status_ok": int((status == 0).sum())},
             "e2e": {"value": e2e, "unit": "gradients/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             # per gradient: forward order (3) + forward + backward order (3) +
-            # backward; shared-matrix bundles: prepare + forward + backward + dA reduce
-            "gpu_launches": (4 if c["model"] == "glv_shared" else 8) * args.steps,
+            # backward; shared-matrix bundles: prepare + forward + factor offsets +
+            # backward + dA contraction + partial sum, and each tensor-core
+            # cluster sweep its digit planes of A and packed r
+            "gpu_launches": (6 + 2 * (s.launch()["fwd_block"] == 512) + 2 * (s.launch()["bwd_block"] == 512)
+                             if c["model"] == "glv_shared" else 8) * args.steps,
             "roofline": roofline,
             "fp64_batched": fp64_value,
             "modes": modes,

@@ -74,7 +74,7 @@ constexpr size_t kBtVPlane = 8 * kBtVKgroup;         // 8,320 bytes
 constexpr size_t kBtVBytes = kBtQV * kBtVPlane;      // 58,240 bytes
 // received partials: [quarter 4][instance 32][component 64] packed double-words
 constexpr size_t kBtPBytes = (size_t)4 * 32 * 64 * sizeof(double); // 64 KB
-constexpr size_t kBtMiscBytes = 1536; // kernel-specific arrays (error maxima, chunks, flags)
+constexpr size_t kBtMiscBytes = 4096; // kernel-specific arrays (error maxima, chunks, flags, instance state)
 constexpr size_t kBtSmem = kBtABytes + kBtVBytes + kBtPBytes + 256 + 128 + kBtMiscBytes + 16;
 constexpr int kBtTmemCols = 512;          // 7 groups x 64 columns, rounded up
 
@@ -666,6 +666,20 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
 // arithmetic per component is the bundle forward's double-word arithmetic;
 // the error ratio is formed in double-words (|e| / tol by double-word
 // division) instead of FP64.
+// Per-instance state of the forward's 32 instances of a CTA, in shared
+// memory: the FP64 controller and the top-of-step logic run in warp 0, one
+// lane per instance (in the instance's own threads every FP64 instruction
+// would issue in 16 warps: the FP64 pipe, 1/64 of FP32 on this GPU, was the
+// forward's bound).
+struct BtFwdInst {
+    double t[32], t1[32], dt[32];
+    double *rec[32];   // the current step's record
+    float2 sdt[32];    // dt as a double-word
+    int count[32], rej[32], fails[32], status[32], chunk[32], slot[32];
+    int mode[32];      // kFwd* flags of this iteration
+};
+constexpr int kFwdAttempt = 1, kFwdTopRecord = 2, kFwdFinished = 4, kFwdAccepted = 8, kFwdDone = 16, kFwdAtTop = 32;
+
 template <class Tab>
 __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads, 1)
     forward_bundle_tc_kernel(BundleTcParams p)
@@ -680,19 +694,16 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
     double *sErr = reinterpret_cast<double *>(c.misc);    // [4 quarters][32 instances] error-ratio maxima
     int *sChunk = reinterpret_cast<int *>(c.misc + 1024); // [32] next checkpoint chunk
     int *sAct = sChunk + 32;                              // [8] CTAs with an attempt this iteration
+    BtFwdInst &S = *reinterpret_cast<BtFwdInst *>(c.misc + 1280);
     const int CH = a.pool.chunk_len;
-    const int inst = c.tile * kBtTile + c.b;
     const int j0 = c.j0;
+    const int inst = c.tile * kBtTile + c.b;
     const bool inb = inst < a.B;
-    const bool lead = c.jg == 0; // runs instance b's controller and allocations
-    const int lead_lane = (c.t & 31) & 16;
-    const uint32_t rank = (uint32_t)(4 * c.mt + c.q);
+    const int lane = c.t & 31;
+    const bool ctl = c.warp == 0; // warp 0: lane L runs instance column L
+    const int cinst = c.tile * kBtTile + 32 * c.mt + lane;
+    const bool cinb = ctl && cinst < a.B;
 
-    // instance state, the same in the 64 threads (4 CTAs x 16) that carry it
-    int status = ST_OK, count = 0, rej = 0, fails = 0, chunk = -1, slot = 0;
-    double t = 0.0, t1 = 0.0, dt = a.dt0;
-    bool at_top = true, done = !inb;
-    double *rec = nullptr; // the current step's record
     dword ys[4], z0[4], K[NS][4];
     const double2 *rp = reinterpret_cast<const double2 *>(p.rpk + (size_t)(inb ? inst : 0) * kBtN + j0);
     auto rv = [&](int e) -> dword {
@@ -700,8 +711,6 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
         return dw_unpack(e & 1 ? r2.y : r2.x);
     };
     if (inb) {
-        t = a.t0[inst];
-        t1 = a.t1[inst];
         const double2 *y2 = reinterpret_cast<const double2 *>(a.y0 + (size_t)inst * kBtN + j0);
         const double2 y01 = y2[0], y23 = y2[1];
         ys[0] = dword(y01.x);
@@ -713,11 +722,23 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
         for (int e = 0; e < 4; e++)
             ys[e] = dword(0.0f, 0.0f);
     }
+    if (ctl) {
+        S.t[lane] = cinb ? a.t0[cinst] : 0.0;
+        S.t1[lane] = cinb ? a.t1[cinst] : 0.0;
+        S.dt[lane] = a.dt0;
+        S.count[lane] = S.rej[lane] = S.fails[lane] = 0;
+        S.status[lane] = ST_OK;
+        S.chunk[lane] = -1;
+        S.slot[lane] = 0;
+        S.mode[lane] = cinb ? kFwdAtTop : kFwdDone;
+        S.rec[lane] = nullptr;
+    }
     const dword datol(a.atol), drtol(a.rtol);
     // every CTA of the cluster has started before any distributed access
     cluster_sync_all();
 
     // the instance's next chunk, from CTA (mt, 0) to the four quarter CTAs
+    // (warp 0, lane = instance column)
     auto alloc_chunk = [&](int prev) {
         int ch = (int)atomicAdd(&a.ctl->pool_next, 1u);
         if (ch >= a.pool.n_chunks) {
@@ -728,9 +749,9 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
         }
 #pragma unroll
         for (int k = 0; k < 4; k++)
-            dsmem_st_s32(dsmem_addr(sChunk + c.bl, (uint32_t)(c.mt * 4 + k)), ch);
+            dsmem_st_s32(dsmem_addr(sChunk + lane, (uint32_t)(c.mt * 4 + k)), ch);
     };
-    if (c.q == 0 && lead && inb)
+    if (c.q == 0 && cinb)
         alloc_chunk(-1);
     // k_1 = f(y_0)
     bt_put(c, ys);
@@ -744,75 +765,97 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
             K[0][e] = ys[e] * (rv(e) + G[e]);
         }
     }
-    if (inb) {
-        chunk = sChunk[c.bl];
-        slot = 0;
-        if (chunk < 0)
-            status = ST_CKPT_BUDGET;
+    if (cinb) {
+        S.chunk[lane] = sChunk[lane];
+        if (S.chunk[lane] < 0)
+            S.status[lane] = ST_CKPT_BUDGET;
     }
 
     for (;;) {
-        // top of step of the instances whose last attempt was accepted (or
-        // at the start): loop test, record, end clamp
-        if (!done && at_top) {
-            const bool end = !(t1 - t > kDblEps);
-            bool fin = status != ST_OK;
-            if (!fin && !end && count >= a.max_steps) {
-                status = ST_MAX_STEPS;
-                fin = true;
-            }
-            if (!fin && slot == CH) {
-                chunk = sChunk[c.bl];
-                slot = 0;
-                if (chunk < 0) {
-                    status = ST_CKPT_BUDGET;
+        // top of step (warp 0): loop test, record, end clamp of the instances
+        // whose last attempt was accepted (or at the start)
+        if (ctl) {
+            int mode = S.mode[lane] & (kFwdDone | kFwdAtTop);
+            if (!(mode & kFwdDone) && (mode & kFwdAtTop)) {
+                double t = S.t[lane], t1 = S.t1[lane], dt = S.dt[lane];
+                int status = S.status[lane], chunk = S.chunk[lane], slot = S.slot[lane];
+                const bool end = !(t1 - t > kDblEps);
+                bool fin = status != ST_OK;
+                if (!fin && !end && S.count[lane] >= a.max_steps) {
+                    status = ST_MAX_STEPS;
                     fin = true;
                 }
-            }
-            if (!fin) {
-                rec = record_ptr<RS>(a.pool, chunk, slot);
-                if (c.q == 0 && lead)
-                    *reinterpret_cast<double2 *>(rec) = make_double2(t, dt);
-                double2 *x0 = reinterpret_cast<double2 *>(rec + 2 + j0);
-                double2 *zz = reinterpret_cast<double2 *>(rec + 2 + (size_t)NS * kBtN + j0);
-                x0[0] = make_double2(dw_pack(ys[0]), dw_pack(ys[1]));
-                x0[1] = make_double2(dw_pack(ys[2]), dw_pack(ys[3]));
-                zz[0] = make_double2(dw_pack(z0[0]), dw_pack(z0[1]));
-                zz[1] = make_double2(dw_pack(z0[2]), dw_pack(z0[3]));
-                slot++;
-                if (slot == CH && !end && c.q == 0 && lead)
-                    alloc_chunk(chunk);
-                fin = end;
-            }
-            if (fin) {
-                // y(T) of this thread's components and their finiteness
-                done = true;
-                bool bad = false;
-#pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    const double y = count > 0 ? to_d(ys[e]) : a.y0[(size_t)inst * kBtN + j0 + e];
-                    if (a.yT)
-                        a.yT[(size_t)inst * kBtN + j0 + e] = y;
-                    bad = bad || !isfinite(y);
+                if (!fin && slot == CH) {
+                    chunk = sChunk[lane];
+                    slot = 0;
+                    if (chunk < 0) {
+                        status = ST_CKPT_BUDGET;
+                        fin = true;
+                    }
                 }
-                if (bad)
-                    atomicOr(&c.sBad[c.bl], 1);
-            } else {
-                if ((t + dt) - t1 > kDblEps)
-                    dt = t1 - t;
-                fails = 0;
-                at_top = false;
+                if (!fin) {
+                    double *rec = record_ptr<RS>(a.pool, chunk, slot);
+                    if (c.q == 0)
+                        *reinterpret_cast<double2 *>(rec) = make_double2(t, dt);
+                    S.rec[lane] = rec;
+                    mode |= kFwdTopRecord;
+                    slot++;
+                    if (slot == CH && !end && c.q == 0)
+                        alloc_chunk(chunk);
+                    fin = end;
+                }
+                if (fin) {
+                    mode = (mode | kFwdDone | kFwdFinished) & ~kFwdAtTop;
+                } else {
+                    if ((t + dt) - t1 > kDblEps)
+                        dt = t1 - t;
+                    S.fails[lane] = 0;
+                    mode &= ~kFwdAtTop;
+                }
+                S.dt[lane] = dt;
+                S.status[lane] = status;
+                S.chunk[lane] = chunk;
+                S.slot[lane] = slot;
             }
+            if (!(mode & kFwdDone)) {
+                mode |= kFwdAttempt;
+                const dword d(S.dt[lane]);
+                S.sdt[lane] = make_float2(d.hi, d.lo);
+            }
+            S.mode[lane] = mode;
+            // whether any instance of the tile attempts: this CTA's flag to all
+            // eight (read after the first stage's cluster barrier)
+            const int mine = __any_sync(0xffffffffu, (mode & kFwdAttempt) != 0);
+            if (lane < kBtCluster)
+                dsmem_st_s32(dsmem_addr(sAct + 4 * c.mt + c.q, (uint32_t)lane), mine);
         }
-        const bool attempt = !done;
-        // whether any instance of the tile attempts: each CTA's flag to all
-        // eight (read after the first stage's cluster barrier)
-        {
-            const int mine = __syncthreads_or(attempt ? 1 : 0);
-            if (c.t < kBtCluster)
-                dsmem_st_s32(dsmem_addr(sAct + rank, (uint32_t)c.t), mine);
+        __syncthreads();
+        const int mode = S.mode[c.bl];
+        const bool attempt = (mode & kFwdAttempt) != 0;
+        double *rec = S.rec[c.bl];
+        if (mode & kFwdTopRecord) {
+            double2 *x0 = reinterpret_cast<double2 *>(rec + 2 + j0);
+            double2 *zz = reinterpret_cast<double2 *>(rec + 2 + (size_t)NS * kBtN + j0);
+            x0[0] = make_double2(dw_pack(ys[0]), dw_pack(ys[1]));
+            x0[1] = make_double2(dw_pack(ys[2]), dw_pack(ys[3]));
+            zz[0] = make_double2(dw_pack(z0[0]), dw_pack(z0[1]));
+            zz[1] = make_double2(dw_pack(z0[2]), dw_pack(z0[3]));
         }
-        const dword sdt = dword(dt);
+        if (mode & kFwdFinished) {
+            // y(T) of this thread's components and their finiteness
+            const bool moved = S.count[c.bl] > 0;
+            bool bad = false;
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const double y = moved ? to_d(ys[e]) : a.y0[(size_t)inst * kBtN + j0 + e];
+                if (a.yT)
+                    a.yT[(size_t)inst * kBtN + j0 + e] = y;
+                bad = bad || !isfinite(y);
+            }
+            if (bad)
+                atomicOr(&c.sBad[c.bl], 1);
+        }
+        const dword sdt(S.sdt[c.bl].x, S.sdt[c.bl].y);
         bool stop = false;
         // stages 2 .. s: X_m = y + dt sum_{j<m} a_mj K_j, K_m = X_m (r + A X_m)
 #pragma unroll
@@ -915,67 +958,66 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
             if (dw_greater(other, rmax))
                 rmax = other;
         }
-        nanr = ((__ballot_sync(0xffffffffu, nanr) >> lead_lane) & 0xffffu) != 0;
-        if (lead) {
+        nanr = ((__ballot_sync(0xffffffffu, nanr) >> (lane & 16)) & 0xffffu) != 0;
+        if (c.jg == 0) {
+            // (a NaN stays NaN through the conversion)
             const double ep = nanr ? __longlong_as_double(0x7ff8000000000000ll) : to_d(rmax);
 #pragma unroll
             for (int k = 0; k < 4; k++)
                 dsmem_st_f64(dsmem_addr(sErr + c.q * 32 + c.bl, (uint32_t)(c.mt * 4 + k)), ep);
         }
         cluster_sync_all();
-        // the controller (odeint's try_step), run by the lead thread
-        int accepted = 0;
-        if (attempt && lead) {
-            double err = 0.0;
-            bool nan = false;
+        // the controller (odeint's try_step), warp 0
+        if (ctl) {
+            int md = S.mode[lane];
+            if (md & kFwdAttempt) {
+                double err = 0.0;
+                bool nan = false;
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const double x = sErr[32 * k + c.bl];
-                nan = nan || x != x;
-                err = fmax(err, x);
-            }
-            if (nan)
-                err = __longlong_as_double(0x7ff8000000000000ll);
-            if (err != err) {
-                status = ST_NONFINITE;
-                at_top = true;
-            } else {
-                bool ok;
-                if (err > 1.0) {
-                    dt = decrease_step<Tab, dword>(dt, err, a.step_pow, nullptr);
-                    rej++;
-                    ok = false;
-                } else {
-                    t = t + dt;
-                    dt = increase_step<Tab, dword>(dt, err, a.step_pow, nullptr);
-                    accepted = 1;
-                    ok = true;
+                for (int k = 0; k < 4; k++) {
+                    const double x = sErr[32 * k + lane];
+                    nan = nan || x != x;
+                    err = fmax(err, x);
                 }
-                if (fails >= a.max_fail) {
-                    status = ST_MAX_REJECTS;
-                    at_top = true;
+                double t = S.t[lane], dt = S.dt[lane];
+                int status = S.status[lane];
+                if (nan) {
+                    status = ST_NONFINITE;
+                    md |= kFwdAtTop;
                 } else {
-                    fails++;
-                    if (ok) {
-                        count++;
-                        at_top = true;
-                    } else if (!(dt > 0.0) || !isfinite(dt)) {
-                        status = ST_NONFINITE;
-                        at_top = true;
+                    bool ok;
+                    if (err > 1.0) {
+                        dt = decrease_step<Tab, dword>(dt, err, a.step_pow, nullptr);
+                        S.rej[lane]++;
+                        ok = false;
+                    } else {
+                        t = t + dt;
+                        dt = increase_step<Tab, dword>(dt, err, a.step_pow, nullptr);
+                        md |= kFwdAccepted;
+                        ok = true;
+                    }
+                    if (S.fails[lane] >= a.max_fail) {
+                        status = ST_MAX_REJECTS;
+                        md |= kFwdAtTop;
+                    } else {
+                        S.fails[lane]++;
+                        if (ok) {
+                            S.count[lane]++;
+                            md |= kFwdAtTop;
+                        } else if (!(dt > 0.0) || !isfinite(dt)) {
+                            status = ST_NONFINITE;
+                            md |= kFwdAtTop;
+                        }
                     }
                 }
+                S.t[lane] = t;
+                S.dt[lane] = dt;
+                S.status[lane] = status;
             }
+            S.mode[lane] = md & ~(kFwdAttempt | kFwdTopRecord | kFwdFinished);
         }
-        // the instance's 16 threads take the lead's result
-        t = __shfl_sync(0xffffffffu, t, lead_lane);
-        dt = __shfl_sync(0xffffffffu, dt, lead_lane);
-        status = __shfl_sync(0xffffffffu, status, lead_lane);
-        count = __shfl_sync(0xffffffffu, count, lead_lane);
-        rej = __shfl_sync(0xffffffffu, rej, lead_lane);
-        fails = __shfl_sync(0xffffffffu, fails, lead_lane);
-        at_top = __shfl_sync(0xffffffffu, at_top ? 1 : 0, lead_lane) != 0;
-        accepted = __shfl_sync(0xffffffffu, accepted, lead_lane);
-        if (accepted) {
+        __syncthreads();
+        if (S.mode[c.bl] & kFwdAccepted) {
 #pragma unroll
             for (int e = 0; e < 4; e++) {
                 ys[e] = yn[e];
@@ -983,22 +1025,27 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
                 z0[e] = zn[e];
             }
         }
+        __syncthreads(); // warp 0 clears the flag at the next top of step
+        if (ctl)
+            S.mode[lane] &= ~kFwdAccepted;
     }
     // counters and status of the tile's instances: y(T)'s finiteness from the
     // four quarter CTAs
     cluster_sync_all();
-    if (c.q == 0 && lead && inb) {
+    if (c.q == 0 && c.jg == 0 && inb) {
+        int status = S.status[c.bl];
         if (bt_bad(c) && status == ST_OK)
             status = ST_NONFINITE;
+        const int count = S.count[c.bl];
         a.inst_T[inst] = count;
-        a.inst_last[inst] = status == ST_OK ? chunk : -1;
+        a.inst_last[inst] = status == ST_OK ? S.chunk[c.bl] : -1;
         a.inst_status[inst] = status;
         if (a.inst_t1)
-            a.inst_t1[inst] = t1;
+            a.inst_t1[inst] = S.t1[c.bl];
         if (a.n_acc_out)
             a.n_acc_out[inst] = count;
         if (a.n_rej_out)
-            a.n_rej_out[inst] = rej;
+            a.n_rej_out[inst] = S.rej[c.bl];
         if (a.status_out)
             a.status_out[inst] = status;
     }
