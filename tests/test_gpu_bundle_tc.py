@@ -171,3 +171,27 @@ def test_tc_backward_repeatable(cuda):
     s.close()
     for k in ("dy0", "dp", "dA"):
         np.testing.assert_array_equal(outs[0][k], outs[1][k])
+
+
+def test_tc_forward_limits(cuda):
+    """A zero-length instance (y(T) = y_0, no step), an instance that reaches
+    max_steps, and ordinary ones share the tiles; counters, statuses and y(T)
+    match the FP32-pipe sweeps, the failed instance's gradients are NaN."""
+    B = 66
+    A, r, x0 = make(B, seed=9)
+    t1 = np.full(B, 10.0)
+    t1[0] = 0.0   # t0 = t1
+    t1[65] = 400.0
+    kw = dict(max_steps=80)
+    tc = run(A, r, x0, t1, "mixed_dw", 0, **kw)
+    pipe = run(A, r, x0, t1, "mixed_dw", -1, **kw)
+    assert tc["launch"]["fwd_block"] == 512 and tc["launch"]["bwd_block"] == 512
+    np.testing.assert_array_equal(tc["status"], pipe["status"])
+    np.testing.assert_array_equal(tc["n_acc"], pipe["n_acc"])
+    assert tc["status"][65] != 0 and tc["n_acc"][65] == 80, (tc["status"][65], tc["n_acc"][65])
+    assert tc["n_acc"][0] == 0 and tc["status"][0] == 0
+    np.testing.assert_array_equal(tc["yT"][0], x0[0])
+    ok = tc["status"] == 0
+    assert rel_y({"yT": tc["yT"][ok]}, {"yT": pipe["yT"][ok]}).max() <= 1e-12
+    assert rel_inst({k: tc[k][ok] for k in ("dy0", "dp")}, {k: pipe[k][ok] for k in ("dy0", "dp")}).max() <= 1e-11
+    assert np.isnan(tc["dy0"][65]).all()

@@ -877,6 +877,14 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel(Bu
         const double yT = ST ? to_d(dw_unpack(rec[2 + i])) : rec[2 + i];
         lam[b] = a.cost == 0 ? 2.0 * yT : a.cost == 1 ? 1.0 : a.lambdaT[(size_t)inst[b] * NT + i];
         j[b] = T[b] - 1;
+        if (j[b] < 0) {
+            // no accepted step (t0 = t1): the seeds are the result
+            a.dy0[(size_t)inst[b] * NT + i] = lam[b];
+            const double d = a.mu_direct ? a.mu_direct[(size_t)inst[b] * NT + i] : 0.0;
+            a.dpar[(size_t)inst[b] * NT + i] = d;
+            if (a.status_out && i == 0)
+                a.status_out[inst[b]] = ST_OK;
+        }
     }
     // this CTA's partial of dA, transposed: part[jj][i] += dA_i,jj
     double *part = bp.dA_part + (size_t)blockIdx.x * NT * NT;
