@@ -70,9 +70,9 @@ DW_FP32_FLOPS = {
 }
 
 # Models whose backward phase is more than one kernel: the shared-matrix
-# backward sweep is followed by the dA contraction (ncu launch list: forward
-# 52%, backward sweep 40%, contraction 8%), so the forward sweep is the
-# single dominant kernel whatever the phase times say.
+# backward sweep is followed by the dA contraction (ncu launch list, cluster
+# sweeps: forward 46%, backward sweep 40%, contraction 13.5%), so the forward
+# sweep is the single dominant kernel whatever the phase times say.
 DOMINANT = {"glv_shared": "forward"}
 
 
@@ -295,7 +295,9 @@ def gemm_tflops(torch, dtype, n):
 # shared-matrix GLV), the backwards read them back.
 DW_TRAFFIC = {("vdpb", "forward"): 121.0e6 + 5557.4e6, ("vdpb", "backward"): 5655.6e6 + 20.8e6,
               ("dho", "forward"): 9.2e6 + 1586.3e6, ("glv10", "backward"): 745.5e6 + 4.3e6,
-              ("vdp1", "forward"): 0.05e6, ("glv256", "forward"): 12.6e6 + 1179.1e6}
+              ("vdp1", "forward"): 0.05e6, ("glv256", "forward"): 12.6e6 + 1179.1e6,
+              # the tensor-core cluster sweeps of GLV-256 (1,024 instances)
+              ("glv256", "tc_forward"): 10.1e6 + 1179.9e6, ("glv256", "tc_backward"): 1238.6e6 + 590.9e6}
 
 
 def measured_bf16_peak():

@@ -156,12 +156,13 @@ typedef struct {
                             inverse root (a few ulps off, ~25% cheaper per attempt).
                             The reduced precisions keep their own controllers     */
     int32_t tensor_products; /* shared-matrix GLV, N = 256, mixed_dw, every step
-                            checkpointed with stage records, DOPRI5 / CK54: 0
-                            (default) -- the backward sweep's stage products
-                            A^T v run on the tensor cores (clusters of 8 CTAs
-                            carry 64 instances in lockstep; error-free digit
-                            split), where the GPU can schedule such clusters;
-                            -1 -- double-word dot products on the FP32 pipe  */
+                            checkpointed with stage records: 0 (default) -- the
+                            sweeps' stage products run on the tensor cores
+                            (clusters of 8 CTAs carry 64 instances in lockstep;
+                            error-free digit split): the backward's A^T v for
+                            DOPRI5 and CK54, the forward's A X for DOPRI5, where
+                            the GPU can schedule such clusters; -1 -- double-word
+                            dot products on the FP32 pipe                      */
     int32_t reserved[2];
 } va_options;
 
