@@ -52,6 +52,7 @@
 
 #include "va_bundle.cuh"
 #include "va_contract.cuh"
+#include "va_kernels_dw.cuh"
 #include "va_tc_matvec.cuh"
 #include "va_tcgen05.cuh"
 
@@ -864,12 +865,19 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
 #pragma unroll
             for (int e = 0; e < 4; e++) {
                 if (attempt) {
-                    dword acc(0.0f, 0.0f);
+                    // compensated sum of the tableau row, then y + dt s
+                    dacc acc{0.0f, 0.0f};
+                    bool first = true;
 #pragma unroll
                     for (int j = 0; j < NS - 1; j++)
-                        if (j < m)
-                            acc = madd(dword(Tab::a(m, j)), K[j][e], acc);
-                    X[e] = madd(acc, sdt, ys[e]);
+                        if (j < m && Tab::a(m, j) != 0.0) {
+                            if (first)
+                                acc = dacc_mul_k(Tab::a(m, j), K[j][e]);
+                            else
+                                dacc_fma_k(acc, Tab::a(m, j), K[j][e]);
+                            first = false;
+                        }
+                    X[e] = axpy_dw(ys[e], sdt, acc);
                 } else {
                     X[e] = dword(0.0f, 0.0f);
                 }
@@ -909,12 +917,18 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
 #pragma unroll
         for (int e = 0; e < 4; e++) {
             if (attempt) {
-                dword acc(0.0f, 0.0f);
+                dacc acc{0.0f, 0.0f};
+                bool first = true;
 #pragma unroll
                 for (int j = 0; j < NS; j++)
-                    if (Tab::b(j) != 0.0)
-                        acc = madd(dword(Tab::b(j)), K[j][e], acc);
-                yn[e] = madd(acc, sdt, ys[e]);
+                    if (Tab::b(j) != 0.0) {
+                        if (first)
+                            acc = dacc_mul_k(Tab::b(j), K[j][e]);
+                        else
+                            dacc_fma_k(acc, Tab::b(j), K[j][e]);
+                        first = false;
+                    }
+                yn[e] = axpy_dw(ys[e], sdt, acc);
             } else {
                 yn[e] = dword(0.0f, 0.0f);
             }
@@ -938,14 +952,14 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
         if (attempt) {
 #pragma unroll
             for (int e = 0; e < 4; e++) {
-                dword acc(0.0f, 0.0f);
+                dacc acc{0.0f, 0.0f};
 #pragma unroll
                 for (int j = 0; j < NS; j++)
                     if (Tab::e(j) != 0.0)
-                        acc = madd(dword(Tab::e(j)), K[j][e], acc);
-                acc = madd(dword(Tab::E_NEW), kn[e], acc);
+                        dacc_fma_k(acc, Tab::e(j), K[j][e]);
+                dacc_fma_k(acc, Tab::E_NEW, kn[e]);
                 const dword tol = datol + drtol * (dabs(ys[e]) + dabs(sdt) * dabs(K[0][e]));
-                const dword ratio = dabs(acc * sdt) / tol;
+                const dword ratio = dabs(dacc_get(acc) * sdt) / tol;
                 if (ratio.hi != ratio.hi)
                     nanr = true;
                 else if (dw_greater(ratio, rmax))
