@@ -195,3 +195,36 @@ def test_tc_forward_limits(cuda):
     assert rel_y({"yT": tc["yT"][ok]}, {"yT": pipe["yT"][ok]}).max() <= 1e-12
     assert rel_inst({k: tc[k][ok] for k in ("dy0", "dp")}, {k: pipe[k][ok] for k in ("dy0", "dp")}).max() <= 1e-11
     assert np.isnan(tc["dy0"][65]).all()
+
+
+def test_tc_sweeps_with_tail(cuda):
+    """1,000 instances: 16 tiles, one more than the 15 clusters a GB300 holds
+    at once, so the last tile's 40 instances run in the double-word bundle
+    sweeps beside the clusters (a programmatic dependent launch).  Every
+    instance, tail included, against FP64; dA against FP64 and the FP32-pipe
+    sweeps; two gradients give the same bits."""
+    B = 1000
+    w = W.make("glv256", batch=B)
+    t1 = np.full(B, 10.0)
+    f64 = run(w["shared"], w["params"], w["y0"], t1, "fp64")
+    pipe = run(w["shared"], w["params"], w["y0"], t1, "mixed_dw", -1)
+    s = Solver("glv_shared", N, N, B, precision="mixed_dw", atol=1e-7, rtol=1e-7)
+    dA = torch.empty(N, N, dtype=torch.float64, device="cuda")
+    s.set_shared(dev(w["shared"]), dA)
+    outs = []
+    for _ in range(2):
+        o = s.gradient("sum", dev(w["y0"]), dev(w["params"]), dev(np.zeros(B)), dev(t1))
+        torch.cuda.synchronize()
+        outs.append({k: v.cpu().numpy().copy() for k, v in o.items()} | {"dA": dA.cpu().numpy().copy()})
+    assert s.launch()["fwd_block"] == 512 and s.launch()["bwd_block"] == 512
+    s.close()
+    tc = outs[0]
+    assert (tc["status"] == 0).all()
+    np.testing.assert_array_equal(tc["n_acc"], f64["n_acc"])
+    assert rel_y(tc, f64).max() <= 1e-12, rel_y(tc, f64).max()
+    assert rel_inst(tc, f64).max() <= 1e-11, rel_inst(tc, f64).max()
+    scale = np.abs(f64["dA"]).max()
+    assert np.abs(tc["dA"] - f64["dA"]).max() <= 1e-8 * scale
+    assert np.abs(tc["dA"] - pipe["dA"]).max() <= 1e-8 * scale
+    for k in ("yT", "dy0", "dp", "dA"):
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])

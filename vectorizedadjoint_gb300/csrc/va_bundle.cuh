@@ -47,6 +47,7 @@ struct BundleParams {
     const dword *Atw;
     double *dA_part;      // [gridDim.x][N][N], transposed per CTA: [j][i] += dA_ij
     int nb;               // instances per CTA (<= NB)
+    int inst0;            // the first CTA's first instance (a tail of the batch; 0: all of it)
     // deferred dA (double-word sweeps with stage records; null: the CTA
     // partials above): factor row k = k_base[b] + n nsv + m of step n, stage m
     // of instance b holds v = Kbar_m . X_m (packed double-words) and a pointer
@@ -363,7 +364,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
     // instances of this CTA
 #pragma unroll
     for (int b = 0; b < NB; b++) {
-        inst[b] = blockIdx.x * bp.nb + b;
+        inst[b] = bp.inst0 + blockIdx.x * bp.nb + b;
         active[b] = b < bp.nb && inst[b] < a.B;
         count[b] = rej[b] = fails[b] = 0;
         status[b] = ST_OK;
@@ -651,6 +652,9 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) forward_bundle_kernel(Bun
             __syncthreads();
         }
     }
+    // launched as the programmatic dependent of a cluster sweep over the
+    // batch's other instances: complete only after it (no-op otherwise)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 // ----------------------------------------------------------- backward sweep
@@ -847,7 +851,7 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel(Bu
     S r[NB];
 #pragma unroll
     for (int b = 0; b < NB; b++) {
-        inst[b] = blockIdx.x * bp.nb + b;
+        inst[b] = bp.inst0 + blockIdx.x * bp.nb + b;
         live[b] = b < bp.nb && inst[b] < a.B;
         T[b] = 0;
         j[b] = -1;
@@ -946,6 +950,9 @@ __global__ void __launch_bounds__(NT, NB <= 2 ? 2 : 0) backward_bundle_kernel(Bu
         }
         __syncthreads();
     }
+    // launched as the programmatic dependent of a cluster sweep over the
+    // batch's other instances: complete only after it (no-op otherwise)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 // dA = sum over CTAs of the transposed partials, in CTA order (FP64 sum of

@@ -3,6 +3,7 @@
 // 5(4) pairs, and the launch.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "va_bundle_tc.cuh"
@@ -65,15 +66,35 @@ const void *bt_kernel(int tableau)
 // the forward needs the FSAL pair (DOPRI5)
 const void *bt_fwd_kernel(int tableau) { return tableau == 0 ? (const void *)forward_bundle_tc_kernel<TabDopri5> : nullptr; }
 
+// the tail sweeps: double-word bundles of one instance per CTA
+const void *tail_fwd_kernel(int tableau)
+{
+    return tableau == 0 ? (const void *)forward_bundle_kernel<kBtN, 1, TabDopri5, dword, true> : nullptr;
+}
+const void *tail_bwd_kernel(int tableau)
+{
+    switch (tableau) {
+    case 0:
+        return (const void *)backward_bundle_kernel<kBtN, 1, TabDopri5, dword, true>;
+    case 1:
+        return (const void *)backward_bundle_kernel<kBtN, 1, TabCK54, dword, true>;
+    default:
+        return nullptr;
+    }
+}
+constexpr size_t kTailFwdSmem = bundle_fwd_smem_bytes<kBtN, 1, dword>();
+constexpr size_t kTailBwdSmem = 3 * sizeof(dword) * (size_t)TabDopri5::S * kBtN; // the stages of one instance
+
 // per device: the kernels' shared-memory attribute is set and a cluster of 8
-// CTAs of kBtSmem bytes fits on this GPU
+// CTAs of kBtSmem bytes fits on this GPU (clusters: how many at once)
 struct BtState {
     std::once_flag once;
     bool ok = false;
+    int clusters = 0;
 };
 BtState g_bt[64];
 
-bool bt_cluster_fits(const void *fn)
+int bt_cluster_fits(const void *fn)
 {
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBtSmem) != cudaSuccess)
         return false;
@@ -89,26 +110,73 @@ bool bt_cluster_fits(const void *fn)
     cfg.attrs = &attr;
     cfg.numAttrs = 1;
     int clusters = 0;
-    return cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) == cudaSuccess && clusters > 0;
+    return cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) == cudaSuccess ? clusters : 0;
 }
 
 void bt_setup(int dev)
 {
-    bool ok = true;
-    for (int tb = 0; tb < 2 && ok; tb++)
-        ok = bt_cluster_fits(bt_kernel(tb));
-    ok = ok && bt_cluster_fits(bt_fwd_kernel(0));
+    int clusters = 1 << 30;
+    for (int tb = 0; tb < 2; tb++)
+        clusters = std::min(clusters, bt_cluster_fits(bt_kernel(tb)));
+    clusters = std::min(clusters, bt_cluster_fits(bt_fwd_kernel(0)));
+    bool ok = clusters > 0;
+    for (int tb = 0; tb < 2 && ok; tb++) {
+        ok = cudaFuncSetAttribute(tail_bwd_kernel(tb), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kTailBwdSmem) == cudaSuccess;
+    }
+    ok = ok && cudaFuncSetAttribute(tail_fwd_kernel(0), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kTailFwdSmem) == cudaSuccess;
     (void)cudaGetLastError(); // a refused attribute or query leaves no sticky error
     g_bt[dev].ok = ok;
+    g_bt[dev].clusters = ok ? clusters : 0;
 }
 
-bool bt_ready()
+BtState *bt_state()
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
-        return false;
+        return nullptr;
     std::call_once(g_bt[dev].once, bt_setup, dev);
-    return g_bt[dev].ok;
+    return &g_bt[dev];
+}
+bool bt_ready()
+{
+    const BtState *st = bt_state();
+    return st && st->ok;
+}
+
+// tiles of the cluster sweep and the instances [tail0, B) left to the tail
+struct BtSplit {
+    int tiles, tail0;
+};
+BtSplit bt_split(int B)
+{
+    const BtState *st = bt_state();
+    const int tiles = (B + kBtTile - 1) / kBtTile;
+    const int c = st ? st->clusters : 0;
+    if (c > 0 && tiles > c && tiles % c == 1)
+        return {tiles - 1, (tiles - 1) * kBtTile};
+    return {tiles, B};
+}
+
+// the tail sweep over instances [tail0, B): one CTA per instance, started
+// once the cluster sweep before it in the stream has all its CTAs resident
+cudaError_t launch_tail(const void *fn, BundleParams bp, int B, int tail0, size_t smem, cudaStream_t s)
+{
+    bp.inst0 = tail0;
+    bp.nb = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(B - tail0));
+    cfg.blockDim = dim3(kBtN);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    void *args[] = {&bp};
+    return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 } // namespace
@@ -130,9 +198,12 @@ cudaError_t enqueue_bundle_tc_forward(const BundleParams &bp, const double *A, u
     p.rpk = rpk;
     p.aexp = aexp;
     p.error = error;
-    const int tiles = (bp.f.B + kBtTile - 1) / kBtTile;
+    const BtSplit sp = bt_split(bp.f.B);
     void *args[] = {&p};
-    return cudaLaunchKernel(fn, dim3(tiles * kBtCluster), dim3(kBtThreads), args, kBtSmem, s);
+    cudaError_t e = cudaLaunchKernel(fn, dim3(sp.tiles * kBtCluster), dim3(kBtThreads), args, kBtSmem, s);
+    if (e == cudaSuccess && sp.tail0 < bp.f.B)
+        e = launch_tail(tail_fwd_kernel(tableau), bp, bp.f.B, sp.tail0, kTailFwdSmem, s);
+    return e;
 }
 
 cudaError_t enqueue_bundle_tc_backward(const BundleParams &bp, const double *A, uint8_t *adig, int *aexp,
@@ -149,9 +220,12 @@ cudaError_t enqueue_bundle_tc_backward(const BundleParams &bp, const double *A, 
     p.rpk = rpk;
     p.aexp = aexp;
     p.error = error;
-    const int tiles = (bp.g.B + kBtTile - 1) / kBtTile;
+    const BtSplit sp = bt_split(bp.g.B);
     void *args[] = {&p};
-    return cudaLaunchKernel(fn, dim3(tiles * kBtCluster), dim3(kBtThreads), args, kBtSmem, s);
+    cudaError_t e = cudaLaunchKernel(fn, dim3(sp.tiles * kBtCluster), dim3(kBtThreads), args, kBtSmem, s);
+    if (e == cudaSuccess && sp.tail0 < bp.g.B)
+        e = launch_tail(tail_bwd_kernel(tableau), bp, bp.g.B, sp.tail0, kTailBwdSmem, s);
+    return e;
 }
 
 } // namespace va

@@ -454,6 +454,8 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
     extern __shared__ __align__(1024) uint8_t smem[];
     BtCta c;
     bt_begin(c, smem, p.adig, p.aexp);
+    // every CTA is resident: a dependent tail sweep may start on the idle SMs
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     int *sMaxT = reinterpret_cast<int *>(c.misc);
     const int CH = a.pool.chunk_len;
 
@@ -692,6 +694,8 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
     extern __shared__ __align__(1024) uint8_t smem[];
     BtCta c;
     bt_begin(c, smem, p.adig, p.aexp);
+    // every CTA is resident: a dependent tail sweep may start on the idle SMs
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     double *sErr = reinterpret_cast<double *>(c.misc);    // [4 quarters][32 instances] error-ratio maxima
     int *sChunk = reinterpret_cast<int *>(c.misc + 1024); // [32] next checkpoint chunk
     int *sAct = sChunk + 32;                              // [8] CTAs with an attempt this iteration
@@ -1070,7 +1074,12 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
 // Host side (va_bundle_tc.cu): whether the cluster sweeps can run for the
 // tableau on this GPU (set up once, before any capture), and their launches:
 // digit planes of A (forward) or A^T (backward) and r as double-words, then
-// one cluster of 8 CTAs per tile of 64 instances.
+// one cluster of 8 CTAs per tile of 64 instances.  When the tiles exceed
+// the clusters the GPU holds at once by exactly one, the last tile's
+// instances run instead in the double-word bundle sweeps (one instance per
+// CTA) on the SMs the clusters leave idle, launched as a programmatic
+// dependent of the cluster sweep (they start once its clusters are resident
+// and complete after it).
 bool bundle_tc_available(int tableau);
 bool bundle_tc_forward_available(int tableau);
 cudaError_t enqueue_bundle_tc_forward(const BundleParams &bp, const double *A, uint8_t *adig, int *aexp,
