@@ -331,16 +331,29 @@ def pipe_rates():
     return out
 
 
-def cluster_mma_flops(attempts_per_instance, forward):
+def cluster_mma_flops(attempts_per_instance, forward, n_tiles):
     """bf16 tensor FLOPs the cluster sweeps of the shared-matrix GLV execute
     (csrc/va_bundle_tc.cuh): per tile of 64 instances, per product, 8 CTAs x
     108 MMAs of M 128, N 64, K 16.  Forward: f(y_0), then 6 products (5
     stages and f(y_new)) per attempt of the tile's longest instance; backward:
-    6 per accepted step of the tile's longest instance."""
+    6 per accepted step of the tile's longest instance.  The first n_tiles
+    tiles (instances past them run in the double-word bundles beside)."""
     per_product = 8 * 108 * 2 * 128 * 64 * 16
-    a = np.asarray(attempts_per_instance, dtype=np.int64)
+    a = np.asarray(attempts_per_instance, dtype=np.int64)[:64 * n_tiles]
     tiles = [int(a[i:i + 64].max()) for i in range(0, len(a), 64)]
     return per_product * sum((1 + 6 * m) if forward else 6 * m for m in tiles)
+
+
+def glv_shared_launches(launch, B):
+    """Kernels per shared-matrix gradient: prepare A, forward, factor offsets,
+    backward, dA contraction and partial sum; each tensor-core cluster sweep
+    adds the digit planes of A and the packed r, and its tail sweep when the
+    clusters leave instances over."""
+    n = 6
+    for blk, grid in (("fwd_block", "fwd_grid"), ("bwd_block", "bwd_grid")):
+        if launch[blk] == 512:
+            n += 2 + (launch[grid] // 8 * 64 < B)
+    return n
 
 
 def roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted, launch=None, per_inst=None):
@@ -362,13 +375,15 @@ def roofline_of(args, c, torch, fms, bms, fl_f, fl_b, attempts, accepted, launch
            "fp64_equivalent": {"achieved": equiv, "dgemm_peak": peak64, "ratio": equiv / peak64}}
     cluster = (launch or {}).get("fwd_block" if fwd_dom else "bwd_block") == 512 and c["model"] == "glv_shared"
     if args.precision == "mixed_dw" and cluster and per_inst is not None:
-        fl = cluster_mma_flops(per_inst[0] if fwd_dom else per_inst[1], fwd_dom)
+        n_tiles = launch["fwd_grid" if fwd_dom else "bwd_grid"] // 8
+        fl = cluster_mma_flops(per_inst[0] if fwd_dom else per_inst[1], fwd_dom, n_tiles)
         peak, src = measured_bf16_peak()
         out.update(kernel=kernel + " (tensor-core cluster sweep)", bound="tensor", achieved=fl / (ms * 1e-3) / 1e12,
                    peak=peak, peak_source=src, flops_per_launch=fl,
                    traffic=DW_TRAFFIC.get((args.config, "tc_" + kernel)),
                    flop_count="bf16 MMA FLOPs executed (8 CTAs x 108 MMAs of 128x64x16 per product and tile; "
-                              "per tile the longest instance's attempts)")
+                              "per tile the longest instance's attempts; instances past the cluster tiles run "
+                              "beside them in double-word bundles and are not counted)")
         out["frac"] = out["achieved"] / out["peak"]
         return out
     dgemm = "cuBLAS DGEMM 4096^3 measured in this run (FP64 is absent from the measured-peaks file)"
@@ -655,8 +670,7 @@ def _bench(args, rank, world, local, torch, dist):
             # backward; shared-matrix bundles: prepare + forward + factor offsets +
             # backward + dA contraction + partial sum, and each tensor-core
             # cluster sweep its digit planes of A and packed r
-            "gpu_launches": (6 + 2 * (s.launch()["fwd_block"] == 512) + 2 * (s.launch()["bwd_block"] == 512)
-                             if c["model"] == "glv_shared" else 8) * args.steps,
+            "gpu_launches": (glv_shared_launches(s.launch(), B) if c["model"] == "glv_shared" else 8) * args.steps,
             "roofline": roofline,
             "fp64_batched": fp64_value,
             "modes": modes,

@@ -579,7 +579,8 @@ va_status enqueue_forward(va_handle *h, const double *y0, const double *params, 
             VA_CUDA(h, cudaMemsetAsync(h->bt_ferr, 0, sizeof(unsigned), s));
             VA_CUDA(h, va::enqueue_bundle_tc_forward(bp, h->shared_A, h->bt_adig_f, h->bt_aexp_f, h->bt_rpk, h->bt_ferr,
                                                      h->opt.tableau, s));
-            h->fwd_grid = (a.B + va::kBtTile - 1) / va::kBtTile * va::kBtCluster;
+            // CTAs of the cluster sweep (instances past its tiles: the tail)
+            h->fwd_grid = va::bundle_tc_tiles(a.B) * va::kBtCluster;
             h->fwd_block = va::kBtThreads;
             return VA_OK;
         }
@@ -689,7 +690,7 @@ va_status enqueue_backward(va_handle *h, const double *params, const double *lam
             // clusters of 8 CTAs, 64 instances each, stage products on the tensor cores
             VA_CUDA(h, va::enqueue_bundle_tc_backward(bp, h->shared_A, h->bt_adig, h->bt_aexp, h->bt_rpk, h->c_err,
                                                       h->opt.tableau, s));
-            h->bwd_grid = (a.B + va::kBtTile - 1) / va::kBtTile * va::kBtCluster;
+            h->bwd_grid = va::bundle_tc_tiles(a.B) * va::kBtCluster;
             h->bwd_block = va::kBtThreads;
         } else {
             VA_CUDA(h, cudaLaunchKernel(bundle_bwd(h), dim3(grid), dim3(h->N), args, bundle_smem_bwd(h), s));

@@ -182,6 +182,7 @@ cudaError_t launch_tail(const void *fn, BundleParams bp, int B, int tail0, size_
 } // namespace
 
 bool bundle_tc_available(int tableau) { return bt_kernel(tableau) && bt_ready(); }
+int bundle_tc_tiles(int B) { return bt_split(B).tiles; }
 bool bundle_tc_forward_available(int tableau) { return bt_fwd_kernel(tableau) && bt_ready(); }
 
 cudaError_t enqueue_bundle_tc_forward(const BundleParams &bp, const double *A, uint8_t *adig, int *aexp,

@@ -1082,6 +1082,8 @@ __global__ void __cluster_dims__(kBtCluster, 1, 1) __launch_bounds__(kBtThreads,
 // and complete after it).
 bool bundle_tc_available(int tableau);
 bool bundle_tc_forward_available(int tableau);
+// tiles of B instances that the cluster sweeps run (the rest: the tail)
+int bundle_tc_tiles(int B);
 cudaError_t enqueue_bundle_tc_forward(const BundleParams &bp, const double *A, uint8_t *adig, int *aexp,
                                       double *rpk, unsigned *error, int tableau, cudaStream_t s);
 cudaError_t enqueue_bundle_tc_backward(const BundleParams &bp, const double *A, uint8_t *adig, int *aexp,
