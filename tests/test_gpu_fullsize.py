@@ -96,14 +96,23 @@ def test_glv256_full_batch(oracle, cuda):
     """GLV N=256 with the shared A, 1,024 instances, double-word: per-instance
     results independent of the batch order, the whole batch's dA the sum of
     its halves' dA, and two instances (the longest among them) within 1e-6
-    of the oracle's FP64 gradient (dy0, dr)."""
+    of the oracle's FP64 gradient (dy0, dr).  The tensor-core cluster sweeps
+    take 64 instances per cluster; where the GPU holds one cluster fewer than
+    the tiles (15 of 16 on a GB300) the last 64 positions of the batch run in
+    the FP32-pipe double-word bundles beside them: bit-identical results for
+    the instances that stay in the clusters in both orders, the double-word
+    level (1e-11) for the others."""
     w, r = full("glv256", "mixed_dw")
     c = w["cfg"]
     B, N = c["batch"], c["n"]
     assert (r["status"] == 0).all()
     _, rr = full("glv256", "mixed_dw", reverse=True)
-    for k in ("yT", "dy0", "dp", "n_acc"):
-        np.testing.assert_array_equal(rr[k], r[k], err_msg=k)
+    np.testing.assert_array_equal(rr["n_acc"], r["n_acc"])
+    mid = slice(64, B - 64)  # in the clusters in both orders
+    for k in ("yT", "dy0", "dp"):
+        np.testing.assert_array_equal(rr[k][mid], r[k][mid], err_msg=k)
+        d = np.abs(rr[k] - r[k]).max(axis=1) / np.abs(r[k]).max(axis=1)
+        assert d.max() <= 1e-11, (k, d.max())
     # dA comes from the tensor-core contraction, whose digits are relative to
     # each 64-row chunk of factor rows: another batch order or split puts other
     # rows in a chunk, so dA moves by its truncation (~1e-9), not by rounding
@@ -112,7 +121,9 @@ def test_glv256_full_batch(oracle, cuda):
     h = B // 2
     parts = [gradient(c, "mixed_dw", w["y0"][sl], w["params"][sl], w["t0"][sl], w["t1"][sl], w["shared"])
              for sl in (slice(0, h), slice(h, B))]
-    np.testing.assert_array_equal(np.concatenate([p["dy0"] for p in parts]), r["dy0"])
+    halves = np.concatenate([p["dy0"] for p in parts])
+    np.testing.assert_array_equal(halves[:B - 64], r["dy0"][:B - 64])
+    assert (np.abs(halves - r["dy0"]).max(axis=1) / np.abs(r["dy0"]).max(axis=1)).max() <= 1e-11
     assert np.abs(parts[0]["dA"] + parts[1]["dA"] - r["dA"]).max() <= 2e-8 * scale
     pb = oracle.problem("glv", "dopri5", N, N + N * N, c["tol"], c["tol"])
     for b in (0, int(np.argmax(r["n_acc"]))):
