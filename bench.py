@@ -296,8 +296,9 @@ def gemm_tflops(torch, dtype, n):
 DW_TRAFFIC = {("vdpb", "forward"): 121.0e6 + 5557.4e6, ("vdpb", "backward"): 5655.6e6 + 20.8e6,
               ("dho", "forward"): 9.2e6 + 1586.3e6, ("glv10", "backward"): 745.5e6 + 4.3e6,
               ("vdp1", "forward"): 0.05e6, ("glv256", "forward"): 12.6e6 + 1179.1e6,
-              # the tensor-core cluster sweeps of GLV-256 (1,024 instances)
-              ("glv256", "tc_forward"): 10.1e6 + 1179.9e6, ("glv256", "tc_backward"): 1238.6e6 + 590.9e6}
+              # the tensor-core cluster sweeps of GLV-256 (1,024 instances: the
+              # 960 of the 15 cluster tiles; the other 64 run in the tail sweep)
+              ("glv256", "tc_forward"): 9.4e6 + 1105.0e6, ("glv256", "tc_backward"): 1161.9e6 + 550.5e6}
 
 
 def measured_bf16_peak():
