@@ -197,18 +197,19 @@ def test_tc_forward_limits(cuda):
     assert np.isnan(tc["dy0"][65]).all()
 
 
-def test_tc_sweeps_with_tail(cuda):
+@pytest.mark.parametrize("tableau", ["dopri5", "ck54"])
+def test_tc_sweeps_with_tail(cuda, tableau):
     """1,000 instances: 16 tiles, one more than the 15 clusters a GB300 holds
     at once, so the last tile's 40 instances run in the double-word bundle
-    sweeps beside the clusters (a programmatic dependent launch).  Every
-    instance, tail included, against FP64; dA against FP64 and the FP32-pipe
-    sweeps; two gradients give the same bits."""
+    sweeps beside the clusters (a programmatic dependent launch; CK54: the
+    backward only).  Every instance, tail included, against FP64; dA against
+    FP64 and the FP32-pipe sweeps; two gradients give the same bits."""
     B = 1000
     w = W.make("glv256", batch=B)
     t1 = np.full(B, 10.0)
-    f64 = run(w["shared"], w["params"], w["y0"], t1, "fp64")
-    pipe = run(w["shared"], w["params"], w["y0"], t1, "mixed_dw", -1)
-    s = Solver("glv_shared", N, N, B, precision="mixed_dw", atol=1e-7, rtol=1e-7)
+    f64 = run(w["shared"], w["params"], w["y0"], t1, "fp64", tableau=tableau)
+    pipe = run(w["shared"], w["params"], w["y0"], t1, "mixed_dw", -1, tableau=tableau)
+    s = Solver("glv_shared", N, N, B, tableau=tableau, precision="mixed_dw", atol=1e-7, rtol=1e-7)
     dA = torch.empty(N, N, dtype=torch.float64, device="cuda")
     s.set_shared(dev(w["shared"]), dA)
     outs = []
@@ -216,7 +217,7 @@ def test_tc_sweeps_with_tail(cuda):
         o = s.gradient("sum", dev(w["y0"]), dev(w["params"]), dev(np.zeros(B)), dev(t1))
         torch.cuda.synchronize()
         outs.append({k: v.cpu().numpy().copy() for k, v in o.items()} | {"dA": dA.cpu().numpy().copy()})
-    assert s.launch()["fwd_block"] == 512 and s.launch()["bwd_block"] == 512
+    assert s.launch()["fwd_block"] == (512 if tableau == "dopri5" else N) and s.launch()["bwd_block"] == 512
     s.close()
     tc = outs[0]
     assert (tc["status"] == 0).all()

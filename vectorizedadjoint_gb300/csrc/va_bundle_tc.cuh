@@ -1,5 +1,7 @@
-// Backward sweep of the shared-matrix GLV (N = 256, double-word stages with
-// stage records) with the stage products A^T v on the tensor cores.
+// Forward and backward sweeps of the shared-matrix GLV (N = 256, double-word
+// stages with stage records) with the stage products on the tensor cores:
+// z = A X in the forward (below, forward_bundle_tc_kernel), A^T v in the
+// backward.  The backward first:
 //
 // The bundle backward (va_bundle.cuh) forms g_m = Kbar_m . (r + z_m) + A^T v_m,
 // v_m = Kbar_m . X_m, for every stage of every step as double-word dot
@@ -31,7 +33,7 @@
 //        P_0 + P_1 + P_2 + P_3, and updates lambda, mu and the Kbar of the
 //        earlier stages.
 //   The operand A (6 digit planes of the CTA's 128 x 64 block, 96 KB) stays
-//   in shared memory for the whole sweep; only the 56 KB of V digits change
+//   in shared memory for the whole sweep; only the 57 KB of V digits change
 //   per stage.  No grid-wide barrier: the clusters are independent.
 //
 // Error-free splitting as in va_tc_matvec.cuh (Ozaki, Ogita, Oishi, Rump
