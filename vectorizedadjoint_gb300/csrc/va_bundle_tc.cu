@@ -66,24 +66,25 @@ const void *bt_kernel(int tableau)
 // the forward needs the FSAL pair (DOPRI5)
 const void *bt_fwd_kernel(int tableau) { return tableau == 0 ? (const void *)forward_bundle_tc_kernel<TabDopri5> : nullptr; }
 
-// the tail sweeps: double-word bundles of one instance per CTA
+// the tail sweeps: double-word bundles of kTailNB instances per CTA
+constexpr int kTailNB = 1;
 const void *tail_fwd_kernel(int tableau)
 {
-    return tableau == 0 ? (const void *)forward_bundle_kernel<kBtN, 1, TabDopri5, dword, true> : nullptr;
+    return tableau == 0 ? (const void *)forward_bundle_kernel<kBtN, kTailNB, TabDopri5, dword, true> : nullptr;
 }
 const void *tail_bwd_kernel(int tableau)
 {
     switch (tableau) {
     case 0:
-        return (const void *)backward_bundle_kernel<kBtN, 1, TabDopri5, dword, true>;
+        return (const void *)backward_bundle_kernel<kBtN, kTailNB, TabDopri5, dword, true>;
     case 1:
-        return (const void *)backward_bundle_kernel<kBtN, 1, TabCK54, dword, true>;
+        return (const void *)backward_bundle_kernel<kBtN, kTailNB, TabCK54, dword, true>;
     default:
         return nullptr;
     }
 }
-constexpr size_t kTailFwdSmem = bundle_fwd_smem_bytes<kBtN, 1, dword>();
-constexpr size_t kTailBwdSmem = 3 * sizeof(dword) * (size_t)TabDopri5::S * kBtN; // the stages of one instance
+constexpr size_t kTailFwdSmem = bundle_fwd_smem_bytes<kBtN, kTailNB, dword>();
+constexpr size_t kTailBwdSmem = 3 * sizeof(dword) * (size_t)TabDopri5::S * kBtN * kTailNB; // the bundle's stages
 
 // per device: the kernels' shared-memory attribute is set and a cluster of 8
 // CTAs of kBtSmem bytes fits on this GPU (clusters: how many at once)
@@ -164,9 +165,9 @@ BtSplit bt_split(int B)
 cudaError_t launch_tail(const void *fn, BundleParams bp, int B, int tail0, size_t smem, cudaStream_t s)
 {
     bp.inst0 = tail0;
-    bp.nb = 1;
+    bp.nb = kTailNB;
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3((unsigned)(B - tail0));
+    cfg.gridDim = dim3((unsigned)((B - tail0 + kTailNB - 1) / kTailNB));
     cfg.blockDim = dim3(kBtN);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
